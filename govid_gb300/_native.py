@@ -1,0 +1,98 @@
+"""Loader for the in-tree native library ``govid_gb300/_lib/libebivgpu.so``.
+
+The product path has no fallback: if the library is missing, importing the
+decoder raises.  Build it with ``python -m govid_gb300.build`` (or
+``__graft_entry__.build()``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libebivgpu.so"
+
+_lib = None
+
+
+class EncoderOptions(C.Structure):
+    _fields_ = [
+        ("width", C.c_int32), ("height", C.c_int32),
+        ("fps_num", C.c_uint32), ("fps_den", C.c_uint32),
+        ("tile_cols", C.c_int32), ("tile_rows", C.c_int32),
+        ("with_tiles_cols", C.c_int32), ("with_tiles_rows", C.c_int32),
+        ("coded", C.c_int32), ("qp", C.c_int32), ("gop", C.c_int32),
+        ("auto_tiles", C.c_int32), ("altref_window", C.c_int32),
+        ("fast_encode", C.c_int32), ("threads", C.c_int32),
+        ("search", C.c_int32), ("exhaustive_range", C.c_int32),
+        ("keep_recon", C.c_int32),
+    ]
+
+
+class Frame(C.Structure):
+    _fields_ = [
+        ("y", C.POINTER(C.c_uint8)), ("cb", C.POINTER(C.c_uint8)), ("cr", C.POINTER(C.c_uint8)),
+        ("y_stride", C.c_int32), ("c_stride", C.c_int32),
+        ("width", C.c_int32), ("height", C.c_int32),
+        ("timestamp_ns", C.c_int64), ("ring_slot", C.c_int32), ("keyframe", C.c_int32),
+    ]
+
+
+def _sig(lib, name, res, *args):
+    f = getattr(lib, name)
+    f.restype = res
+    f.argtypes = list(args)
+
+
+def lib() -> C.CDLL:
+    """Returns the loaded native library, raising if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: build the GB300 decoder first (python -m govid_gb300.build)")
+    L = C.CDLL(str(LIB_PATH))
+    P, S, I, I64, U8P = C.c_void_p, C.c_size_t, C.c_int, C.c_int64, C.POINTER(C.c_uint8)
+    PP = C.POINTER(C.c_void_p)
+    # decoder
+    _sig(L, "ebivgpu_create", I, I, PP)
+    _sig(L, "ebivgpu_decode", I, P, C.c_char_p, S, I64, C.POINTER(Frame))
+    _sig(L, "ebivgpu_flush", None, P)
+    _sig(L, "ebivgpu_destroy", None, P)
+    _sig(L, "ebivgpu_frame_rgba", I, P, I, U8P, S)
+    _sig(L, "ebivgpu_codec_launches", I64, P)
+    _sig(L, "ebivgpu_status_string", C.c_char_p, I)
+    _sig(L, "ebivgpu_device_available", I)
+    # encoder
+    _sig(L, "ebiv_encoder_default_options", None, C.POINTER(EncoderOptions))
+    _sig(L, "ebiv_encoder_create", I, C.POINTER(EncoderOptions), PP)
+    _sig(L, "ebiv_encoder_write_frame", I, P, C.c_char_p, S)
+    _sig(L, "ebiv_encoder_close", I, P)
+    _sig(L, "ebiv_encoder_output", I, P, C.POINTER(U8P), C.POINTER(S))
+    _sig(L, "ebiv_encoder_recon", I, P, I, U8P, S)
+    _sig(L, "ebiv_encoder_recon_count", I, P)
+    _sig(L, "ebiv_encoder_sad_evaluations", C.c_uint64, P)
+    _sig(L, "ebiv_encoder_set_candidates", I, P, C.POINTER(C.c_int16), I, I, I)
+    _sig(L, "ebiv_encoder_destroy", None, P)
+    # reader
+    _sig(L, "ebiv_reader_open", I, C.c_char_p, S, PP)
+    _sig(L, "ebiv_reader_info", I, P, C.POINTER(C.c_int64))
+    _sig(L, "ebiv_reader_next_packet", I, P, C.POINTER(U8P), C.POINTER(S), C.POINTER(I64), C.POINTER(I))
+    _sig(L, "ebiv_reader_packet", I, P, I, C.POINTER(U8P), C.POINTER(S), C.POINTER(I))
+    _sig(L, "ebiv_reader_seek", I, P, I64, C.POINTER(I64))
+    _sig(L, "ebiv_reader_duration", I64, P)
+    _sig(L, "ebiv_reader_frame_time", I64, P, I64)
+    _sig(L, "ebiv_reader_frame_index_at", I64, P, I64)
+    _sig(L, "ebiv_reader_close", I, P)
+    _sig(L, "ebiv_reader_destroy", None, P)
+    _sig(L, "ebiv_parse_frame_header", I, C.c_char_p, S, C.POINTER(C.c_int32))
+    # synthetic content
+    _sig(L, "ebiv_synth_frame", I, I, I, I, U8P, S)
+    _sig(L, "ebiv_synth_pan", I, I, I, I, U8P, S)
+    _sig(L, "ebiv_scene_create", I, C.POINTER(C.c_int64), PP)
+    _sig(L, "ebiv_scene_render", I, P, I, U8P, S)
+    _sig(L, "ebiv_scene_destroy", None, P)
+    _sig(L, "ebiv_encode_scene", I, C.POINTER(C.c_int64), I, C.POINTER(EncoderOptions), C.POINTER(U8P),
+         C.POINTER(S))
+    _sig(L, "ebiv_free", None, P)
+    _lib = L
+    return L

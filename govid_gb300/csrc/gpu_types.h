@@ -1,0 +1,74 @@
+// Device-side data layout of the GB300 EBIV decoder, shared by the kernels
+// and the host orchestration.
+//
+// HBM layout per stream:
+//   * three padded frame buffers (work / last-reference / golden), each the
+//     luma plane (mbCols*16 x mbRows*16) followed by Cb and Cr
+//     (mbCols*8 x mbRows*8), rows contiguous, stride = padded width;
+//   * per decode slot: the packet bytes, a FrameDesc, the resolved rANS
+//     tables, the tile ranges, one 48-byte MBRec per macroblock, a fixed
+//     408-word coefficient region per macroblock and the motion-vector grid.
+#pragma once
+
+#include <cstdint>
+
+#include "payload.h"
+
+namespace ebiv {
+
+// Per-macroblock output of the entropy stage.
+enum : uint8_t { kRecSkip = 0, kRecInter = 1, kRecIntra = 2, kRecNone = 0xFF };
+
+struct alignas(16) MBRec {
+  uint8_t mode;    // kRecSkip / kRecInter / kRecIntra / kRecNone
+  uint8_t ref;     // refLast / refGolden
+  uint8_t part;    // partition shape
+  uint8_t cbp;     // coded-block pattern (inter)
+  uint8_t tx;      // luma transform index
+  uint8_t cmode;   // chroma intra mode
+  uint8_t pad0, pad1;
+  int16_t mv[4][2];       // per-partition vectors, quarter pel
+  uint8_t lmode[16];      // luma intra mode per transform block (raster)
+  uint32_t nzmask;        // bit k: luma block k has coefficients; 16: Cb; 17: Cr
+  uint32_t wmask;         // bit k: luma block k written; 16: Cb; 17: Cr
+};
+static_assert(sizeof(MBRec) == 48, "MBRec layout");
+
+// Coefficient region per macroblock, in 32-bit words: each block has its
+// nonzero count followed by entries packing (row-major position in bits 0-7,
+// signed level in bits 8-31).  Luma block k of an n x n transform starts at
+// k*(n*n+1); Cb at kCoefCb, Cr at kCoefCr.
+constexpr int kCoefCb = 272;
+constexpr int kCoefCr = 337;
+constexpr int kCoefPerMB = 408;
+constexpr uint32_t kWriteAll = 0x3FFFFu;
+
+struct TileStat {
+  int32_t err;         // 0 or an ebiv status
+  int32_t intraCount;  // intra macroblocks decoded in this tile
+};
+
+struct FrameDesc {
+  // Planes (padded).  ref/gold may alias rec's siblings; never rec itself.
+  uint8_t* rec[3];
+  const uint8_t* ref[3];
+  const uint8_t* gold[3];
+  int32_t strideY, strideC;  // = padded widths
+  int32_t padW, padH, padCW, padCH;
+  int32_t mbCols, mbRows;
+  int32_t inter;
+  int32_t qdc, qac;
+  int32_t tileCount;
+  int32_t pad;
+  const uint8_t* pkt;
+  const DeviceTables* tables;
+  const TileRange* tiles;
+  MBRec* mbrec;
+  uint32_t* coef;
+  int16_t* mvgrid;
+  TileStat* tileStat;
+  int32_t* status;      // frame status, written by the commit step
+  const int32_t* gate;  // when set and nonzero, this job is skipped
+};
+
+}  // namespace ebiv

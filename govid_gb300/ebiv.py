@@ -1,0 +1,472 @@
+"""Host-side mirror of govid's EBIV plugin API over the GB300 decoder.
+
+The names, argument meaning and error behaviour follow the reference:
+
+* ``Codec`` is ``ebiv.Codec`` (``NewCodec(WithFrameRing(n))``,
+  ``Decode(Packet) (*Frame, error)``, ``Flush()``; ebiv/codec.go:48-117) —
+  decoding runs on the GPU through the C-ABI in ``include/ebivgpu.h``.
+* ``Reader`` is ``ebiv.Reader``, a ``govid.Demuxer`` (ebiv/reader.go).
+* ``Encoder`` is ``ebiv.Encoder`` with its functional options
+  (ebiv/encoder.go:50-148).
+* Errors are exception classes matching the ``ebiv`` sentinels
+  (ebiv/format.go:110-119); ``isinstance`` plays the role of ``errors.Is``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native
+
+# ---------------------------------------------------------------------------
+# Errors (ebiv/format.go:110-119)
+# ---------------------------------------------------------------------------
+
+
+class EbivError(Exception):
+    status = -1
+
+
+class ErrCorrupt(EbivError):
+    status = 1
+
+
+class ErrNoKeyframe(EbivError):
+    status = 2
+
+
+class ErrDimensions(EbivError):
+    status = 3
+
+
+class ErrUnsupported(EbivError):
+    status = 4
+
+
+class ErrVersion(EbivError):
+    status = 5
+
+
+class ErrBadMagic(EbivError):
+    status = 6
+
+
+class ErrConfig(EbivError):
+    status = 7
+
+
+class ErrWriterClosed(EbivError):
+    status = 8
+
+
+class EOF(EbivError):
+    status = 9
+
+
+class ErrDevice(EbivError):
+    status = 11
+
+
+class ErrArgument(EbivError):
+    status = 12
+
+
+_ERRORS = {c.status: c for c in (ErrCorrupt, ErrNoKeyframe, ErrDimensions, ErrUnsupported, ErrVersion,
+                                  ErrBadMagic, ErrConfig, ErrWriterClosed, EOF, ErrDevice, ErrArgument)}
+
+
+def _check(status: int, what: str = "") -> None:
+    if status == 0:
+        return
+    L = _native.lib()
+    msg = L.ebivgpu_status_string(status).decode()
+    raise _ERRORS.get(status, EbivError)(f"{what}: {msg}" if what else msg)
+
+
+# ---------------------------------------------------------------------------
+# Packets and frames (govid.go:9-22)
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class Packet:
+    data: bytes
+    timestamp_ns: int = 0
+    keyframe: bool = False
+
+
+@dataclass
+class Frame:
+    """A decoded 4:2:0 frame.  y/cb/cr are strided views into the codec's
+    ring, valid for ``ring`` further decodes (ebiv/codec.go:15-22)."""
+    y: np.ndarray
+    cb: np.ndarray
+    cr: np.ndarray
+    timestamp_ns: int
+    width: int
+    height: int
+    ring_slot: int = -1
+    keyframe: bool = False
+    _codec: "Codec | None" = field(default=None, repr=False)
+
+    def packed(self) -> bytes:
+        """Tightly packed Y, Cb, Cr planes (the on-disk raw layout)."""
+        cw, ch = (self.width + 1) // 2, (self.height + 1) // 2
+        return (np.ascontiguousarray(self.y[: self.height, : self.width]).tobytes()
+                + np.ascontiguousarray(self.cb[:ch, :cw]).tobytes()
+                + np.ascontiguousarray(self.cr[:ch, :cw]).tobytes())
+
+    def rgba(self) -> np.ndarray:
+        """RGBA (h, w, 4) computed on the GPU (frame.go:8-67, 127-135)."""
+        if self._codec is None:
+            raise ErrArgument("frame has no codec")
+        return self._codec.rgba(self)
+
+
+# ---------------------------------------------------------------------------
+# Codec (ebiv/codec.go)
+# ---------------------------------------------------------------------------
+
+
+class Codec:
+    """GPU EBIV decoder with the ebiv.Codec contract."""
+
+    def __init__(self, ring: int = 3):
+        L = _native.lib()
+        h = C.c_void_p()
+        _check(L.ebivgpu_create(int(ring), C.byref(h)), "NewCodec")
+        self._h = h
+        self._L = L
+
+    def decode(self, pkt: Packet | bytes) -> Frame:
+        data = pkt.data if isinstance(pkt, Packet) else bytes(pkt)
+        ts = pkt.timestamp_ns if isinstance(pkt, Packet) else 0
+        f = _native.Frame()
+        _check(self._L.ebivgpu_decode(self._h, data, len(data), ts, C.byref(f)))
+        w, h, ys, cs = f.width, f.height, f.y_stride, f.c_stride
+        ch = (h + 1) // 2
+        y = np.ctypeslib.as_array(f.y, shape=(h * ys,)).reshape(h, ys)
+        cb = np.ctypeslib.as_array(f.cb, shape=(ch * cs,)).reshape(ch, cs)
+        cr = np.ctypeslib.as_array(f.cr, shape=(ch * cs,)).reshape(ch, cs)
+        return Frame(y, cb, cr, f.timestamp_ns, w, h, f.ring_slot, bool(f.keyframe), self)
+
+    Decode = decode
+
+    def flush(self) -> None:
+        self._L.ebivgpu_flush(self._h)
+
+    Flush = flush
+
+    def rgba(self, frame: Frame) -> np.ndarray:
+        out = np.empty((frame.height, frame.width, 4), np.uint8)
+        _check(self._L.ebivgpu_frame_rgba(self._h, frame.ring_slot,
+                                          out.ctypes.data_as(C.POINTER(C.c_uint8)), out.nbytes))
+        return out
+
+    def launches(self) -> int:
+        return int(self._L.ebivgpu_codec_launches(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.ebivgpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def NewCodec(ring: int = 3) -> Codec:
+    return Codec(ring)
+
+
+def device_available() -> bool:
+    return bool(_native.lib().ebivgpu_device_available())
+
+
+# ---------------------------------------------------------------------------
+# Demuxer (ebiv/reader.go)
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class VideoInfo:
+    width: int
+    height: int
+    frame_rate: float
+
+
+@dataclass
+class IndexEntry:
+    size: int
+    keyframe: bool
+
+
+class Reader:
+    """In-memory EBIV demuxer (govid.Demuxer)."""
+
+    def __init__(self, data: bytes):
+        L = _native.lib()
+        h = C.c_void_p()
+        _check(L.ebiv_reader_open(data, len(data), C.byref(h)), "NewDemuxer")
+        self._h, self._L = h, L
+        info = (C.c_int64 * 8)()
+        L.ebiv_reader_info(h, info)
+        self.width, self.height = int(info[0]), int(info[1])
+        self.fps_num, self.fps_den = int(info[2]), int(info[3])
+        self.frame_count = int(info[4])
+        self.tile_cols, self.tile_rows = int(info[5]), int(info[6])
+        self.rebuilt_index = bool(info[7])
+
+    def next_packet(self) -> Packet:
+        d = C.POINTER(C.c_uint8)()
+        n, ts, k = C.c_size_t(), C.c_int64(), C.c_int()
+        _check(self._L.ebiv_reader_next_packet(self._h, C.byref(d), C.byref(n), C.byref(ts), C.byref(k)))
+        return Packet(C.string_at(d, n.value), ts.value, bool(k.value))
+
+    NextPacket = next_packet
+
+    def packet(self, i: int) -> Packet:
+        d = C.POINTER(C.c_uint8)()
+        n, k = C.c_size_t(), C.c_int()
+        _check(self._L.ebiv_reader_packet(self._h, int(i), C.byref(d), C.byref(n), C.byref(k)))
+        return Packet(C.string_at(d, n.value), self.frame_time(i), bool(k.value))
+
+    def packets(self) -> list[Packet]:
+        return [self.packet(i) for i in range(self.frame_count)]
+
+    def index(self) -> list[IndexEntry]:
+        out = []
+        for i in range(self.frame_count):
+            p = self.packet(i)
+            out.append(IndexEntry(len(p.data), p.keyframe))
+        return out
+
+    def seek(self, t_ns: int) -> int:
+        landed = C.c_int64()
+        _check(self._L.ebiv_reader_seek(self._h, int(t_ns), C.byref(landed)))
+        return landed.value
+
+    Seek = seek
+
+    def duration(self) -> int:
+        return int(self._L.ebiv_reader_duration(self._h))
+
+    def frame_time(self, i: int) -> int:
+        return int(self._L.ebiv_reader_frame_time(self._h, int(i)))
+
+    def frame_index_at(self, t_ns: int) -> int:
+        return int(self._L.ebiv_reader_frame_index_at(self._h, int(t_ns)))
+
+    def video_info(self) -> VideoInfo:
+        return VideoInfo(self.width, self.height, self.fps_num / self.fps_den)
+
+    def close(self) -> None:
+        self._L.ebiv_reader_close(self._h)
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._L.ebiv_reader_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def __iter__(self):
+        while True:
+            try:
+                yield self.next_packet()
+            except EOF:
+                return
+
+
+def NewDemuxer(data: bytes) -> Reader:
+    return Reader(data)
+
+
+def parse_frame_header(pkt: bytes) -> dict:
+    info = (C.c_int32 * 6)()
+    _check(_native.lib().ebiv_parse_frame_header(pkt, len(pkt), info))
+    return {"type": info[0], "coding": info[1], "width": info[2], "height": info[3],
+            "golden_override": bool(info[4]), "body_offset": info[5]}
+
+
+# ---------------------------------------------------------------------------
+# Encoder (ebiv/encoder.go)
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class Config:
+    width: int
+    height: int
+    fps_num: int = 30
+    fps_den: int = 1
+    tile_cols: int = 0
+    tile_rows: int = 0
+
+
+def packed_size(w: int, h: int) -> int:
+    return w * h + 2 * ((w + 1) // 2) * ((h + 1) // 2)
+
+
+class Encoder:
+    """EBIV encoder.  Options mirror WithIntra / WithGOP / WithTiles /
+    WithAutoTiles / WithAltRef / WithFastEncode."""
+
+    def __init__(self, cfg: Config, intra: int | None = None, gop: int = 1, tiles: tuple[int, int] | None = None,
+                 auto_tiles: int = 0, altref: int = 0, fast: bool = False, threads: int = 1,
+                 search: str = "diamond", exhaustive_range: int = 16, keep_recon: bool = False):
+        L = _native.lib()
+        o = _native.EncoderOptions()
+        L.ebiv_encoder_default_options(C.byref(o))
+        o.width, o.height = cfg.width, cfg.height
+        o.fps_num, o.fps_den = cfg.fps_num, cfg.fps_den
+        o.tile_cols, o.tile_rows = cfg.tile_cols, cfg.tile_rows
+        if tiles is not None:
+            o.with_tiles_cols, o.with_tiles_rows = tiles
+        if intra is not None:
+            o.coded, o.qp = 1, int(intra)
+        o.gop = int(gop)
+        o.auto_tiles = int(auto_tiles)
+        o.altref_window = int(altref)
+        o.fast_encode = int(bool(fast))
+        o.threads = int(threads)
+        o.search = {"diamond": 0, "exhaustive": 1, "proposed": 2}[search]
+        o.exhaustive_range = int(exhaustive_range)
+        o.keep_recon = int(bool(keep_recon))
+        h = C.c_void_p()
+        _check(L.ebiv_encoder_create(C.byref(o), C.byref(h)), "NewEncoder")
+        self._h, self._L, self.cfg = h, L, cfg
+
+    def write_frame(self, packed: bytes | np.ndarray) -> None:
+        b = packed.tobytes() if isinstance(packed, np.ndarray) else bytes(packed)
+        _check(self._L.ebiv_encoder_write_frame(self._h, b, len(b)), "WriteFrame")
+
+    WriteFrame = write_frame
+
+    def close(self) -> None:
+        _check(self._L.ebiv_encoder_close(self._h), "Close")
+
+    Close = close
+
+    def output(self) -> bytes:
+        d = C.POINTER(C.c_uint8)()
+        n = C.c_size_t()
+        self._L.ebiv_encoder_output(self._h, C.byref(d), C.byref(n))
+        return C.string_at(d, n.value)
+
+    def recons(self) -> list[bytes]:
+        n = self._L.ebiv_encoder_recon_count(self._h)
+        sz = packed_size(self.cfg.width, self.cfg.height)
+        buf = (C.c_uint8 * sz)()
+        out = []
+        for i in range(n):
+            _check(self._L.ebiv_encoder_recon(self._h, i, buf, sz))
+            out.append(bytes(buf))
+        return out
+
+    def sad_evaluations(self) -> int:
+        return int(self._L.ebiv_encoder_sad_evaluations(self._h))
+
+    def set_candidates(self, mv: np.ndarray) -> None:
+        """mv: int16 (frames, mbs, k, 2) quarter-pel candidates for search='proposed'."""
+        a = np.ascontiguousarray(mv, dtype=np.int16)
+        f, m, k, _ = a.shape
+        _check(self._L.ebiv_encoder_set_candidates(self._h, a.ctypes.data_as(C.POINTER(C.c_int16)), f, m, k))
+        self._cand = a
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._L.ebiv_encoder_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# Synthetic content
+# ---------------------------------------------------------------------------
+
+
+def synth_frame(w: int, h: int, seed: int) -> bytes:
+    """ebiv/harness_test.go:105-129 (gradient, diagonal edge, checker)."""
+    buf = (C.c_uint8 * packed_size(w, h))()
+    _check(_native.lib().ebiv_synth_frame(w, h, seed, buf, len(buf)))
+    return bytes(buf)
+
+
+def synth_pan(w: int, h: int, seed: int) -> bytes:
+    """ebiv/harness_test.go:134-171 (texture panned 2 px/frame)."""
+    buf = (C.c_uint8 * packed_size(w, h))()
+    _check(_native.lib().ebiv_synth_pan(w, h, seed, buf, len(buf)))
+    return bytes(buf)
+
+
+@dataclass
+class SceneSpec:
+    width: int = 640
+    height: int = 360
+    seed: int = 1
+    sprites: int = 6
+    vel_max_q: int = 16
+    integer_vel: bool = True
+    pan_max_q: int = 0
+    flash_period: int = 0
+    flash_start: int = 30
+    flash_len: int = 3
+    flash_amp: int = 40
+    noise_y16: int = 32
+    noise_c16: int = 16
+
+    def as_array(self):
+        v = [self.width, self.height, self.seed, self.sprites, self.vel_max_q, int(self.integer_vel),
+             self.pan_max_q, self.flash_period, self.flash_start, self.flash_len, self.flash_amp,
+             self.noise_y16, self.noise_c16]
+        return (C.c_int64 * 13)(*v)
+
+
+class Scene:
+    def __init__(self, spec: SceneSpec):
+        h = C.c_void_p()
+        _check(_native.lib().ebiv_scene_create(spec.as_array(), C.byref(h)))
+        self._h, self.spec = h, spec
+
+    def render(self, i: int) -> bytes:
+        buf = (C.c_uint8 * packed_size(self.spec.width, self.spec.height))()
+        _check(_native.lib().ebiv_scene_render(self._h, int(i), buf, len(buf)))
+        return bytes(buf)
+
+    def __del__(self):
+        try:
+            if self._h:
+                _native.lib().ebiv_scene_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+def encode_scene(spec: SceneSpec, frames: int, qp: int, gop: int, tiles: tuple[int, int], fast: bool = False,
+                 threads: int = 1, altref: int = 0) -> bytes:
+    """Renders and encodes a sprite scene in one native call."""
+    L = _native.lib()
+    o = _native.EncoderOptions()
+    L.ebiv_encoder_default_options(C.byref(o))
+    o.width, o.height = spec.width, spec.height
+    o.coded, o.qp, o.gop = 1, qp, gop
+    o.with_tiles_cols, o.with_tiles_rows = tiles
+    o.fast_encode = int(fast)
+    o.threads = threads
+    o.altref_window = altref
+    d = C.POINTER(C.c_uint8)()
+    n = C.c_size_t()
+    _check(L.ebiv_encode_scene(spec.as_array(), int(frames), C.byref(o), C.byref(d), C.byref(n)), "encode")
+    try:
+        return C.string_at(d, n.value)
+    finally:
+        L.ebiv_free(d)

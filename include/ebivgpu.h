@@ -1,0 +1,83 @@
+/*
+ * ebivgpu — GB300 (sm_103a) EBIV decoder, C-ABI drop-in boundary.
+ *
+ * These entry points are what a cgo binding of govid's Codec contract calls
+ * (see INTEGRATION.md for the Go side).  Plain pointers and sizes only; no
+ * exceptions cross the boundary; every call returns an ebiv status code.
+ *
+ * Reference interfaces replaced (govid, paths relative to its root):
+ *   ebivgpu_create   <- ebiv.NewCodec(WithFrameRing(n))  ebiv/codec.go:48-64
+ *   ebivgpu_decode   <- (*ebiv.Codec).Decode(govid.Packet) ebiv/codec.go:70-111
+ *                       via govid.Codec.Decode             govid.go:41-44
+ *   ebivgpu_flush    <- (*ebiv.Codec).Flush()              ebiv/codec.go:115-117
+ *   ebivgpu_destroy  <- (garbage collection of the Codec)
+ *   ebivgpu_frame_rgba <- govid.Frame.ConvertRGBA / RGBA   frame.go:72-91
+ *   ebivgpu_batch_*  <- many independent Codec.Decode call chains at once
+ *                       (no single reference counterpart; the reference runs
+ *                       one Codec per stream)
+ */
+#ifndef EBIVGPU_H
+#define EBIVGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes: one per ebiv error sentinel (ebiv/format.go:110-119), plus
+ * the boundary's own. */
+enum {
+  EBIV_OK = 0,
+  EBIV_ERR_CORRUPT = 1,      /* ebiv.ErrCorrupt */
+  EBIV_ERR_NOKEYFRAME = 2,   /* ebiv.ErrNoKeyframe */
+  EBIV_ERR_DIMENSIONS = 3,   /* ebiv.ErrDimensions */
+  EBIV_ERR_UNSUPPORTED = 4,  /* ebiv.ErrUnsupported */
+  EBIV_ERR_VERSION = 5,      /* ebiv.ErrVersion */
+  EBIV_ERR_BADMAGIC = 6,     /* ebiv.ErrBadMagic */
+  EBIV_ERR_CONFIG = 7,       /* ebiv.ErrConfig */
+  EBIV_ERR_WRITER_CLOSED = 8,/* ebiv.ErrWriterClosed */
+  EBIV_ERR_EOF = 9,          /* io.EOF from a demuxer */
+  EBIV_ERR_IO = 10,
+  EBIV_ERR_DEVICE = 11,      /* CUDA failure or no usable GPU */
+  EBIV_ERR_ARG = 12          /* invalid argument at the boundary */
+};
+
+typedef struct ebivgpu_codec ebivgpu_codec;
+
+/* A decoded frame: host-visible 4:2:0 planes owned by the codec's ring
+ * (valid for `ring` further decodes, as in ebiv/codec.go:15-22), strides
+ * aligned to 64 bytes (ebiv/geometry.go:22-49). */
+typedef struct {
+  const uint8_t* y;
+  const uint8_t* cb;
+  const uint8_t* cr;
+  int32_t y_stride, c_stride;
+  int32_t width, height;
+  int64_t timestamp_ns;
+  int32_t ring_slot;
+  int32_t keyframe;
+} ebivgpu_frame;
+
+/* Creates a codec on the current CUDA device; ring >= 2 (else 3). */
+int ebivgpu_create(int ring, ebivgpu_codec** out);
+/* Decodes one packet.  The packet bytes are consumed before return, so the
+ * caller may reuse them (govid.Packet.Data aliases a reused buffer,
+ * ebiv/reader.go:186-188). */
+int ebivgpu_decode(ebivgpu_codec* c, const uint8_t* pkt, size_t n, int64_t ts_ns, ebivgpu_frame* out);
+void ebivgpu_flush(ebivgpu_codec* c);
+void ebivgpu_destroy(ebivgpu_codec* c);
+/* YCbCr -> RGBA (BT.601 fixed point, frame.go:8-67) of the frame in ring
+ * slot `slot`, computed on the GPU; dst holds width*height*4 bytes. */
+int ebivgpu_frame_rgba(ebivgpu_codec* c, int slot, uint8_t* dst, size_t cap);
+/* Kernel launches this codec has issued (for launch accounting). */
+int64_t ebivgpu_codec_launches(ebivgpu_codec* c);
+const char* ebivgpu_status_string(int status);
+/* Non-zero when a CUDA device is usable from this process. */
+int ebivgpu_device_available(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
