@@ -28,6 +28,11 @@ class EncoderOptions(C.Structure):
     ]
 
 
+class PlaneView(C.Structure):
+    _fields_ = [("y", C.c_void_p), ("cb", C.c_void_p), ("cr", C.c_void_p),
+                ("y_stride", C.c_int32), ("c_stride", C.c_int32), ("width", C.c_int32), ("height", C.c_int32)]
+
+
 class Frame(C.Structure):
     _fields_ = [
         ("y", C.POINTER(C.c_uint8)), ("cb", C.POINTER(C.c_uint8)), ("cr", C.POINTER(C.c_uint8)),
@@ -62,6 +67,26 @@ def lib() -> C.CDLL:
     _sig(L, "ebivgpu_codec_launches", I64, P)
     _sig(L, "ebivgpu_status_string", C.c_char_p, I)
     _sig(L, "ebivgpu_device_available", I)
+    # batch
+    _sig(L, "ebivgpu_batch_create", I, PP)
+    _sig(L, "ebivgpu_batch_destroy", None, P)
+    _sig(L, "ebivgpu_batch_add_stream", I, P, C.POINTER(C.c_char_p), C.POINTER(S), I, I, C.POINTER(I))
+    _sig(L, "ebivgpu_batch_add_streaming", I, P, I, C.POINTER(I))
+    _sig(L, "ebivgpu_batch_submit", I, P, I, C.c_char_p, S)
+    _sig(L, "ebivgpu_batch_seek", I, P, I, I64)
+    _sig(L, "ebivgpu_batch_set_active", I, P, I, I)
+    _sig(L, "ebivgpu_batch_remove_stream", I, P, I)
+    _sig(L, "ebivgpu_batch_remaining", I64, P, I)
+    _sig(L, "ebivgpu_batch_round", I, P, C.POINTER(I))
+    _sig(L, "ebivgpu_batch_round_for", I, P, C.POINTER(I), I, C.POINTER(I))
+    _sig(L, "ebivgpu_batch_result_count", I, P)
+    _sig(L, "ebivgpu_batch_result", I, P, I, C.POINTER(I), C.POINTER(I64), C.POINTER(I), C.POINTER(I))
+    _sig(L, "ebivgpu_batch_result_planes", I, P, I, C.POINTER(PlaneView))
+    _sig(L, "ebivgpu_batch_result_download", I, P, I, U8P, S)
+    _sig(L, "ebivgpu_batch_timing", I, P, I, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double))
+    _sig(L, "ebivgpu_batch_launches", I64, P)
+    _sig(L, "ebivgpu_batch_device_bytes", C.c_uint64, P)
+    _sig(L, "ebivgpu_stream_footprint", C.c_uint64, I, I, I)
     # encoder
     _sig(L, "ebiv_encoder_default_options", None, C.POINTER(EncoderOptions))
     _sig(L, "ebiv_encoder_create", I, C.POINTER(EncoderOptions), PP)

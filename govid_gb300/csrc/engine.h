@@ -1,0 +1,111 @@
+// Multi-stream GB300 EBIV decode engine.
+//
+// Each stream owns a pool of padded frame buffers in HBM.  A frame decodes
+// straight into a free pool buffer, which then *is* the decoded output (the
+// visible region at a 64-byte aligned stride), the next frame's last
+// reference, and — for a key frame — the golden reference.  Reference and
+// golden are therefore aliases, never copies.  A buffer returns to the free
+// list once it is neither the last reference, the golden reference, nor one
+// of the stream's `ring` most recent outputs (ebiv/codec.go:15-22).
+//
+// A round decodes the next packet of every active stream: the host plans each
+// coded payload (ebiv/frame.go:242-274, ebiv/rans.go:396-471), uploads one
+// block of descriptors, and launches the entropy, inter and intra kernels once
+// for all streams' tiles and macroblocks.  Reference-side effects follow
+// ebiv/codec.go:70-192 exactly, including on errors.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+#include "ebiv_format.h"
+#include "gpu_types.h"
+#include "payload.h"
+
+namespace ebiv {
+
+struct EngineFrameView {
+  const uint8_t* y = nullptr;  // device pointers into the pool buffer
+  const uint8_t* cb = nullptr;
+  const uint8_t* cr = nullptr;
+  int yStride = 0, cStride = 0, width = 0, height = 0;
+  int buffer = -1;
+};
+
+struct RoundResult {
+  int stream = -1;
+  int status = kOK;
+  int64_t frameIndex = -1;  // packet index within the stream
+  bool keyframe = false;
+  EngineFrameView view;     // valid when status == kOK
+};
+
+class Engine {
+ public:
+  Engine();
+  ~Engine();
+  int init(cudaStream_t s = nullptr);
+  cudaStream_t stream() const { return stream_; }
+
+  // A stream whose packets are all resident in HBM (uploaded here).
+  int addResidentStream(const uint8_t* const* pkts, const size_t* lens, int n, int ring, int* id);
+  // A stream fed one packet per round through submit().
+  int addStreamingStream(int ring, int* id);
+  int submit(int id, const uint8_t* pkt, size_t n);
+  // Rewinds a resident stream to packet `index` (the caller seeks to a key
+  // frame); Flush semantics: only the output cursor resets.
+  int seekStream(int id, int64_t index);
+  int streams() const { return (int)streams_.size(); }
+  int64_t remaining(int id) const;
+  // Marks a stream inactive (it keeps its buffers until removed).
+  int setActive(int id, bool active);
+  int removeStream(int id);
+
+  // Decodes one packet for every active stream with work; returns the number
+  // of frames attempted.  Results (one per attempted frame) are appended.
+  int round(std::vector<RoundResult>* results);
+  // Same, for an explicit subset of streams.
+  int roundFor(const std::vector<int>& ids, std::vector<RoundResult>* results);
+
+  int downloadFrame(const EngineFrameView& v, uint8_t* packed, size_t cap);
+  int downloadStrided(const EngineFrameView& v, uint8_t* y, int ys, uint8_t* cb, uint8_t* cr, int cs);
+  int copyReference(int id, int which, uint8_t* dst, size_t cap);
+  int64_t launches() const { return launches_; }
+  size_t deviceBytes() const { return deviceBytes_; }
+  // Per-stream HBM footprint (pool + scratch) for a geometry.
+  static size_t footprint(int w, int h, int ring);
+
+  // Kernel-time accounting: CUDA events recorded around each round's
+  // kernels on the engine's stream.
+  void enableTiming(bool on) { timing_ = on; }
+  double kernelMillis() const { return kernelMs_; }
+  double entropyMillis() const { return entropyMs_; }
+  double reconMillis() const { return reconMs_; }
+  void resetTiming() { kernelMs_ = entropyMs_ = reconMs_ = 0; }
+
+ private:
+  struct Stream;
+  struct Job;
+  int configure(Stream& s, int w, int h);
+  int takeFree(Stream& s);
+  int planFrame(Stream& s, Job& j, std::vector<RoundResult>* results);
+  void finishFrame(Stream& s, Job& j, const int32_t* statuses, std::vector<RoundResult>* results);
+  int ensureStage(size_t bytes);
+
+  cudaStream_t stream_ = nullptr;
+  bool ownStream_ = false;
+  std::vector<std::unique_ptr<Stream>> streams_;
+  uint8_t* dStage_ = nullptr;
+  uint8_t* hStage_ = nullptr;
+  size_t stageCap_ = 0;
+  int64_t launches_ = 0;
+  size_t deviceBytes_ = 0;
+  bool timing_ = false;
+  cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+  double kernelMs_ = 0, entropyMs_ = 0, reconMs_ = 0;
+};
+
+}  // namespace ebiv

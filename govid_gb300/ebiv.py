@@ -189,6 +189,111 @@ def device_available() -> bool:
 
 
 # ---------------------------------------------------------------------------
+# Batched decode of many streams (include/ebivgpu.h, ebivgpu_batch_*)
+# ---------------------------------------------------------------------------
+
+
+@dataclass
+class BatchResult:
+    stream: int
+    frame_index: int
+    status: int
+    keyframe: bool
+    index: int  # position in the round's result list
+
+
+class Batch:
+    """Many independent EBIV streams decoded together: each round decodes the
+    next packet of every active stream with one set of kernel launches."""
+
+    def __init__(self):
+        L = _native.lib()
+        h = C.c_void_p()
+        _check(L.ebivgpu_batch_create(C.byref(h)), "batch")
+        self._h, self._L = h, L
+
+    def add_stream(self, packets: list[bytes], ring: int = 3) -> int:
+        n = len(packets)
+        arr = (C.c_char_p * n)(*packets)
+        lens = (C.c_size_t * n)(*[len(p) for p in packets])
+        sid = C.c_int()
+        _check(self._L.ebivgpu_batch_add_stream(self._h, arr, lens, n, ring, C.byref(sid)), "add_stream")
+        return sid.value
+
+    def add_streaming(self, ring: int = 3) -> int:
+        sid = C.c_int()
+        _check(self._L.ebivgpu_batch_add_streaming(self._h, ring, C.byref(sid)))
+        return sid.value
+
+    def submit(self, sid: int, pkt: bytes) -> None:
+        _check(self._L.ebivgpu_batch_submit(self._h, sid, pkt, len(pkt)))
+
+    def seek(self, sid: int, packet_index: int) -> None:
+        _check(self._L.ebivgpu_batch_seek(self._h, sid, packet_index))
+
+    def set_active(self, sid: int, active: bool) -> None:
+        _check(self._L.ebivgpu_batch_set_active(self._h, sid, int(active)))
+
+    def remove_stream(self, sid: int) -> None:
+        _check(self._L.ebivgpu_batch_remove_stream(self._h, sid))
+
+    def remaining(self, sid: int) -> int:
+        return int(self._L.ebivgpu_batch_remaining(self._h, sid))
+
+    def round(self, ids: list[int] | None = None) -> list[BatchResult]:
+        n = C.c_int()
+        if ids is None:
+            _check(self._L.ebivgpu_batch_round(self._h, C.byref(n)))
+        else:
+            arr = (C.c_int * len(ids))(*ids)
+            _check(self._L.ebivgpu_batch_round_for(self._h, arr, len(ids), C.byref(n)))
+        out = []
+        for i in range(self._L.ebivgpu_batch_result_count(self._h)):
+            s, st, k = C.c_int(), C.c_int(), C.c_int()
+            fi = C.c_int64()
+            self._L.ebivgpu_batch_result(self._h, i, C.byref(s), C.byref(fi), C.byref(st), C.byref(k))
+            out.append(BatchResult(s.value, fi.value, st.value, bool(k.value), i))
+        return out
+
+    def download(self, r: BatchResult, width: int, height: int) -> bytes:
+        n = packed_size(width, height)
+        buf = (C.c_uint8 * n)()
+        _check(self._L.ebivgpu_batch_result_download(self._h, r.index, buf, n))
+        return bytes(buf)
+
+    def planes(self, r: BatchResult) -> "_native.PlaneView":
+        v = _native.PlaneView()
+        _check(self._L.ebivgpu_batch_result_planes(self._h, r.index, C.byref(v)))
+        return v
+
+    def timing(self, enable: int = -1) -> tuple[float, float, float]:
+        k, e, r = C.c_double(), C.c_double(), C.c_double()
+        self._L.ebivgpu_batch_timing(self._h, enable, C.byref(k), C.byref(e), C.byref(r))
+        return k.value, e.value, r.value
+
+    def launches(self) -> int:
+        return int(self._L.ebivgpu_batch_launches(self._h))
+
+    def device_bytes(self) -> int:
+        return int(self._L.ebivgpu_batch_device_bytes(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.ebivgpu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def stream_footprint(width: int, height: int, ring: int = 3) -> int:
+    return int(_native.lib().ebivgpu_stream_footprint(width, height, ring))
+
+
+# ---------------------------------------------------------------------------
 # Demuxer (ebiv/reader.go)
 # ---------------------------------------------------------------------------
 

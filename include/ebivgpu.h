@@ -74,6 +74,46 @@ int ebivgpu_frame_rgba(ebivgpu_codec* c, int slot, uint8_t* dst, size_t cap);
 /* Kernel launches this codec has issued (for launch accounting). */
 int64_t ebivgpu_codec_launches(ebivgpu_codec* c);
 const char* ebivgpu_status_string(int status);
+
+/* ---- Batched decode of many independent streams --------------------------
+ * A batch holds streams whose packets are resident in HBM (add_stream) or fed
+ * one packet per round (add_streaming + submit).  Each round decodes the next
+ * packet of every active stream with one set of kernel launches; decoded
+ * frames stay in the stream's device frame pool (valid for `ring` further
+ * frames of that stream). */
+typedef struct ebivgpu_batch ebivgpu_batch;
+typedef struct {
+  const uint8_t* y;   /* device pointers */
+  const uint8_t* cb;
+  const uint8_t* cr;
+  int32_t y_stride, c_stride;
+  int32_t width, height;
+} ebivgpu_plane_view;
+
+int ebivgpu_batch_create(ebivgpu_batch** out);
+void ebivgpu_batch_destroy(ebivgpu_batch* b);
+int ebivgpu_batch_add_stream(ebivgpu_batch* b, const uint8_t* const* pkts, const size_t* lens, int n, int ring,
+                             int* stream_id);
+int ebivgpu_batch_add_streaming(ebivgpu_batch* b, int ring, int* stream_id);
+int ebivgpu_batch_submit(ebivgpu_batch* b, int stream_id, const uint8_t* pkt, size_t n);
+/* Repositions a resident stream at a packet index (seek to a key frame). */
+int ebivgpu_batch_seek(ebivgpu_batch* b, int stream_id, int64_t packet_index);
+int ebivgpu_batch_set_active(ebivgpu_batch* b, int stream_id, int active);
+int ebivgpu_batch_remove_stream(ebivgpu_batch* b, int stream_id);
+int64_t ebivgpu_batch_remaining(ebivgpu_batch* b, int stream_id);
+/* One round over every active stream; *frames = frames attempted. */
+int ebivgpu_batch_round(ebivgpu_batch* b, int* frames);
+int ebivgpu_batch_round_for(ebivgpu_batch* b, const int* stream_ids, int count, int* frames);
+int ebivgpu_batch_result_count(ebivgpu_batch* b);
+int ebivgpu_batch_result(ebivgpu_batch* b, int i, int* stream_id, int64_t* frame_index, int* status, int* keyframe);
+int ebivgpu_batch_result_planes(ebivgpu_batch* b, int i, ebivgpu_plane_view* out);
+int ebivgpu_batch_result_download(ebivgpu_batch* b, int i, uint8_t* packed, size_t cap);
+/* enable: 1 on (resets counters), 0 off, -1 read only. */
+int ebivgpu_batch_timing(ebivgpu_batch* b, int enable, double* kernel_ms, double* entropy_ms, double* recon_ms);
+int64_t ebivgpu_batch_launches(ebivgpu_batch* b);
+uint64_t ebivgpu_batch_device_bytes(ebivgpu_batch* b);
+/* HBM bytes one stream of this geometry holds (frame pool + scratch). */
+uint64_t ebivgpu_stream_footprint(int width, int height, int ring);
 /* Non-zero when a CUDA device is usable from this process. */
 int ebivgpu_device_available(void);
 
