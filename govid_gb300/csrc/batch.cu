@@ -21,6 +21,35 @@ inline size_t al(size_t v, size_t a) { return (v + a - 1) / a * a; }
 inline int stride64(int w) { return (w + 63) & ~63; }
 }  // namespace
 
+// Per-frame scratch in HBM for one in-flight frame of a stream.
+struct Slot {
+  MBRec* rec = nullptr;
+  uint32_t* coef = nullptr;
+  int16_t* mv = nullptr;
+  int16_t* lv = nullptr;
+  uint32_t* intra = nullptr;  // intra list, then the level-sorted copy
+  TileStat* ts = nullptr;
+  bool alloc(size_t mbs) {
+    return cudaMalloc(&rec, mbs * sizeof(MBRec)) == cudaSuccess &&
+           cudaMalloc(&coef, mbs * kCoefPerMB * sizeof(uint32_t)) == cudaSuccess &&
+           cudaMalloc(&mv, mbs * 2 * sizeof(int16_t)) == cudaSuccess &&
+           cudaMalloc(&lv, mbs * sizeof(int16_t)) == cudaSuccess &&
+           cudaMalloc(&intra, 2 * mbs * sizeof(uint32_t)) == cudaSuccess &&
+           cudaMalloc(&ts, mbs * sizeof(TileStat)) == cudaSuccess;
+  }
+  void release() {
+    cudaFree(rec);
+    cudaFree(coef);
+    cudaFree(mv);
+    cudaFree(lv);
+    cudaFree(intra);
+    cudaFree(ts);
+  }
+  static size_t bytes(size_t mbs) {
+    return mbs * (sizeof(MBRec) + kCoefPerMB * 4 + 4 + 2 + 8 + sizeof(TileStat));
+  }
+};
+
 struct Engine::Stream {
   int id = -1;
   bool active = true;
@@ -31,7 +60,7 @@ struct Engine::Stream {
   size_t yBytes = 0, cBytes = 0, bufBytes = 0;
   bool ready = false;
   std::vector<uint8_t*> pool;
-  std::vector<int> outputs;  // FIFO of buffer indices, oldest first
+  std::vector<int> outputs;  // FIFO of committed output buffers, oldest first
   int ref = -1, golden = -1;
   TableHistory hist;
   // Resident packets: host copies (for planning) and one device block.
@@ -42,12 +71,7 @@ struct Engine::Stream {
   // Streaming: the submitted packet awaiting its round.
   std::vector<uint8_t> pendingPkt;
   bool pending = false;
-  // Per-frame scratch.
-  MBRec* dRec = nullptr;
-  uint32_t* dCoef = nullptr;
-  int16_t* dMV = nullptr;
-  TileStat* dTileStat = nullptr;
-  TileStat* dTileStatOv = nullptr;
+  std::vector<Slot> slots;
   size_t mbs = 0;
   size_t bytes = 0;
 
@@ -57,17 +81,10 @@ struct Engine::Stream {
   void release() {
     for (auto p : pool) cudaFree(p);
     pool.clear();
+    for (auto& sl : slots) sl.release();
+    slots.clear();
     if (dPkts) cudaFree(dPkts);
-    if (dRec) cudaFree(dRec);
-    if (dCoef) cudaFree(dCoef);
-    if (dMV) cudaFree(dMV);
-    if (dTileStat) cudaFree(dTileStat);
-    if (dTileStatOv) cudaFree(dTileStatOv);
     dPkts = nullptr;
-    dRec = nullptr;
-    dCoef = nullptr;
-    dMV = nullptr;
-    dTileStat = dTileStatOv = nullptr;
   }
 };
 
@@ -81,12 +98,16 @@ struct Engine::Job {
   int status = kOK;  // host-side result when the frame never reaches the GPU
   bool gpu = false;  // frame has kernels this round
   int work = -1, ovBuf = -1;
+  int ref = -1, golden = -1;  // references the frame decodes against
   bool hasOv = false;
   int ovPlanStatus = kOK;
   PayloadPlan main, ov;
-  TableHistory ovHist;
+  TableHistory hMain;    // table history after the main payload was planned
+  TableHistory hBefore;  // table history before this frame was planned
+  int step = 0, slot = -1;
   int mainDesc = -1, ovDesc = -1;
-  size_t stageOff = 0;  // for streamed packets: offset in the staging block
+  int gateDesc = -1;  // descriptor whose status gates this frame (-1: none)
+  size_t stageOff = 0;
 };
 
 Engine::Engine() {}
@@ -114,11 +135,19 @@ int Engine::init(cudaStream_t s) {
   return ensureDeviceTables();
 }
 
-size_t Engine::footprint(int w, int h, int ring) {
+int Engine::setLookahead(int k) {
+  if (k < 1 || k > 64) return kErrArg;
+  for (auto& s : streams_)
+    if (s && s->ready) return kErrArg;  // pools are sized at configure
+  lookahead_ = k;
+  return kOK;
+}
+
+size_t Engine::footprint(int w, int h, int ring, int lookahead) {
   const Geometry g = Geometry::of(w, h);
   const size_t yb = (size_t)stride64(g.padW()) * g.padH(), cb = (size_t)stride64(g.padCW()) * g.padCH();
   const size_t mbs = (size_t)g.mbCols * g.mbRows;
-  return (size_t)(ring + 4) * (yb + 2 * cb) + mbs * (sizeof(MBRec) + kCoefPerMB * 4 + 4 + 2 * sizeof(TileStat));
+  return (size_t)(ring + 2 * lookahead + 3) * (yb + 2 * cb) + (size_t)(lookahead + 1) * Slot::bytes(mbs);
 }
 
 int Engine::addResidentStream(const uint8_t* const* pkts, const size_t* lens, int n, int ring, int* id) {
@@ -203,7 +232,8 @@ int Engine::configure(Stream& s, int w, int h) {
   s.yBytes = (size_t)s.strideY * s.geo.padH();
   s.cBytes = (size_t)s.strideC * s.geo.padCH();
   s.bufBytes = s.yBytes + 2 * s.cBytes;
-  const int P = s.ring + 4;
+  const int k = s.resident ? lookahead_ : 1;
+  const int P = s.ring + 2 * k + 3;
   for (int i = 0; i < P; i++) {
     uint8_t* p = nullptr;
     if (cudaMalloc(&p, s.bufBytes) != cudaSuccess) return kErrDevice;
@@ -214,26 +244,14 @@ int Engine::configure(Stream& s, int w, int h) {
   s.ref = 0;
   s.golden = 1;
   s.mbs = (size_t)s.geo.mbCols * s.geo.mbRows;
-  if (cudaMalloc(&s.dRec, s.mbs * sizeof(MBRec)) != cudaSuccess) return kErrDevice;
-  if (cudaMalloc(&s.dCoef, s.mbs * kCoefPerMB * sizeof(uint32_t)) != cudaSuccess) return kErrDevice;
-  if (cudaMalloc(&s.dMV, s.mbs * 2 * sizeof(int16_t)) != cudaSuccess) return kErrDevice;
-  if (cudaMalloc(&s.dTileStat, s.mbs * sizeof(TileStat)) != cudaSuccess) return kErrDevice;
-  if (cudaMalloc(&s.dTileStatOv, s.mbs * sizeof(TileStat)) != cudaSuccess) return kErrDevice;
-  const size_t b = (size_t)P * s.bufBytes + s.mbs * (sizeof(MBRec) + kCoefPerMB * 4 + 4 + 2 * sizeof(TileStat));
+  s.slots.resize((size_t)k + 1);
+  for (auto& sl : s.slots)
+    if (!sl.alloc(s.mbs)) return kErrDevice;
+  const size_t b = (size_t)P * s.bufBytes + (size_t)(k + 1) * Slot::bytes(s.mbs);
   s.bytes += b;
   deviceBytes_ += b;
   s.ready = true;
   return kOK;
-}
-
-int Engine::takeFree(Stream& s) {
-  std::vector<char> used(s.pool.size(), 0);
-  if (s.ref >= 0) used[(size_t)s.ref] = 1;
-  if (s.golden >= 0) used[(size_t)s.golden] = 1;
-  for (int b : s.outputs) used[(size_t)b] = 1;
-  for (size_t i = 0; i < s.pool.size(); i++)
-    if (!used[i]) return (int)i;
-  return -1;
 }
 
 int Engine::ensureStage(size_t bytes) {
@@ -253,25 +271,40 @@ int Engine::ensureStage(size_t bytes) {
   return kOK;
 }
 
+// A pool buffer outside `busy` (the committed references and outputs plus
+// everything the round has already claimed).
+static int freeBuffer(size_t poolSize, const std::vector<char>& busy) {
+  for (size_t i = 0; i < poolSize; i++)
+    if (!busy[i]) return (int)i;
+  return -1;
+}
+
 // Host half of Codec.Decode for one packet: header, configure, raw frames,
-// payload planning.  Leaves j.gpu set when kernels must run.
-int Engine::planFrame(Stream& s, Job& j, std::vector<RoundResult>* results) {
-  (void)results;
+// payload planning (ebiv/codec.go:70-192).  ref/golden are the references the
+// frame decodes against; busy marks pool buffers it must not claim.
+int Engine::planFrame(Stream& s, Job& j, std::vector<char>& busy) {
   j.status = parseFrameHeader(j.hPkt, j.n, &j.fh);
   if (j.status) return j.status;
   if (j.fh.type == kFrameKey) {
+    const bool first = !s.ready;
     j.status = configure(s, j.fh.width, j.fh.height);
     if (j.status) return j.status;
+    if (first) {
+      busy.assign(s.pool.size(), 0);
+      busy[(size_t)s.ref] = busy[(size_t)s.golden] = 1;
+      j.ref = s.ref;
+      j.golden = s.golden;
+    }
   } else if (!s.ready) {
     return j.status = kErrNoKeyframe;
   }
   const FrameHeader& fh = j.fh;
   if (fh.coding == kCodingRaw) {  // decodeRaw — ebiv/codec.go:195-207
-    const size_t blen = j.n - fh.bodyOffset;
-    if (blen != s.geo.packedSize()) return j.status = kErrCorrupt;
-    j.work = takeFree(s);
+    if (j.n - fh.bodyOffset != s.geo.packedSize()) return j.status = kErrCorrupt;
+    j.work = freeBuffer(s.pool.size(), busy);
     if (j.work < 0) return j.status = kErrDevice;
-    return kOK;  // scattered by the round, no kernels
+    busy[(size_t)j.work] = 1;
+    return kOK;
   }
   if (fh.coding != kCodingIntra && fh.coding != kCodingInter) return j.status = kErrUnsupported;
   const bool key = fh.type == kFrameKey;
@@ -287,28 +320,23 @@ int Engine::planFrame(Stream& s, Job& j, std::vector<RoundResult>* results) {
   }
   j.status = planPayload(j.hPkt, bodyOff, bodyLen, key, s.geo.mbCols, s.geo.mbRows, s.hist, &j.main);
   if (j.status) return j.status;
-  j.work = takeFree(s);
+  j.hMain = s.hist;
+  j.work = freeBuffer(s.pool.size(), busy);
   if (j.work < 0) return j.status = kErrDevice;
+  busy[(size_t)j.work] = 1;
   if (key && fh.goldenOverride) {
     j.hasOv = true;
-    j.ovHist = s.hist;
-    j.ovPlanStatus = planPayload(j.hPkt, ovOff, ovLen, false, s.geo.mbCols, s.geo.mbRows, j.ovHist, &j.ov);
+    // The override's tables chain after the key's (ebiv/codec.go:177-183);
+    // s.hist holds them speculatively until the key's own decode is known.
+    j.ovPlanStatus = planPayload(j.hPkt, ovOff, ovLen, false, s.geo.mbCols, s.geo.mbRows, s.hist, &j.ov);
     if (j.ovPlanStatus == kOK) {
       // The override decodes over a copy of the current golden so that a
       // failing override leaves the same partial image the reference's
       // in-place decode does.
-      std::vector<char> used(s.pool.size(), 0);
-      for (size_t i = 0; i < s.pool.size(); i++) {
-        if ((int)i == s.ref || (int)i == s.golden || (int)i == j.work) used[i] = 1;
-      }
-      for (int b : s.outputs) used[(size_t)b] = 1;
-      for (size_t i = 0; i < s.pool.size(); i++)
-        if (!used[i]) {
-          j.ovBuf = (int)i;
-          break;
-        }
+      j.ovBuf = freeBuffer(s.pool.size(), busy);
       if (j.ovBuf < 0) return j.status = kErrDevice;
-      if (cudaMemcpyAsync(s.pool[(size_t)j.ovBuf], s.pool[(size_t)s.golden], s.bufBytes, cudaMemcpyDeviceToDevice,
+      busy[(size_t)j.ovBuf] = 1;
+      if (cudaMemcpyAsync(s.pool[(size_t)j.ovBuf], s.pool[(size_t)j.golden], s.bufBytes, cudaMemcpyDeviceToDevice,
                           stream_) != cudaSuccess)
         return j.status = kErrDevice;
     }
@@ -328,28 +356,28 @@ void Engine::finishFrame(Stream& s, Job& j, const int32_t* st, std::vector<Round
     out = j.work;
   } else if (status == kOK && j.gpu) {
     status = st[j.mainDesc];
+    const bool key = j.fh.type == kFrameKey;
+    if (status != kOK) {
+      if (j.hasOv) s.hist = j.hMain;  // the override's tables were never parsed
+    } else if (key && j.hasOv) {
+      if (j.ovPlanStatus != kOK) {
+        status = j.ovPlanStatus;
+      } else {
+        s.golden = j.ovBuf;  // written in place over golden, even on failure
+        status = st[j.ovDesc];
+      }
+    } else if (key) {
+      s.golden = j.work;
+    }
     if (status == kOK) {
-      const bool key = j.fh.type == kFrameKey;
-      if (key && j.hasOv) {
-        s.hist = j.ovHist;  // the override's tables were parsed (ebiv/codec.go:177-183)
-        if (j.ovPlanStatus != kOK) {
-          status = j.ovPlanStatus;
-        } else {
-          s.golden = j.ovBuf;  // written in place over golden, even on failure
-          status = st[j.ovDesc];
-        }
-      } else if (key) {
-        s.golden = j.work;
-      }
-      if (status == kOK) {
-        s.ref = j.work;
-        out = j.work;
-      }
+      s.ref = j.work;
+      out = j.work;
     }
   }
   if (out >= 0) {
     s.outputs.push_back(out);
-    while ((int)s.outputs.size() > s.ring) s.outputs.erase(s.outputs.begin());
+    const int cap = s.ring + (s.resident ? lookahead_ : 1);
+    while ((int)s.outputs.size() > cap) s.outputs.erase(s.outputs.begin());
     r.view.y = s.plane(out, 0);
     r.view.cb = s.plane(out, 1);
     r.view.cr = s.plane(out, 2);
@@ -372,33 +400,67 @@ int Engine::round(std::vector<RoundResult>* results) {
 }
 
 int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* results) {
+  // ---- plan: up to `lookahead` frames per resident stream --------------------
   std::vector<Job> jobs;
-  jobs.reserve(ids.size());
+  jobs.reserve(ids.size() * (size_t)lookahead_);
+  std::vector<std::vector<int>> chains;  // per stream, indices into jobs in decode order
   size_t streamedBytes = 0;
   for (int id : ids) {
     if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) continue;
     Stream& s = *streams_[(size_t)id];
-    Job j;
-    j.stream = id;
-    if (s.resident) {
-      if (s.next >= (int64_t)s.hostPkts.size()) continue;
-      j.pktIndex = s.next;
-      j.hPkt = s.hostPkts[(size_t)s.next].data();
-      j.n = s.hostPkts[(size_t)s.next].size();
-      j.dPkt = s.dPkts + s.dOff[(size_t)s.next];
-      s.next++;
-    } else {
-      if (!s.pending) continue;
-      j.hPkt = s.pendingPkt.data();
-      j.n = s.pendingPkt.size();
-      j.pktIndex = s.next++;
+    std::vector<int> chain;
+    std::vector<char> busy;
+    int provRef = s.ref, provGolden = s.golden;
+    auto resetBusy = [&] {
+      busy.assign(s.pool.size(), 0);
+      if (provRef >= 0) busy[(size_t)provRef] = 1;
+      if (provGolden >= 0) busy[(size_t)provGolden] = 1;
+      for (int b : s.outputs) busy[(size_t)b] = 1;
+    };
+    resetBusy();
+    const int k = s.resident ? lookahead_ : 1;
+    int lastGpu = -1;  // job index of the chain's last GPU frame
+    for (int step = 0; step < k; step++) {
+      Job j;
+      j.stream = id;
+      j.step = step;
+      if (s.resident) {
+        if (s.next >= (int64_t)s.hostPkts.size()) break;
+        j.pktIndex = s.next;
+        j.hPkt = s.hostPkts[(size_t)s.next].data();
+        j.n = s.hostPkts[(size_t)s.next].size();
+        j.dPkt = s.dPkts + s.dOff[(size_t)s.next];
+        s.next++;
+      } else {
+        if (!s.pending) break;
+        j.hPkt = s.pendingPkt.data();
+        j.n = s.pendingPkt.size();
+        j.pktIndex = s.next++;
+      }
+      j.ref = provRef;
+      j.golden = provGolden;
+      j.slot = step;
+      if (step > 0) j.hBefore = s.hist;
+      planFrame(s, j, busy);
+      // (configure may have allocated the pool: references start as the zeroed buffers)
+      if (j.ref < 0) j.ref = s.ref;
+      if (j.golden < 0) j.golden = s.golden;
+      if (j.status == kOK && j.gpu) {
+        j.gateDesc = lastGpu;  // resolved to a descriptor index below
+        if (!s.resident) {
+          j.stageOff = streamedBytes;
+          streamedBytes += al(j.n, 16);
+        }
+        provRef = j.work;
+        if (j.fh.type == kFrameKey) provGolden = (j.hasOv && j.ovPlanStatus == kOK) ? j.ovBuf : j.work;
+        lastGpu = (int)jobs.size();
+      }
+      const bool stop = j.hasOv;  // an override's outcome decides golden: end the chain here
+      chain.push_back((int)jobs.size());
+      jobs.push_back(std::move(j));
+      if (stop) break;
     }
-    planFrame(s, j, results);
-    if (j.status == kOK && j.gpu && !s.resident) {
-      j.stageOff = streamedBytes;
-      streamedBytes += al(j.n, 16);
-    }
-    jobs.push_back(std::move(j));
+    if (!chain.empty()) chains.push_back(std::move(chain));
   }
   // Raw frames: scatter the packed planes into their pool buffer.
   for (Job& j : jobs) {
@@ -414,35 +476,48 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
                           stream_))
       j.status = kErrDevice;
   }
-  // Lay out the staging block: descriptors, statuses, tables, tiles, jobs,
-  // streamed packet bytes.
-  int nMain = 0, nOv = 0, tMain = 0, tOv = 0, maxMBs = 0, maxMBsOv = 0;
-  for (Job& j : jobs) {
-    if (j.status != kOK || !j.gpu) continue;
-    const Stream& s = *streams_[(size_t)j.stream];
-    j.mainDesc = nMain++;
-    tMain += (int)j.main.tiles.size();
-    if (j.main.tiles.size() && j.fh.coding == kCodingInter) maxMBs = std::max(maxMBs, (int)s.mbs);
-    if (j.hasOv && j.ovPlanStatus == kOK) {
-      nOv++;
-      tOv += (int)j.ov.tiles.size();
-      maxMBsOv = std::max(maxMBsOv, (int)s.mbs);
+  // ---- descriptors grouped by step: [main step 0][ov step 0][main step 1]... --
+  int maxStep = -1;
+  for (const Job& j : jobs)
+    if (j.status == kOK && j.gpu) maxStep = std::max(maxStep, j.step);
+  struct StepInfo {
+    int mainFirst = 0, mainCount = 0, ovFirst = 0, ovCount = 0;
+    int jobFirst = 0, jobCount = 0, ovJobFirst = 0, ovJobCount = 0;
+    int maxInterMBs = 0, maxOvMBs = 0;
+  };
+  std::vector<StepInfo> steps((size_t)(maxStep + 1));
+  int nDesc = 0, nTiles = 0;
+  for (int st = 0; st <= maxStep; st++) {
+    StepInfo& si = steps[(size_t)st];
+    si.mainFirst = nDesc;
+    si.jobFirst = nTiles;
+    for (Job& j : jobs) {
+      if (j.status != kOK || !j.gpu || j.step != st) continue;
+      j.mainDesc = nDesc++;
+      si.mainCount++;
+      nTiles += (int)j.main.tiles.size();
+      si.jobCount += (int)j.main.tiles.size();
+      if (j.fh.coding == kCodingInter) si.maxInterMBs = std::max(si.maxInterMBs, (int)streams_[(size_t)j.stream]->mbs);
+    }
+    si.ovFirst = nDesc;
+    si.ovJobFirst = nTiles;
+    for (Job& j : jobs) {
+      if (j.status != kOK || !j.gpu || j.step != st || !j.hasOv || j.ovPlanStatus != kOK) continue;
+      j.ovDesc = nDesc++;
+      si.ovCount++;
+      nTiles += (int)j.ov.tiles.size();
+      si.ovJobCount += (int)j.ov.tiles.size();
+      si.maxOvMBs = std::max(si.maxOvMBs, (int)streams_[(size_t)j.stream]->mbs);
     }
   }
-  {
-    int k = 0;
-    for (Job& j : jobs)
-      if (j.status == kOK && j.gpu && j.hasOv && j.ovPlanStatus == kOK) j.ovDesc = nMain + k++;
-  }
-  const int nDesc = nMain + nOv;
   std::vector<int32_t> statuses((size_t)std::max(nDesc, 1), 0);
   if (nDesc > 0) {
     const size_t oDesc = 0;
     const size_t oStat = al(oDesc + sizeof(FrameDesc) * nDesc, 64);
     const size_t oTab = al(oStat + sizeof(int32_t) * nDesc, 64);
     const size_t oTiles = al(oTab + sizeof(DeviceTables) * nDesc, 64);
-    const size_t oJobs = al(oTiles + sizeof(TileRange) * (size_t)(tMain + tOv), 64);
-    const size_t oPkt = al(oJobs + sizeof(int2) * (size_t)(tMain + tOv), 256);
+    const size_t oJobs = al(oTiles + sizeof(TileRange) * (size_t)nTiles, 64);
+    const size_t oPkt = al(oJobs + sizeof(int2) * (size_t)nTiles, 256);
     const size_t total = oPkt + streamedBytes;
     if (ensureStage(total)) return -1;
     uint8_t* h = hStage_;
@@ -452,9 +527,23 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
     DeviceTables* ht = reinterpret_cast<DeviceTables*>(h + oTab);
     TileRange* hr = reinterpret_cast<TileRange*>(h + oTiles);
     int2* hj = reinterpret_cast<int2*>(h + oJobs);
-    int tileCur = 0;
-    auto fill = [&](Job& j, const PayloadPlan& plan, int di, int rec, int ref, int gold, bool inter, int gateDesc,
-                    TileStat* ts) {
+    // Tile jobs are laid out in descriptor order, so each descriptor's tiles
+    // and each step's job ranges are contiguous.
+    std::vector<int> tileFirst((size_t)nDesc, 0);
+    {
+      std::vector<int> tilesOf((size_t)nDesc, 0);
+      for (const Job& j : jobs) {
+        if (j.mainDesc >= 0) tilesOf[(size_t)j.mainDesc] = (int)j.main.tiles.size();
+        if (j.ovDesc >= 0) tilesOf[(size_t)j.ovDesc] = (int)j.ov.tiles.size();
+      }
+      int acc = 0;
+      for (int di = 0; di < nDesc; di++) {
+        tileFirst[(size_t)di] = acc;
+        acc += tilesOf[(size_t)di];
+      }
+    }
+    auto fill = [&](const Job& j, const PayloadPlan& plan, int di, int rec, int ref, int gold, bool inter, int gateDesc,
+                    const Slot& sl) {
       const Stream& s = *streams_[(size_t)j.stream];
       FrameDesc& fd = hd[di];
       std::memset(&fd, 0, sizeof(fd));
@@ -478,51 +567,54 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
       fd.tileCount = (int)plan.tiles.size();
       fd.pkt = j.dPkt ? j.dPkt : d + oPkt + j.stageOff;
       fd.tables = reinterpret_cast<const DeviceTables*>(d + oTab) + di;
-      fd.tiles = reinterpret_cast<const TileRange*>(d + oTiles) + tileCur;
-      fd.mbrec = s.dRec;
-      fd.coef = s.dCoef;
-      fd.mvgrid = s.dMV;
-      fd.tileStat = ts;
+      const int tf = tileFirst[(size_t)di];
+      fd.tiles = reinterpret_cast<const TileRange*>(d + oTiles) + tf;
+      fd.mbrec = sl.rec;
+      fd.coef = sl.coef;
+      fd.mvgrid = sl.mv;
+      fd.lvgrid = sl.lv;
+      fd.intraList = sl.intra;
+      fd.intraSorted = sl.intra + s.mbs;
+      fd.tileStat = sl.ts;
       fd.status = reinterpret_cast<int32_t*>(d + oStat) + di;
       fd.gate = gateDesc >= 0 ? reinterpret_cast<const int32_t*>(d + oStat) + gateDesc : nullptr;
       hs[di] = 0;
       ht[di] = plan.tables;
       for (size_t t = 0; t < plan.tiles.size(); t++) {
-        hr[tileCur + t] = plan.tiles[t];
-        hj[tileCur + t] = make_int2(di, (int)t);
+        hr[tf + t] = plan.tiles[t];
+        hj[tf + t] = make_int2(di, (int)t);
       }
-      tileCur += (int)plan.tiles.size();
     };
     for (Job& j : jobs) {
-      if (j.status != kOK || !j.gpu) continue;
+      if (j.mainDesc < 0) continue;
       Stream& s = *streams_[(size_t)j.stream];
-      fill(j, j.main, j.mainDesc, j.work, s.ref, s.golden, j.fh.coding == kCodingInter, -1, s.dTileStat);
+      const int gate = j.gateDesc >= 0 ? jobs[(size_t)j.gateDesc].mainDesc : -1;
+      fill(j, j.main, j.mainDesc, j.work, j.ref, j.golden, j.fh.coding == kCodingInter, gate, s.slots[(size_t)j.slot]);
       if (!s.resident) std::memcpy(h + oPkt + j.stageOff, j.hPkt, j.n);
-    }
-    for (Job& j : jobs) {
-      if (j.status != kOK || !j.gpu || j.ovDesc < 0) continue;
-      Stream& s = *streams_[(size_t)j.stream];
-      fill(j, j.ov, j.ovDesc, j.ovBuf, j.work, j.work, true, j.mainDesc, s.dTileStatOv);
+      if (j.ovDesc >= 0)
+        fill(j, j.ov, j.ovDesc, j.ovBuf, j.work, j.work, true, j.mainDesc, s.slots.back());
     }
     if (cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, stream_) != cudaSuccess) return -1;
     const FrameDesc* dd = reinterpret_cast<const FrameDesc*>(d + oDesc);
     const int2* dj = reinterpret_cast<const int2*>(d + oJobs);
     if (timing_) cudaEventRecord(ev_[0], stream_);
-    launchEntropy(dd, dj, tMain, stream_);
+    launchEntropy(dd, dj, nTiles, stream_);
+    launches_++;
     if (timing_) cudaEventRecord(ev_[1], stream_);
-    if (maxMBs > 0) {
-      launchInter(dd, nMain, maxMBs, stream_);
-      launches_++;
-    }
-    launchIntra(dd, dj, tMain, stream_);
-    launches_ += 2;
-    if (nOv > 0) {
-      // Override tile jobs index descriptors absolutely; the inter kernel
-      // takes its frame from blockIdx.y, so it gets the override sub-array.
-      launchEntropy(dd, dj + tMain, tOv, stream_);
-      launchInter(dd + nMain, nOv, maxMBsOv, stream_);
-      launchIntra(dd, dj + tMain, tOv, stream_);
-      launches_ += 3;
+    for (const StepInfo& si : steps) {
+      if (si.maxInterMBs > 0) {
+        launchInter(dd + si.mainFirst, si.mainCount, si.maxInterMBs, stream_);
+        launches_++;
+      }
+      if (si.jobCount > 0) {
+        launchIntra(dd, dj + si.jobFirst, si.jobCount, stream_);
+        launches_++;
+      }
+      if (si.ovCount > 0) {
+        launchInter(dd + si.ovFirst, si.ovCount, si.maxOvMBs, stream_);
+        launchIntra(dd, dj + si.ovJobFirst, si.ovJobCount, stream_);
+        launches_ += 2;
+      }
     }
     if (timing_) cudaEventRecord(ev_[2], stream_);
     if (cudaMemcpyAsync(statuses.data(), d + oStat, sizeof(int32_t) * nDesc, cudaMemcpyDeviceToHost, stream_) !=
@@ -541,12 +633,25 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
     reconMs_ += b;
     kernelMs_ += a + b;
   }
-  for (Job& j : jobs) {
-    Stream& s = *streams_[(size_t)j.stream];
+  // ---- commit each stream's chain in order; roll back at the first skipped frame
+  int attempted = 0;
+  for (const auto& chain : chains) {
+    Stream& s = *streams_[(size_t)jobs[(size_t)chain[0]].stream];
+    for (size_t c = 0; c < chain.size(); c++) {
+      Job& j = jobs[(size_t)chain[c]];
+      if (j.mainDesc >= 0 && statuses[(size_t)j.mainDesc] == kSkipped) {
+        // The frame this one depended on failed: re-plan from here next round
+        // with the table history as it stood before this frame was planned.
+        s.hist = j.hBefore;
+        s.next = j.pktIndex;
+        break;
+      }
+      finishFrame(s, j, statuses.data(), results);
+      attempted++;
+    }
     if (!s.resident) s.pending = false;
-    finishFrame(s, j, statuses.data(), results);
   }
-  return (int)jobs.size();
+  return attempted;
 }
 
 int Engine::downloadFrame(const EngineFrameView& v, uint8_t* packed, size_t cap) {
@@ -715,8 +820,12 @@ int ebivgpu_batch_timing(ebivgpu_batch* b, int enable, double* kernel_ms, double
   return kOK;
 }
 
+int ebivgpu_batch_set_lookahead(ebivgpu_batch* b, int frames) { return b ? b->e.setLookahead(frames) : kErrArg; }
+
 int64_t ebivgpu_batch_launches(ebivgpu_batch* b) { return b ? b->e.launches() : 0; }
 uint64_t ebivgpu_batch_device_bytes(ebivgpu_batch* b) { return b ? (uint64_t)b->e.deviceBytes() : 0; }
-uint64_t ebivgpu_stream_footprint(int w, int h, int ring) { return (uint64_t)Engine::footprint(w, h, ring); }
+uint64_t ebivgpu_stream_footprint(int w, int h, int ring, int lookahead) {
+  return (uint64_t)Engine::footprint(w, h, ring, lookahead < 1 ? 1 : lookahead);
+}
 
 }  // extern "C"

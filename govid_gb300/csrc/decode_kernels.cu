@@ -47,42 +47,72 @@ __device__ __forceinline__ int16_t clampMV(int v) {
 // ---------------------------------------------------------------------------
 // Stage A: entropy decode
 // ---------------------------------------------------------------------------
+// Per-warp symbol tables.  sym[c*16+s] packs the cumulative start (low 16
+// bits) and frequency (high 16) of symbol s in context c.  lut[c*64+b] is the
+// symbol whose range holds slot b*64 — the decoder starts there and walks
+// forward at most a few entries; 0xFF marks an unused context.
 struct WarpTables {
-  uint16_t start[kNumContexts * 17];
-  uint8_t used[kNumContexts];
+  uint32_t sym[kNumContexts * 16];
+  uint8_t lut[kNumContexts * 64];
+};
+constexpr int kRowMax = 128;  // tiles at most this many macroblocks wide keep their rows in shared memory
+struct WarpRows {
+  uint32_t mv[2][kRowMax];   // packed motion vectors of the row above / the current row
+  int16_t lvl[2][kRowMax];   // intra dependency levels (-1: not intra)
+  uint32_t rec[12];          // the macroblock record being assembled
 };
 
-// A tile's rANS decoder.  Every field is warp-uniform: all 32 lanes hold the
-// same values and take the same branches.
+__device__ __forceinline__ void buildWarpTables(WarpTables& T, const DeviceTables& src, int lane) {
+  for (int i = lane; i < kNumContexts * 16; i += 32) {
+    const int c = i >> 4, sidx = i & 15;
+    const uint32_t st = src.start[c][sidx], nx = src.start[c][sidx + 1];
+    T.sym[i] = (st == 0xFFFFu || nx == 0xFFFFu) ? 0xFFFFu : (st | ((nx - st) << 16));
+  }
+  for (int i = lane; i < kNumContexts * 64; i += 32) T.lut[i] = 0xFF;
+  __syncwarp();
+  // Each (context, symbol) pair fills the buckets whose first slot it covers.
+  for (int i = lane; i < kNumContexts * 16; i += 32) {
+    const int c = i >> 4, sidx = i & 15;
+    if (!src.used[c]) continue;
+    const uint32_t st = src.start[c][sidx], nx = src.start[c][sidx + 1];
+    if (st == 0xFFFFu || nx == 0xFFFFu || nx <= st) continue;
+    for (uint32_t b = (st + 63) >> 6; b < 64 && (b << 6) < nx; b++) T.lut[c * 64 + b] = (uint8_t)sidx;
+  }
+  __syncwarp();
+}
+
+// A tile's rANS decoder (ebiv/rans.go:222-304).  All fields are warp-uniform;
+// the two next stream bytes are prefetched so renormalisation rarely waits.
 struct Chain {
   const uint8_t* buf;
   int32_t pos;
   uint32_t x0, x1, x2, x3;  // states in use order: x0 decodes the next symbol
+  uint32_t b1, b2;          // buf[pos-1], buf[pos-2] when present
   int32_t err;
   const WarpTables* t;
-  int lane;
+
+  __device__ __forceinline__ uint32_t byteAt(int i) const { return i >= 0 ? (uint32_t)__ldg(buf + i) : 0u; }
 
   __device__ __forceinline__ int sym(int ctx) {
     if (err) return 0;
-    if (!t->used[ctx]) {
-      err = kErrCorrupt;
+    const uint32_t slot = x0 & (kM - 1);
+    int s = t->lut[ctx * 64 + (slot >> 6)];
+    if (s == 0xFF) {
+      err = kErrCorrupt;  // symbol decoded from an unused context
       return 0;
     }
-    uint32_t x = x0;
-    const uint32_t slot = x & (kM - 1);
-    const uint32_t st = lane < 17 ? (uint32_t)t->start[ctx * 17 + lane] : 0xFFFFu;
-    const unsigned bal = __ballot_sync(kFull, st <= slot);
-    const int s = __popc(bal) - 1;
-    const uint32_t s0 = __shfl_sync(kFull, st, s);
-    const uint32_t s1 = __shfl_sync(kFull, st, s + 1);
-    x = (s1 - s0) * (x >> kScaleBits) + slot - s0;
+    uint32_t w = t->sym[ctx * 16 + s];
+    while (slot >= (w & 0xFFFFu) + (w >> 16)) w = t->sym[ctx * 16 + (++s)];
+    uint32_t x = (w >> 16) * (x0 >> kScaleBits) + slot - (w & 0xFFFFu);
     while (x < kLower) {
       if (pos == 0) {
-        err = kErrCorrupt;
+        err = kErrCorrupt;  // stream underrun
         return 0;
       }
       pos--;
-      x = (x << 8) | (uint32_t)__ldg(buf + pos);
+      x = (x << 8) | b1;
+      b1 = b2;
+      b2 = byteAt(pos - 2);
     }
     x0 = x1;
     x1 = x2;
@@ -95,35 +125,32 @@ struct Chain {
     for (int i = 0; i < n; i++) v = v << 1 | (uint32_t)sym(ctxBypass);
     return v;
   }
-  __device__ __forceinline__ uint32_t classValue(int classCtx, int maxClass) {
+  // getClassValue — ebiv/mv.go:95-108
+  __device__ __forceinline__ uint32_t classValue(int classCtx) {
     const int cls = sym(classCtx);
-    if (cls < 0 || cls >= maxClass) {
-      if (!err) err = kErrCorrupt;
-      return 0;
-    }
-    if (cls == 0) return 0;
-    if (cls == 1) return 1;
+    if (cls <= 1) return (uint32_t)cls;
     return (1u << (cls - 1)) | rawBits(cls - 1);
   }
   __device__ __forceinline__ int mvComponent(int classCtx) {
-    const uint32_t u = classValue(classCtx, kNumMVClasses);
+    const uint32_t u = classValue(classCtx);
     return (int)(u >> 1) ^ -(int)(u & 1);
   }
 };
 
 // decodeBlock (ebiv/residual.go:79-126): writes the block's nonzero levels as
-// packed entries after a count word.  Returns the nonzero count.
-__device__ int entropyBlock(Chain& d, int plane, int txIdx, int n, uint32_t* region) {
-  // The scan follows the block size; txIdx only selects luma contexts.
-  const uint8_t* scan = cScan[n == 4 ? 0 : (n == 8 ? 1 : 2)];
+// packed entries after a count word; lane 0 stores.  Returns the count.
+__device__ __forceinline__ int entropyBlock(Chain& d, int plane, int txIdx, int n, uint32_t* region, int lane) {
+  const uint8_t* scan = cScan[n == 4 ? 0 : (n == 8 ? 1 : 2)];  // scan follows the block size
   const int total = n * n;
+  const int ctxBase = plane == kPlaneLuma ? ctxTokenBase + txIdx * kNumBands * kNumPrevClass
+                                          : ctxTokenBase + kLumaTokenCtx;
   int first = -1, last = -1, count = 0;
   int32_t sumAbs = 0;
   int prevClass = 0;
   uint32_t firstPos = 0;
   int32_t firstMag = 0;
   for (int i = 0; i < total; i++) {
-    const int t = d.sym(tokenCtx(plane, txIdx, bandOf(i), prevClass));
+    const int t = d.sym(ctxBase + bandOf(i) * kNumPrevClass + prevClass);
     if (t == tEOB) break;
     if (t == tZero) {
       prevClass = 0;
@@ -131,7 +158,7 @@ __device__ int entropyBlock(Chain& d, int plane, int txIdx, int n, uint32_t* reg
     }
     int mag;
     if (t == tEscape) {
-      mag = 5 + (int)d.classValue(ctxEscClass, kNumEscClasses);
+      mag = 5 + (int)d.classValue(ctxEscClass);
       prevClass = 2;
     } else {
       mag = t;
@@ -143,40 +170,21 @@ __device__ int entropyBlock(Chain& d, int plane, int txIdx, int n, uint32_t* reg
       first = i;
       firstPos = pos;
       firstMag = mag;
-      count++;  // slot 1 is reserved for the first coefficient
     } else {
       if (d.sym(ctxSign) == 1) mag = -mag;
-      if (d.lane == 0) region[1 + count] = pos | ((uint32_t)mag << 8);
-      count++;
+      if (lane == 0) region[1 + count] = pos | ((uint32_t)mag << 8);
     }
+    count++;
     last = i;
   }
   if (first >= 0) {
-    bool neg;
-    if (last - first >= kSDHMinSpan)
-      neg = (sumAbs & 1) == 1;
-    else
-      neg = d.sym(ctxSign) == 1;
-    const int32_t m = neg ? -firstMag : firstMag;
-    if (d.lane == 0) region[1] = firstPos | ((uint32_t)m << 8);
+    const bool neg = (last - first >= kSDHMinSpan) ? (sumAbs & 1) == 1 : d.sym(ctxSign) == 1;
+    if (lane == 0) region[1] = firstPos | ((uint32_t)(neg ? -firstMag : firstMag) << 8);
   }
-  if (d.lane == 0) region[0] = (uint32_t)count;
+  if (lane == 0) region[0] = (uint32_t)count;
   return count;
 }
 
-struct TileCtx {
-  Chain d;
-  const FrameDesc* f;
-  int bx0, bx1, by0, by1;  // tile bounds in macroblocks
-};
-
-__device__ __forceinline__ short2 loadMV(const FrameDesc& f, int idx) {
-  return reinterpret_cast<const short2*>(f.mvgrid)[idx];
-}
-__device__ __forceinline__ void storeMV(const FrameDesc& f, int idx, short2 v, int lane) {
-  if (lane == 0) reinterpret_cast<short2*>(f.mvgrid)[idx] = v;
-  __syncwarp();
-}
 __device__ __forceinline__ int16_t median3(int16_t a, int16_t b, int16_t c) {
   if (a > b) {
     const int16_t t = a;
@@ -187,267 +195,329 @@ __device__ __forceinline__ int16_t median3(int16_t a, int16_t b, int16_t c) {
   if (a > b) b = a;
   return b;
 }
-// predictMV — ebiv/mv.go:21-52
-__device__ short2 predictMV(const TileCtx& tc, int mbx, int mby) {
-  const FrameDesc& f = *tc.f;
-  const int stride = f.mbCols;
-  short2 a = make_short2(0, 0), bv = make_short2(0, 0), c = make_short2(0, 0);
-  const bool aOK = mbx > tc.bx0, bOK = mby > tc.by0;
-  bool cOK = false;
-  if (aOK) a = loadMV(f, mby * stride + mbx - 1);
-  if (bOK) {
-    bv = loadMV(f, (mby - 1) * stride + mbx);
-    if (mbx + 1 < tc.bx1) {
-      c = loadMV(f, (mby - 1) * stride + mbx + 1);
-      cOK = true;
-    } else if (aOK) {
-      c = loadMV(f, (mby - 1) * stride + mbx - 1);
-      cOK = true;
+__device__ __forceinline__ uint32_t packMV(int x, int y) { return (uint32_t)(uint16_t)x | ((uint32_t)(uint16_t)y << 16); }
+__device__ __forceinline__ int mvX(uint32_t v) { return (int16_t)(v & 0xFFFFu); }
+__device__ __forceinline__ int mvY(uint32_t v) { return (int16_t)(v >> 16); }
+
+// Tile context: bounds, neighbour rows, record staging.
+struct TileCtx {
+  Chain d;
+  int lane;
+  int x0, x1, y0, y1;  // tile bounds in macroblocks
+  int mbCols;
+  bool wide;           // rows live in global memory
+  WarpRows* rows;
+  uint32_t* gmv;       // wide-tile fallback: one packed vector per macroblock
+  int16_t* glv;        // wide-tile fallback: one level per macroblock
+
+  __device__ __forceinline__ uint32_t mvAt(int mbx, int mby) const {
+    return wide ? gmv[mby * mbCols + mbx] : rows->mv[(mby - y0) & 1][mbx - x0];
+  }
+  __device__ __forceinline__ int lvAt(int mbx, int mby) const {
+    return wide ? glv[mby * mbCols + mbx] : rows->lvl[(mby - y0) & 1][mbx - x0];
+  }
+  __device__ __forceinline__ void setMV(int mbx, int mby, uint32_t v, int lv) {
+    if (lane == 0) {
+      if (wide) {
+        gmv[mby * mbCols + mbx] = v;
+        glv[mby * mbCols + mbx] = (int16_t)lv;
+      } else {
+        rows->mv[(mby - y0) & 1][mbx - x0] = v;
+        rows->lvl[(mby - y0) & 1][mbx - x0] = (int16_t)lv;
+      }
     }
   }
-  if (!aOK && !bOK && !cOK) return make_short2(0, 0);
-  if (aOK && !bOK && !cOK) return a;
-  if (!aOK && bOK && !cOK) return bv;
-  return make_short2(median3(a.x, bv.x, c.x), median3(a.y, bv.y, c.y));
+  // predictMV — ebiv/mv.go:21-52 (neighbours within the tile)
+  __device__ __forceinline__ uint32_t predictMV(int mbx, int mby) const {
+    const bool aOK = mbx > x0, bOK = mby > y0;
+    uint32_t a = 0, bv = 0, c = 0;
+    bool cOK = false;
+    if (aOK) a = mvAt(mbx - 1, mby);
+    if (bOK) {
+      bv = mvAt(mbx, mby - 1);
+      if (mbx + 1 < x1) {
+        c = mvAt(mbx + 1, mby - 1);
+        cOK = true;
+      } else if (aOK) {
+        c = mvAt(mbx - 1, mby - 1);
+        cOK = true;
+      }
+    }
+    if (!aOK && !bOK && !cOK) return 0;
+    if (aOK && !bOK && !cOK) return a;
+    if (!aOK && bOK && !cOK) return bv;
+    return packMV(median3((int16_t)mvX(a), (int16_t)mvX(bv), (int16_t)mvX(c)),
+                  median3((int16_t)mvY(a), (int16_t)mvY(bv), (int16_t)mvY(c)));
+  }
+  // Intra dependency level of an intra macroblock at (mbx, mby).
+  __device__ __forceinline__ int intraLevel(int mbx, int mby) const {
+    int m = -1;
+    if (mbx > x0) m = max(m, lvAt(mbx - 1, mby));
+    if (mby > y0) {
+      m = max(m, lvAt(mbx, mby - 1));
+      if (mbx > x0) m = max(m, lvAt(mbx - 1, mby - 1));
+      if (mbx + 1 < x1) m = max(m, lvAt(mbx + 1, mby - 1));
+    }
+    return m + 1;
+  }
+};
+
+// Record words (see MBRec): 0 mode|ref<<8|part<<16|cbp<<24, 1 tx|cmode<<8,
+// 2-5 mv[0..3], 6-9 luma modes, 10 nzmask, 11 wmask.  Lane 0 writes fields
+// into the warp's staging copy; lanes 0-11 store it.
+__device__ __forceinline__ void recSet(TileCtx& tc, int word, uint32_t v) {
+  if (tc.lane == 0) tc.rows->rec[word] = v;
+}
+__device__ __forceinline__ void recOr(TileCtx& tc, int word, uint32_t v) {
+  if (tc.lane == 0) tc.rows->rec[word] |= v;
 }
 
-// Intra macroblock symbols (decodeLumaMB + decodeChromaMB).
-__device__ void entropyIntraMB(TileCtx& tc, MBRec& r, uint32_t* coef) {
+// The coded blocks of one macroblock, decoded by a single inlined block
+// decoder in bitstream order.  kind: 0 luma block preceded by its intra mode,
+// 1 luma block, 2 chroma Cb (preceded by the chroma intra mode when intra),
+// 3 chroma Cr.
+struct BlockList {
+  int count;
+  int tx;
+  bool intra;
+  uint8_t kind[18];
+};
+
+// Decodes the listed blocks; returns how many completed before an error and
+// the nonzero mask (bit k luma block k, 16 Cb, 17 Cr).
+__device__ __forceinline__ int entropyBlocks(TileCtx& tc, const BlockList& bl, uint32_t* coef, uint32_t* nzOut) {
   Chain& d = tc.d;
-  int tx = d.sym(ctxTxSize);
-  if (tx < 0 || tx >= 3) {
-    if (!d.err) d.err = kErrCorrupt;
-    tx = 0;
-  }
-  const int n = 4 << tx;
-  const int nb = 16 >> (2 * tx);
-  r.mode = kRecIntra;
-  r.tx = (uint8_t)tx;
+  const int n = 4 << bl.tx;
+  uint32_t nz = 0;
   int done = 0;
-  for (int k = 0; k < nb && !d.err; k++) {
-    const int mode = d.sym(ctxLumaMode);
-    r.lmode[k] = (uint8_t)mode;
-    const int cnt = entropyBlock(d, kPlaneLuma, tx, n, coef + k * (n * n + 1));
+  int luma = 0;
+  for (int e = 0; e < bl.count; e++) {
+    const int kind = bl.kind[e];
+    int plane = kPlaneLuma, bn = n, txi = bl.tx;
+    uint32_t* region;
+    uint32_t bit;
+    if (kind <= 1) {
+      if (kind == 0) recOr(tc, 6 + (luma >> 2), (uint32_t)d.sym(ctxLumaMode) << ((luma & 3) * 8));
+      region = coef + luma * (n * n + 1);
+      bit = 1u << luma;
+      luma++;
+    } else {
+      if (kind == 2 && bl.intra) recOr(tc, 1, (uint32_t)d.sym(ctxChromaMode) << 8);
+      plane = kPlaneChroma;
+      bn = 8;
+      txi = 0;
+      region = coef + (kind == 2 ? kCoefCb : kCoefCr);
+      bit = kind == 2 ? (1u << 16) : (1u << 17);
+    }
+    const int cnt = entropyBlock(d, plane, txi, bn, region, tc.lane);
     if (d.err) break;
-    if (cnt) r.nzmask |= 1u << k;
+    if (cnt) nz |= bit;
     done++;
   }
-  uint32_t w = (1u << done) - 1;
-  if (!d.err) {
-    r.cmode = (uint8_t)d.sym(ctxChromaMode);
-    int cnt = entropyBlock(d, kPlaneChroma, 0, 8, coef + kCoefCb);
-    if (!d.err) {
-      w |= 1u << 16;
-      if (cnt) r.nzmask |= 1u << 16;
-      cnt = entropyBlock(d, kPlaneChroma, 0, 8, coef + kCoefCr);
-      if (!d.err) {
-        w |= 1u << 17;
-        if (cnt) r.nzmask |= 1u << 17;
-      }
-    }
-  }
-  r.wmask = w;
+  *nzOut = nz;
+  return done;
 }
 
-// Inter-frame macroblock symbols (decodeInterMB + reconInterMB grammar).
-__device__ void entropyInterMB(TileCtx& tc, int mbx, int mby, MBRec& r, uint32_t* coef, int& intraCount) {
+// Intra macroblock symbols (decodeLumaMB + decodeChromaMB,
+// ebiv/decode_intra.go:137-187).  Returns the write mask.
+__device__ __forceinline__ uint32_t entropyIntraMB(TileCtx& tc, uint32_t* coef) {
   Chain& d = tc.d;
-  const FrameDesc& f = *tc.f;
-  const int idx = mby * f.mbCols + mbx;
+  int tx = d.sym(ctxTxSize);
+  if (tx >= 3) tx = 0;  // alphabet size 3: unreachable
+  const int nb = 16 >> (2 * tx);
+  BlockList bl;
+  bl.tx = tx;
+  bl.intra = true;
+  bl.count = nb + 2;
+  for (int k = 0; k < nb; k++) bl.kind[k] = 0;
+  bl.kind[nb] = 2;
+  bl.kind[nb + 1] = 3;
+  recSet(tc, 0, kRecIntra);
+  recSet(tc, 1, (uint32_t)tx);
+  uint32_t nz;
+  const int done = d.err ? 0 : entropyBlocks(tc, bl, coef, &nz);
+  if (d.err && done == 0) nz = 0;
+  recSet(tc, 10, nz);
+  uint32_t w = (1u << min(done, nb)) - 1;
+  if (done > nb) w |= 1u << 16;
+  if (done > nb + 1) w |= 1u << 17;
+  return w;
+}
+
+// Inter-frame macroblock symbols (decodeInterMB + reconInterMB grammar,
+// ebiv/decode_inter.go:8-118).  Returns the write mask.
+__device__ __forceinline__ uint32_t entropyInterMB(TileCtx& tc, int mbx, int mby, uint32_t* coef, bool* intra) {
+  Chain& d = tc.d;
   const int mode = d.sym(ctxMBMode);
   if (mode == mbSkip) {
-    const short2 p = predictMV(tc, mbx, mby);
-    storeMV(f, idx, p, d.lane);
-    r.mode = kRecSkip;
-    r.mv[0][0] = p.x;
-    r.mv[0][1] = p.y;
-    r.wmask = kWriteAll;
-    return;
+    const uint32_t p = tc.predictMV(mbx, mby);
+    tc.setMV(mbx, mby, p, -1);
+    recSet(tc, 0, kRecSkip);
+    recSet(tc, 2, p);
+    return kWriteAll;
   }
   if (mode == mbIntra) {
-    entropyIntraMB(tc, r, coef);
-    storeMV(f, idx, make_short2(0, 0), d.lane);
-    if (r.wmask) intraCount++;
-    return;
+    *intra = true;
+    return entropyIntraMB(tc, coef);  // the caller records the zero vector and level
   }
   if (mode != mbInter) {
-    if (!d.err) d.err = kErrCorrupt;
-    r.mode = kRecNone;
-    return;
+    d.err = kErrCorrupt;
+    return 0;
   }
   const int refSel = d.sym(ctxRef);
-  if (refSel < 0 || refSel >= kNumRefs) {
-    if (!d.err) d.err = kErrCorrupt;
-    r.mode = kRecNone;
-    return;
-  }
-  short2 pred = predictMV(tc, mbx, mby);
-  if (refSel == refGolden) pred = make_short2(0, 0);
-  const int part = d.sym(ctxPart);
-  if (part < 0 || part >= kNumPartModes) {
-    if (!d.err) d.err = kErrCorrupt;
-    r.mode = kRecNone;
-    return;
-  }
+  uint32_t pred = tc.predictMV(mbx, mby);
+  if (refSel == refGolden) pred = 0;
+  int part = d.sym(ctxPart);
+  if (part >= kNumPartModes) part = 0;  // alphabet size 4: unreachable
   const int np = part == partWhole ? 1 : (part == part8x8 ? 4 : 2);
+  uint32_t mv0 = 0;
   for (int i = 0; i < np; i++) {
-    const int ppx = i > 0 ? r.mv[0][0] : pred.x;
-    const int ppy = i > 0 ? r.mv[0][1] : pred.y;
+    const uint32_t pp = i > 0 ? mv0 : pred;
     const int dx = d.mvComponent(ctxMVClassX);
-    r.mv[i][0] = clampMV(ppx + dx);
+    const int vx = clampMV(mvX(pp) + dx);
     const int dy = d.mvComponent(ctxMVClassY);
-    r.mv[i][1] = clampMV(ppy + dy);
+    const int vy = clampMV(mvY(pp) + dy);
+    const uint32_t v = packMV(vx, vy);
+    if (i == 0) mv0 = v;
+    recSet(tc, 2 + i, v);
   }
-  if (d.err) {
-    r.mode = kRecNone;
-    return;
-  }
-  storeMV(f, idx, refSel == refGolden ? make_short2(0, 0) : make_short2(r.mv[0][0], r.mv[0][1]), d.lane);
-  r.mode = kRecInter;
-  r.ref = (uint8_t)refSel;
-  r.part = (uint8_t)part;
+  if (d.err) return 0;
+  tc.setMV(mbx, mby, refSel == refGolden ? 0u : mv0, -1);
   const int cbp = d.sym(ctxCBP);
-  if (cbp < 0 || cbp >= kNumCBP || d.err) {
-    if (!d.err) d.err = kErrCorrupt;
-    r.wmask = 0;
-    return;
-  }
-  r.cbp = (uint8_t)cbp;
-  uint32_t w = 0;
+  recSet(tc, 0, kRecInter | ((uint32_t)refSel << 8) | ((uint32_t)part << 16) | ((uint32_t)cbp << 24));
+  if (d.err) return 0;
+  BlockList bl;
+  bl.intra = false;
+  bl.tx = 0;
+  bl.count = 0;
+  int nb = 0;
   if (cbp & cbpLuma) {
     int tx = d.sym(ctxTxSize);
-    if (tx < 0 || tx >= 3) {
-      if (!d.err) d.err = kErrCorrupt;
-      tx = 0;
-    }
-    r.tx = (uint8_t)tx;
-    const int n = 4 << tx, nb = 16 >> (2 * tx);
-    int done = 0;
-    for (int k = 0; k < nb && !d.err; k++) {
-      const int cnt = entropyBlock(d, kPlaneLuma, tx, n, coef + k * (n * n + 1));
-      if (d.err) break;
-      if (cnt) r.nzmask |= 1u << k;
-      done++;
-    }
-    if (d.err) {
-      r.wmask = (1u << done) - 1;
-      return;
-    }
-    w = 0xFFFFu;
-  } else {
-    w = 0xFFFFu;  // motion-compensated luma, written directly
+    if (tx >= 3) tx = 0;
+    if (d.err) return 0;
+    recSet(tc, 1, (uint32_t)tx);
+    bl.tx = tx;
+    nb = 16 >> (2 * tx);
+    for (int k = 0; k < nb; k++) bl.kind[bl.count++] = 1;
   }
-  if (cbp & cbpCb) {
-    const int cnt = entropyBlock(d, kPlaneChroma, 0, 8, coef + kCoefCb);
-    if (!d.err) {
-      w |= 1u << 16;
-      if (cnt) r.nzmask |= 1u << 16;
-    }
-  } else {
-    w |= 1u << 16;
-  }
-  if (cbp & cbpCr) {
-    if (!d.err) {
-      const int cnt = entropyBlock(d, kPlaneChroma, 0, 8, coef + kCoefCr);
-      if (!d.err) {
-        w |= 1u << 17;
-        if (cnt) r.nzmask |= 1u << 17;
-      }
-    }
-  } else {
-    w |= 1u << 17;
-  }
-  r.wmask = w;
-}
-
-__device__ __forceinline__ void storeRec(MBRec* dst, const MBRec& r, int lane) {
-  const uint32_t* s = reinterpret_cast<const uint32_t*>(&r);
-  uint32_t* o = reinterpret_cast<uint32_t*>(dst);
-  if (lane < 12) o[lane] = s[lane];
+  const int cbEntry = (cbp & cbpCb) ? bl.count : -1;
+  if (cbp & cbpCb) bl.kind[bl.count++] = 2;
+  const int crEntry = (cbp & cbpCr) ? bl.count : -1;
+  if (cbp & cbpCr) bl.kind[bl.count++] = 3;
+  uint32_t nz = 0;
+  const int done = entropyBlocks(tc, bl, coef, &nz);
+  recSet(tc, 10, nz);
+  if (done < nb) return (1u << done) - 1;  // a coded luma block failed: nothing else is written
+  uint32_t w = 0xFFFFu;                    // coded luma complete, or motion-compensated luma
+  if (cbEntry < 0 || done > cbEntry) w |= 1u << 16;
+  if (crEntry < 0 || done > crEntry) w |= 1u << 17;
+  return w;
 }
 
 constexpr int kEntropyWarps = 4;
 
 __global__ void __launch_bounds__(32 * kEntropyWarps) kEntropy(const FrameDesc* frames, const int2* jobs, int njobs) {
   __shared__ WarpTables sT[kEntropyWarps];
+  __shared__ WarpRows sR[kEntropyWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int j = blockIdx.x * kEntropyWarps + warp;
   if (j >= njobs) return;
-  const FrameDesc& f = frames[jobs[j].x];
-  if (f.gate && *f.gate) return;
+  const FrameDesc* fp = frames + jobs[j].x;
   const int tile = jobs[j].y;
-  WarpTables& T = sT[warp];
-  {
-    const uint16_t* src = &f.tables->start[0][0];
-    for (int i = lane; i < kNumContexts * 17; i += 32) T.start[i] = src[i];
-    for (int i = lane; i < kNumContexts; i += 32) T.used[i] = f.tables->used[i];
-  }
-  __syncwarp();
-  const TileRange tr = f.tiles[tile];
+  // Descriptor fields into registers: the kernel's global stores cannot alias them then.
+  const int mbCols = fp->mbCols;
+  const int inter = fp->inter;
+  MBRec* const recs = fp->mbrec;
+  uint32_t* const coefBase = fp->coef;
+  uint32_t* const intraList = fp->intraList;
+  TileStat* const tstat = fp->tileStat;
+  int32_t* const status = fp->status;
+  const TileRange tr = fp->tiles[tile];
+  buildWarpTables(sT[warp], *fp->tables, lane);
+
   TileCtx tc;
-  tc.f = &f;
-  tc.bx0 = tr.mbX0;
-  tc.bx1 = tr.mbX1;
-  tc.by0 = tr.mbY0;
-  tc.by1 = tr.mbY1;
+  tc.lane = lane;
+  tc.x0 = tr.mbX0;
+  tc.x1 = tr.mbX1;
+  tc.y0 = tr.mbY0;
+  tc.y1 = tr.mbY1;
+  tc.mbCols = mbCols;
+  tc.rows = &sR[warp];
+  tc.wide = (tc.x1 - tc.x0) > kRowMax;
+  tc.gmv = reinterpret_cast<uint32_t*>(fp->mvgrid);
+  tc.glv = fp->lvgrid;
   Chain& d = tc.d;
-  d.buf = f.pkt + tr.offset;
+  d.buf = fp->pkt + tr.offset;
   d.pos = (int32_t)tr.length;
   d.err = 0;
-  d.t = &T;
-  d.lane = lane;
-  const int tw = tc.bx1 - tc.bx0;
-  const int total = tw * (tc.by1 - tc.by0);
-  int done = 0;
-  int intraCount = 0;
+  d.t = &sT[warp];
+  const int tw = tc.x1 - tc.x0;
+  const int total = tw * (tc.y1 - tc.y0);
+  int done = 0, intraCount = 0, maxLevel = -1;
   if (tr.length < (uint32_t)(kStates * 4)) {
-    d.err = kErrCorrupt;
+    d.err = kErrCorrupt;  // tile stream too short to initialise rANS
   } else {
     uint32_t st[4];
+#pragma unroll
     for (int i = kStates - 1; i >= 0; i--) {
-      const uint32_t a = __ldg(d.buf + d.pos - 1), b = __ldg(d.buf + d.pos - 2), c = __ldg(d.buf + d.pos - 3),
-                     e = __ldg(d.buf + d.pos - 4);
+      st[i] = d.byteAt(d.pos - 1) << 24 | d.byteAt(d.pos - 2) << 16 | d.byteAt(d.pos - 3) << 8 | d.byteAt(d.pos - 4);
       d.pos -= 4;
-      st[i] = a << 24 | b << 16 | c << 8 | e;
     }
     d.x0 = st[0];
     d.x1 = st[1];
     d.x2 = st[2];
     d.x3 = st[3];
+    d.b1 = d.byteAt(d.pos - 1);
+    d.b2 = d.byteAt(d.pos - 2);
+    int mbx = tc.x0, mby = tc.y0;
     for (; done < total; done++) {
-      const int mbx = tc.bx0 + done % tw, mby = tc.by0 + done / tw;
-      const int idx = mby * f.mbCols + mbx;
-      MBRec r;
-      {
-        uint32_t* z = reinterpret_cast<uint32_t*>(&r);
-#pragma unroll
-        for (int k = 0; k < 12; k++) z[k] = 0;
-      }
-      uint32_t* coef = f.coef + (size_t)idx * kCoefPerMB;
-      if (f.inter) {
-        entropyInterMB(tc, mbx, mby, r, coef, intraCount);
+      const int idx = mby * mbCols + mbx;
+      if (lane < 12) tc.rows->rec[lane] = 0;
+      __syncwarp();
+      uint32_t* coef = coefBase + (size_t)idx * kCoefPerMB;
+      bool intra = !inter;
+      uint32_t w;
+      if (inter) {
+        w = entropyInterMB(tc, mbx, mby, coef, &intra);
       } else {
-        entropyIntraMB(tc, r, coef);
-        if (r.wmask) intraCount++;
+        w = entropyIntraMB(tc, coef);
       }
-      storeRec(f.mbrec + idx, r, lane);
+      if (intra) {
+        const int lv = tc.intraLevel(mbx, mby);
+        tc.setMV(mbx, mby, 0u, w ? lv : -1);
+        if (w) {
+          if (lane == 0) intraList[tr.mbBase + intraCount] = (uint32_t)idx | ((uint32_t)lv << kLevelShift);
+          intraCount++;
+          maxLevel = max(maxLevel, lv);
+        }
+      }
+      recSet(tc, 11, w);
+      __syncwarp();
+      if (lane < 12) reinterpret_cast<uint32_t*>(recs + idx)[lane] = tc.rows->rec[lane];
       if (d.err) {
         done++;
         break;
+      }
+      if (++mbx == tc.x1) {
+        mbx = tc.x0;
+        mby++;
       }
     }
   }
   // Macroblocks the tile never reached are left untouched by reconstruction.
   for (int k = done + lane; k < total; k += 32) {
-    const int mbx = tc.bx0 + k % tw, mby = tc.by0 + k / tw;
-    MBRec* r = f.mbrec + (size_t)mby * f.mbCols + mbx;
+    MBRec* r = recs + (size_t)(tc.y0 + k / tw) * mbCols + tc.x0 + k % tw;
     r->mode = kRecNone;
     r->wmask = 0;
   }
   if (lane == 0) {
-    f.tileStat[tile].err = d.err;
-    f.tileStat[tile].intraCount = intraCount;
-    if (d.err) atomicExch(f.status, kErrCorrupt);
+    TileStat ts;
+    ts.err = d.err;
+    ts.intraCount = intraCount;
+    ts.maxLevel = maxLevel;
+    ts.pad = 0;
+    tstat[tile] = ts;
+    if (d.err) atomicExch(status, kErrCorrupt);
   }
 }
 
@@ -544,7 +614,11 @@ __global__ void __launch_bounds__(32 * kInterWarps) kInterRecon(const FrameDesc*
   __shared__ InterScratch sS[kInterWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const FrameDesc& f = frames[blockIdx.y];
-  if (!f.inter || (f.gate && *f.gate)) return;
+  if (f.gate && *f.gate) {
+    if (threadIdx.x == 0) atomicExch(f.status, kSkipped);
+    return;
+  }
+  if (!f.inter) return;
   const int idx = blockIdx.x * kInterWarps + warp;
   if (idx >= f.mbCols * f.mbRows) return;
   const MBRec& r = f.mbrec[idx];
@@ -751,27 +825,77 @@ __device__ void intraMB(const FrameDesc& f, IntraScratch& S, int mbx, int mby, i
   }
 }
 
+constexpr int kLevelBuckets = 2048;
+
+// One CTA per tile.  The tile's intra macroblocks (listed by the entropy
+// stage with their dependency levels) are counting-sorted by level, then each
+// level is reconstructed in parallel with a CTA barrier between levels.  Key
+// frames get the classic wavefront (level = x + 2y); inter frames with a few
+// isolated intra macroblocks take one or two levels.
 __global__ void __launch_bounds__(32 * kIntraWarps) kIntraRecon(const FrameDesc* frames, const int2* jobs, int njobs) {
   __shared__ IntraScratch sS[kIntraWarps];
+  __shared__ int sStart[kLevelBuckets + 1];
+  __shared__ int sCur[kLevelBuckets];
   const int j = blockIdx.x;
   if (j >= njobs) return;
   const FrameDesc& f = frames[jobs[j].x];
-  if (f.gate && *f.gate) return;
+  if (f.gate && *f.gate) {
+    if (threadIdx.x == 0) atomicExch(f.status, kSkipped);
+    return;
+  }
   const int tile = jobs[j].y;
-  if (f.tileStat[tile].intraCount == 0) return;
+  const TileStat ts = f.tileStat[tile];
+  const int n = ts.intraCount;
+  if (n == 0) return;
   const TileRange tr = f.tiles[tile];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tw = tr.mbX1 - tr.mbX0, th = tr.mbY1 - tr.mbY0;
-  const int waves = tw + 2 * (th - 1);
-  for (int t = 0; t < waves; t++) {
-    // Macroblocks (x, y) of the tile with x + 2y == t.
-    int ylo = t - (tw - 1) > 0 ? (t - (tw - 1) + 1) / 2 : 0;
-    int yhi = t / 2 < th - 1 ? t / 2 : th - 1;
-    for (int y = ylo + warp; y <= yhi; y += kIntraWarps) {
-      const int x = t - 2 * y;
-      intraMB(f, sS[warp], tr.mbX0 + x, tr.mbY0 + y, tr.mbX0, tr.mbX1, tr.mbY0, lane);
+  const int L = ts.maxLevel + 1;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, tid = threadIdx.x;
+  const uint32_t* list = f.intraList + tr.mbBase;
+  uint32_t* sorted = f.intraSorted + tr.mbBase;
+  auto runMB = [&](uint32_t e) {
+    const int idx = (int)(e & kIndexMask);
+    intraMB(f, sS[warp], idx % f.mbCols, idx / f.mbCols, tr.mbX0, tr.mbX1, tr.mbY0, lane);
+  };
+  if (L <= kLevelBuckets) {
+    for (int l = tid; l <= L; l += blockDim.x) sStart[l] = 0;
+    __syncthreads();
+    for (int i = tid; i < n; i += blockDim.x) atomicAdd(&sStart[(list[i] >> kLevelShift) + 1], 1);
+    __syncthreads();
+    if (warp == 0) {  // inclusive scan of counts -> exclusive level starts
+      const int per = (L + 1 + 31) / 32;
+      const int b = lane * per, e = min(b + per, L + 1);
+      int run = 0;
+      for (int l = b; l < e; l++) run += sStart[l];
+      int incl = run;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += v;
+      }
+      int acc = incl - run;
+      for (int l = b; l < e; l++) {
+        acc += sStart[l];
+        sStart[l] = acc;
+      }
     }
     __syncthreads();
+    for (int l = tid; l < L; l += blockDim.x) sCur[l] = sStart[l];
+    __syncthreads();
+    for (int i = tid; i < n; i += blockDim.x) {
+      const uint32_t e = list[i];
+      sorted[atomicAdd(&sCur[e >> kLevelShift], 1)] = e;
+    }
+    __syncthreads();
+    for (int l = 0; l < L; l++) {
+      for (int k = sStart[l] + warp; k < sStart[l + 1]; k += kIntraWarps) runMB(sorted[k]);
+      __syncthreads();
+    }
+  } else {
+    // Very wide or tall tiles: scan the list once per level.
+    for (int l = 0; l < L; l++) {
+      for (int i = warp; i < n; i += kIntraWarps)
+        if ((int)(list[i] >> kLevelShift) == l) runMB(list[i]);
+      __syncthreads();
+    }
   }
 }
 

@@ -201,30 +201,41 @@ std::vector<uint8_t> serializeTables(const std::vector<Freqs>& freqs, const std:
 // ---------------------------------------------------------------------------
 // Transforms and quantization (ebiv/transform.go:44-194, ebiv/quant.go)
 // ---------------------------------------------------------------------------
+// forwardDCT — ebiv/transform.go:44-79.  Encoder inputs are residuals of
+// two bytes (|v| <= 255), so both passes fit in int32 exactly: the column
+// sums stay below 255 * 46341 and the row sums below 1443 * 46341.
+template <int N>
+void forwardDCTN(const int32_t* src, int32_t* dst) {
+  const int32_t* c = codingTables().dct[N == 4 ? 0 : (N == 8 ? 1 : 2)];
+  int32_t acc[N * N];
+  int32_t tmp[N * N];
+  for (int k = 0; k < N * N; k++) acc[k] = 0;
+  for (int i = 0; i < N; i++) {
+    const int32_t* srow = src + i * N;
+    for (int k = 0; k < N; k++) {
+      const int32_t cki = c[k * N + i];
+      int32_t* arow = acc + k * N;
+      for (int j = 0; j < N; j++) arow[j] += cki * srow[j];
+    }
+  }
+  for (int k = 0; k < N * N; k++) tmp[k] = (acc[k] + 4096) >> 13;
+  for (int k = 0; k < N; k++) {
+    const int32_t* trow = tmp + k * N;
+    for (int l = 0; l < N; l++) {
+      const int32_t* crow = c + l * N;
+      int32_t a = 0;
+      for (int j = 0; j < N; j++) a += crow[j] * trow[j];
+      dst[k * N + l] = (a + 4096) >> 13;
+    }
+  }
+}
 void forwardDCT(const int32_t* src, int32_t* dst, int n) {
-  const int32_t* c = codingTables().dct[txIndexOf(n)];
-  const int64_t round = 1LL << 12;
-  int64_t acc[kMaxLevels];
-  int32_t tmp[kMaxLevels];
-  std::memset(acc, 0, sizeof(int64_t) * n * n);
-  for (int i = 0; i < n; i++) {
-    const int32_t* srow = src + i * n;
-    for (int k = 0; k < n; k++) {
-      const int64_t cki = c[k * n + i];
-      int64_t* arow = acc + k * n;
-      for (int j = 0; j < n; j++) arow[j] += cki * (int64_t)srow[j];
-    }
-  }
-  for (int k = 0; k < n * n; k++) tmp[k] = (int32_t)((acc[k] + round) >> 13);
-  for (int k = 0; k < n; k++) {
-    const int32_t* trow = tmp + k * n;
-    for (int l = 0; l < n; l++) {
-      const int32_t* crow = c + l * n;
-      int64_t a = 0;
-      for (int j = 0; j < n; j++) a += (int64_t)crow[j] * (int64_t)trow[j];
-      dst[k * n + l] = (int32_t)((a + round) >> 13);
-    }
-  }
+  if (n == 4)
+    forwardDCTN<4>(src, dst);
+  else if (n == 8)
+    forwardDCTN<8>(src, dst);
+  else
+    forwardDCTN<16>(src, dst);
 }
 
 void inverseDCT(const int32_t* src, int32_t* dst, int n) {
@@ -262,24 +273,43 @@ void inverseDCT(const int32_t* src, int32_t* dst, int n) {
     }
 }
 
-void fwht(int32_t* a, int n, int step) {
-  for (int span = 1; span < n; span <<= 1)
-    for (int i = 0; i < n; i += span << 1)
-      for (int j = i; j < i + span; j++) {
-        const int32_t x = a[j * step], y = a[(j + span) * step];
-        a[j * step] = x + y;
-        a[(j + span) * step] = x - y;
-      }
+// satd / fwht — ebiv/transform.go:86-119, unrolled per block size.
+template <int N>
+inline void fwhtRows(int32_t* t) {
+  for (int r = 0; r < N; r++) {
+    int32_t* a = t + r * N;
+    for (int span = 1; span < N; span <<= 1)
+      for (int i = 0; i < N; i += span << 1)
+        for (int j = i; j < i + span; j++) {
+          const int32_t x = a[j], y = a[j + span];
+          a[j] = x + y;
+          a[j + span] = x - y;
+        }
+  }
 }
-// satd — ebiv/transform.go:86-107
-int64_t satd(const int32_t* residual, int n) {
-  int32_t t[kMaxLevels];
-  std::memcpy(t, residual, sizeof(int32_t) * n * n);
-  for (int r = 0; r < n; r++) fwht(t + r * n, n, 1);
-  for (int c = 0; c < n; c++) fwht(t + c, n, n);
+template <int N>
+int64_t satdN(const int32_t* residual) {
+  int32_t t[N * N];
+  for (int i = 0; i < N * N; i++) t[i] = residual[i];
+  fwhtRows<N>(t);
+  // Columns: the same butterflies applied to whole rows at once.
+  for (int span = 1; span < N; span <<= 1)
+    for (int i = 0; i < N; i += span << 1)
+      for (int j = i; j < i + span; j++) {
+        int32_t* x = t + j * N;
+        int32_t* y = t + (j + span) * N;
+        for (int c = 0; c < N; c++) {
+          const int32_t a = x[c], b = y[c];
+          x[c] = a + b;
+          y[c] = a - b;
+        }
+      }
   int64_t s = 0;
-  for (int i = 0; i < n * n; i++) s += t[i] < 0 ? -(int64_t)t[i] : t[i];
+  for (int i = 0; i < N * N; i++) s += t[i] < 0 ? -(int64_t)t[i] : t[i];
   return s;
+}
+int64_t satd(const int32_t* residual, int n) {
+  return n == 4 ? satdN<4>(residual) : (n == 8 ? satdN<8>(residual) : satdN<16>(residual));
 }
 
 using CostModel = std::vector<std::vector<double>>;
@@ -630,15 +660,15 @@ void mcLuma(const Plane& r, int srcX, int srcY, int fx, int fy, int pw, int ph, 
       for (int x = 0; x < pw; x++)
         o[x] = clampByte((t[0] * s[x - st] + t[1] * s[x] + t[2] * s[x + st] + t[3] * s[x + 2 * st] + 32) >> 6);
     } else {
+      // Separable: four horizontally filtered rows, then the vertical taps.
       const int32_t *tx = kTaps[fx], *ty = kTaps[fy];
-      for (int x = 0; x < pw; x++) {
-        int32_t acc = 0;
-        for (int k = 0; k < 4; k++) {
-          const uint8_t* q = s + (k - 1) * st + x;
-          acc += ty[k] * (tx[0] * q[-1] + tx[1] * q[0] + tx[2] * q[1] + tx[3] * q[2]);
-        }
-        o[x] = clampByte((acc + 2048) >> 12);
+      int32_t h[4][16];
+      for (int k = 0; k < 4; k++) {
+        const uint8_t* q = s + (k - 1) * st;
+        for (int x = 0; x < pw; x++) h[k][x] = tx[0] * q[x - 1] + tx[1] * q[x] + tx[2] * q[x + 1] + tx[3] * q[x + 2];
       }
+      for (int x = 0; x < pw; x++)
+        o[x] = clampByte((ty[0] * h[0][x] + ty[1] * h[1][x] + ty[2] * h[2][x] + ty[3] * h[3][x] + 2048) >> 12);
     }
   }
 }

@@ -54,6 +54,11 @@ class Engine {
   int addResidentStream(const uint8_t* const* pkts, const size_t* lens, int n, int ring, int* id);
   // A stream fed one packet per round through submit().
   int addStreamingStream(int ring, int* id);
+  // Frames per resident stream decoded per round (entropy of all of them in
+  // one launch, reconstruction in dependency order).  Set before the streams
+  // see their first key frame.
+  int setLookahead(int k);
+  int lookahead() const { return lookahead_; }
   int submit(int id, const uint8_t* pkt, size_t n);
   // Rewinds a resident stream to packet `index` (the caller seeks to a key
   // frame); Flush semantics: only the output cursor resets.
@@ -76,7 +81,7 @@ class Engine {
   int64_t launches() const { return launches_; }
   size_t deviceBytes() const { return deviceBytes_; }
   // Per-stream HBM footprint (pool + scratch) for a geometry.
-  static size_t footprint(int w, int h, int ring);
+  static size_t footprint(int w, int h, int ring, int lookahead);
 
   // Kernel-time accounting: CUDA events recorded around each round's
   // kernels on the engine's stream.
@@ -90,8 +95,7 @@ class Engine {
   struct Stream;
   struct Job;
   int configure(Stream& s, int w, int h);
-  int takeFree(Stream& s);
-  int planFrame(Stream& s, Job& j, std::vector<RoundResult>* results);
+  int planFrame(Stream& s, Job& j, std::vector<char>& busy);
   void finishFrame(Stream& s, Job& j, const int32_t* statuses, std::vector<RoundResult>* results);
   int ensureStage(size_t bytes);
 
@@ -102,6 +106,7 @@ class Engine {
   uint8_t* hStage_ = nullptr;
   size_t stageCap_ = 0;
   int64_t launches_ = 0;
+  int lookahead_ = 1;
   size_t deviceBytes_ = 0;
   bool timing_ = false;
   cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};

@@ -45,8 +45,20 @@ constexpr uint32_t kWriteAll = 0x3FFFFu;
 
 struct TileStat {
   int32_t err;         // 0 or an ebiv status
-  int32_t intraCount;  // intra macroblocks decoded in this tile
+  int32_t intraCount;  // intra macroblocks reconstructed in this tile
+  int32_t maxLevel;    // highest intra dependency level in this tile
+  int32_t pad;
 };
+
+// Intra dependency levels: an intra macroblock's level is one more than the
+// highest level among its intra neighbours (left, above-left, above,
+// above-right within the tile; ebiv/predict.go:50-129), so every macroblock
+// of one level can be reconstructed in parallel once the lower levels are
+// done.  List entries pack the frame macroblock index (bits 0-17) and the
+// level (bits 18-28).
+constexpr int32_t kSkipped = 1000;
+constexpr int kLevelShift = 18;
+constexpr uint32_t kIndexMask = (1u << kLevelShift) - 1;
 
 struct FrameDesc {
   // Planes (padded).  ref/gold may alias rec's siblings; never rec itself.
@@ -65,10 +77,16 @@ struct FrameDesc {
   const TileRange* tiles;
   MBRec* mbrec;
   uint32_t* coef;
-  int16_t* mvgrid;
+  int16_t* mvgrid;      // 2 x int16 per macroblock (wide-tile fallback rows)
+  int16_t* lvgrid;      // 1 x int16 per macroblock (wide-tile fallback rows)
+  uint32_t* intraList;  // per tile at mbBase: intra macroblocks, raster order
+  uint32_t* intraSorted;// per tile at mbBase: the same grouped by level
   TileStat* tileStat;
   int32_t* status;      // frame status, written by the commit step
-  const int32_t* gate;  // when set and nonzero, this job is skipped
+  // Status of the frame this one depends on (the previous frame of the
+  // stream decoded in the same round).  When it is nonzero the reconstruction
+  // kernels skip this frame and mark it kSkipped; the host re-plans it.
+  const int32_t* gate;
 };
 
 }  // namespace ebiv

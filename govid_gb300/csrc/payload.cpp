@@ -118,15 +118,19 @@ int planPayload(const uint8_t* base, size_t bodyOffset, size_t len, bool key, in
     r.offset = (uint32_t)(bodyOffset + pos);
     r.length = (uint32_t)tl;
     r.mbX0 = r.mbX1 = r.mbY0 = r.mbY1 = 0;
+    r.mbBase = 0;
     plan->tiles.push_back(r);
     pos += (size_t)tl;
   }
   // decodeCoded's grid check — ebiv/decode_intra.go:60-63
   const TileGrid grid(mbCols, mbRows, (int)cols, (int)rows);
   if ((uint64_t)grid.count() != plan->tiles.size()) return kErrCorrupt;
+  uint32_t base = 0;
   for (int i = 0; i < grid.count(); i++) {
     int x0, x1, y0, y1;
     grid.bounds(i, &x0, &x1, &y0, &y1);
+    plan->tiles[(size_t)i].mbBase = base;
+    base += (uint32_t)((x1 - x0) * (y1 - y0));
     plan->tiles[(size_t)i].mbX0 = (uint16_t)x0;
     plan->tiles[(size_t)i].mbX1 = (uint16_t)x1;
     plan->tiles[(size_t)i].mbY0 = (uint16_t)y0;

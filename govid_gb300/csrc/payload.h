@@ -37,6 +37,7 @@ struct TileRange {
   uint32_t offset;  // byte offset within the packet
   uint32_t length;
   uint16_t mbX0, mbX1, mbY0, mbY1;
+  uint32_t mbBase;  // macroblocks in the tiles before this one (tile order)
 };
 
 struct PayloadPlan {

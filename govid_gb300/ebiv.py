@@ -206,11 +206,13 @@ class Batch:
     """Many independent EBIV streams decoded together: each round decodes the
     next packet of every active stream with one set of kernel launches."""
 
-    def __init__(self):
+    def __init__(self, lookahead: int = 1):
         L = _native.lib()
         h = C.c_void_p()
         _check(L.ebivgpu_batch_create(C.byref(h)), "batch")
         self._h, self._L = h, L
+        if lookahead != 1:
+            _check(L.ebivgpu_batch_set_lookahead(h, int(lookahead)), "lookahead")
 
     def add_stream(self, packets: list[bytes], ring: int = 3) -> int:
         n = len(packets)
@@ -289,8 +291,8 @@ class Batch:
             pass
 
 
-def stream_footprint(width: int, height: int, ring: int = 3) -> int:
-    return int(_native.lib().ebivgpu_stream_footprint(width, height, ring))
+def stream_footprint(width: int, height: int, ring: int = 3, lookahead: int = 1) -> int:
+    return int(_native.lib().ebivgpu_stream_footprint(width, height, ring, lookahead))
 
 
 # ---------------------------------------------------------------------------

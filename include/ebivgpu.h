@@ -110,10 +110,15 @@ int ebivgpu_batch_result_planes(ebivgpu_batch* b, int i, ebivgpu_plane_view* out
 int ebivgpu_batch_result_download(ebivgpu_batch* b, int i, uint8_t* packed, size_t cap);
 /* enable: 1 on (resets counters), 0 off, -1 read only. */
 int ebivgpu_batch_timing(ebivgpu_batch* b, int enable, double* kernel_ms, double* entropy_ms, double* recon_ms);
+/* Frames per resident stream per round (default 1).  Entropy decoding of
+ * later frames needs no pixels of earlier ones, so a round decodes all their
+ * tiles in one launch and reconstructs the frames in order.  Set it before
+ * adding streams. */
+int ebivgpu_batch_set_lookahead(ebivgpu_batch* b, int frames);
 int64_t ebivgpu_batch_launches(ebivgpu_batch* b);
 uint64_t ebivgpu_batch_device_bytes(ebivgpu_batch* b);
 /* HBM bytes one stream of this geometry holds (frame pool + scratch). */
-uint64_t ebivgpu_stream_footprint(int width, int height, int ring);
+uint64_t ebivgpu_stream_footprint(int width, int height, int ring, int lookahead);
 /* Non-zero when a CUDA device is usable from this process. */
 int ebivgpu_device_available(void);
 

@@ -26,9 +26,10 @@ def _streams():
     return out
 
 
-def test_batch_matches_oracle(gpu_required):
+@pytest.mark.parametrize("lookahead", [1, 4])
+def test_batch_matches_oracle(gpu_required, lookahead):
     streams = _streams()
-    b = ebiv.Batch()
+    b = ebiv.Batch(lookahead=lookahead)
     want, ids, dims = {}, [], {}
     for cont, w, h in streams:
         pkts = [p.data for p in ebiv.Reader(cont).packets()]
@@ -87,3 +88,91 @@ def test_batch_seek_replays_exactly(gpu_required):
         (r,) = b.round()
         assert r.frame_index == i and r.status == 0
         assert b.download(r, 160, 96) == want[i][1]
+
+
+def _zero_tile(pkt: bytes, tile: int) -> bytes:
+    """Zeroes one tile's rANS bytes: the decoder underruns inside that tile."""
+    from govid_gb300 import ebiv as E
+
+    hdr = E.parse_frame_header(pkt)
+    b = bytearray(pkt)
+    pos = hdr["body_offset"] + 1  # skip qp
+
+    def uvar(p):
+        x, s = 0, 0
+        while True:
+            c = b[p]
+            x |= (c & 0x7F) << s
+            p += 1
+            if c < 0x80:
+                return x, p
+            s += 7
+
+    _, pos = uvar(pos)  # tile cols
+    _, pos = uvar(pos)  # tile rows
+    tl, pos = uvar(pos)
+    pos += tl  # tables
+    for t in range(tile + 1):
+        n, pos = uvar(pos)
+        if t == tile:
+            b[pos:pos + n] = bytes(n)
+        pos += n
+    return bytes(b)
+
+
+@pytest.mark.parametrize("lookahead", [1, 4])
+def test_batch_error_mid_chain_matches_oracle(gpu_required, lookahead):
+    # A frame that fails on the GPU leaves its references untouched
+    # (ebiv/codec.go:174-191); later frames of the same round are re-planned.
+    spec = ebiv.SceneSpec(width=160, height=96, seed=21, sprites=3)
+    cont = ebiv.encode_scene(spec, 12, qp=22, gop=12, tiles=(2, 1), fast=True)
+    pkts = [p.data for p in ebiv.Reader(cont).packets()]
+    pkts[3] = _zero_tile(pkts[3], 1)
+    pkts[8] = _zero_tile(pkts[8], 0)
+    want = ebiv_oracle.decode_all(pkts)
+    assert want[3][0] == ebiv.ErrCorrupt.status and want[8][0] == ebiv.ErrCorrupt.status
+    b = ebiv.Batch(lookahead=lookahead)
+    b.add_stream(pkts)
+    got = {}
+    while True:
+        res = b.round()
+        if not res:
+            break
+        for r in res:
+            got[r.frame_index] = (r.status, b.download(r, 160, 96) if r.status == 0 else None)
+    assert sorted(got) == list(range(len(pkts)))
+    for i, (ws, wp) in enumerate(want):
+        assert got[i][0] == ws, f"frame {i}: status {got[i][0]} vs oracle {ws}"
+        assert got[i][1] == wp, f"frame {i} differs from the oracle"
+
+
+def test_fuzzed_packets_match_oracle(gpu_required):
+    # FuzzDecodePacket-style (ebiv/fuzz_test.go): seeded byte flips in the
+    # seed clip's packets; statuses and every decoded plane match the oracle.
+    import random
+
+    from helpers import encode_gen
+
+    cont, _, _ = encode_gen(64, 48, 6, lambda w, h, i: ebiv.synth_frame(w, h, 1 if i < 3 else 2), intra=20, gop=4,
+                            altref=4, fast=True, keep_recon=False)
+    clean = [p.data for p in ebiv.Reader(cont).packets()]
+    rng = random.Random(1234)
+    for case in range(24):
+        pkts = []
+        for p in clean:
+            b = bytearray(p)
+            for _ in range(rng.randint(0, 3)):
+                i = rng.randrange(len(b))
+                b[i] ^= 1 << rng.randrange(8)
+            if rng.random() < 0.1:
+                b = b[: rng.randrange(1, len(b) + 1)]
+            pkts.append(bytes(b))
+        want = ebiv_oracle.decode_all(pkts)
+        c = ebiv.Codec()
+        for i, p in enumerate(pkts):
+            try:
+                g = (0, c.decode(p).packed())
+            except ebiv.EbivError as e:
+                g = (e.status, None)
+            assert g[0] == want[i][0], f"case {case} frame {i}: status {g[0]} vs oracle {want[i][0]}"
+            assert g[1] == want[i][1], f"case {case} frame {i}: planes differ from the oracle"
