@@ -1754,4 +1754,49 @@ int Encoder::close() {
   return kOK;
 }
 
+
+// Encodes one block of levels the way the encoder codes a residual block:
+// sign-data hiding (ebiv/residual.go:134-180), the token grammar
+// (ebiv/residual.go:30-75), per-context tables normalized from the block's
+// own token counts (ebiv/rans.go:46-85) and the interleaved rANS coder
+// (ebiv/rans.go:186-214).  Returns the adjusted levels, the stream and the
+// frequency tables (16 entries per context).
+int encodeBlockStream(int32_t* levels, int n, int plane, int txIdx, std::vector<uint8_t>* stream,
+                      std::vector<uint32_t>* freqs, std::vector<uint8_t>* used) {
+  if (n != 4 && n != 8 && n != 16) return kErrArg;
+  applySignDataHiding(levels, n);
+  TokStream ts;
+  encodeBlock(ts, plane, txIdx, levels, n);
+  return encodeTokenStream(ts.toks.data() ? reinterpret_cast<const uint16_t*>(ts.toks.data()) : nullptr,
+                           (int)ts.toks.size(), stream, freqs, used);
+}
+
+// rANS-encodes a (context, symbol) token list with tables normalized from its
+// own counts; the bypass context is the fixed uniform table.
+int encodeTokenStream(const uint16_t* pairs, int count, std::vector<uint8_t>* stream, std::vector<uint32_t>* freqs,
+                      std::vector<uint8_t>* used) {
+  std::vector<Tok> toks((size_t)count);
+  for (int i = 0; i < count; i++) toks[(size_t)i] = {pairs[2 * i], pairs[2 * i + 1]};
+  std::vector<std::vector<uint32_t>> counts(kNumContexts);
+  for (int c = 0; c < kNumContexts; c++) counts[c].assign((size_t)alphabetSize(c), 0);
+  for (const Tok& t : toks) {
+    if (t.ctx >= kNumContexts || t.sym >= alphabetSize(t.ctx)) return kErrArg;
+    counts[t.ctx][t.sym]++;
+  }
+  std::vector<EncTable> tables(kNumContexts);
+  freqs->assign((size_t)kNumContexts * 16, 0);
+  used->assign((size_t)kNumContexts, 0);
+  for (int c = 0; c < kNumContexts; c++) {
+    if (c == ctxBypass) continue;
+    const Freqs f = normalizeFreqs(counts[c]);
+    tables[c] = buildEncTable(f.empty() ? Freqs((size_t)alphabetSize(c), 0) : f, alphabetSize(c));
+    if (!f.empty()) {
+      (*used)[(size_t)c] = 1;
+      for (size_t s = 0; s < f.size(); s++) (*freqs)[(size_t)c * 16 + s] = f[s];
+    }
+  }
+  tables[ctxBypass] = buildEncTable(Freqs{kM / 2, kM / 2}, 2);
+  *stream = ransEncode(toks, tables);
+  return kOK;
+}
 }  // namespace ebiv

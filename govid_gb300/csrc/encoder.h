@@ -99,4 +99,10 @@ class Encoder {
   int gridRows() const;
 };
 
+// Single-block and token-stream coding hooks (see encoder.cpp).
+int encodeBlockStream(int32_t* levels, int n, int plane, int txIdx, std::vector<uint8_t>* stream,
+                      std::vector<uint32_t>* freqs, std::vector<uint8_t>* used);
+int encodeTokenStream(const uint16_t* pairs, int count, std::vector<uint8_t>* stream, std::vector<uint32_t>* freqs,
+                      std::vector<uint8_t>* used);
+
 }  // namespace ebiv

@@ -296,4 +296,32 @@ int ebiv_encode_scene(const int64_t* spec, int frames, const ebiv_encoder_option
 
 void ebiv_free(void* p) { std::free(p); }
 
+int ebiv_encode_block(int32_t* levels, int n, int plane, int tx_idx, uint8_t* stream, size_t cap, size_t* len,
+                      uint32_t* freqs, uint8_t* used) {
+  std::vector<uint8_t> st, u;
+  std::vector<uint32_t> f;
+  const int r = encodeBlockStream(levels, n, plane, tx_idx, &st, &f, &u);
+  if (r) return r;
+  if (st.size() > cap) return kErrArg;
+  std::memcpy(stream, st.data(), st.size());
+  *len = st.size();
+  std::memcpy(freqs, f.data(), f.size() * 4);
+  std::memcpy(used, u.data(), u.size());
+  return kOK;
+}
+
+int ebiv_encode_tokens(const uint16_t* pairs, int count, uint8_t* stream, size_t cap, size_t* len, uint32_t* freqs,
+                       uint8_t* used) {
+  std::vector<uint8_t> st, u;
+  std::vector<uint32_t> f;
+  const int r = encodeTokenStream(pairs, count, &st, &f, &u);
+  if (r) return r;
+  if (st.size() > cap) return kErrArg;
+  std::memcpy(stream, st.data(), st.size());
+  *len = st.size();
+  std::memcpy(freqs, f.data(), f.size() * 4);
+  std::memcpy(used, u.data(), u.size());
+  return kOK;
+}
+
 }  // extern "C"

@@ -96,6 +96,18 @@ void ebiv_scene_destroy(ebiv_scene* s);
 int ebiv_encode_scene(const int64_t* spec13, int frames, const ebiv_encoder_options* o, uint8_t** out, size_t* n);
 void ebiv_free(void* p);
 
+/* Codes one n x n block of levels as the encoder codes a residual block:
+ * sign-data hiding (ebiv/residual.go:134-180, levels are adjusted in place),
+ * token grammar (ebiv/residual.go:30-75) and rANS (ebiv/rans.go:186-214)
+ * with tables normalized from the block's own tokens.  freqs receives 16
+ * entries per context (72 contexts), used one flag per context. */
+int ebiv_encode_block(int32_t* levels, int n, int plane, int tx_idx, uint8_t* stream, size_t cap, size_t* len,
+                      uint32_t* freqs, uint8_t* used);
+/* rANS-codes `count` (context, symbol) pairs with tables normalized from
+ * their own counts (ebiv/rans.go:46-85, 186-214). */
+int ebiv_encode_tokens(const uint16_t* pairs, int count, uint8_t* stream, size_t cap, size_t* len, uint32_t* freqs,
+                       uint8_t* used);
+
 #ifdef __cplusplus
 }
 #endif

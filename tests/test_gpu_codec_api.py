@@ -1,0 +1,119 @@
+"""The reference-facing C-ABI codec (include/ebivgpu.h) against the
+ebiv.Codec contract (ebiv/codec.go:70-192): error statuses, ring cursor and
+Flush, RGBA conversion (frame.go:8-67), and side effects of failing frames,
+each checked against the CPU oracle."""
+import numpy as np
+import pytest
+
+import ebiv_oracle
+from govid_gb300 import ebiv
+
+from helpers import encode_gen, noisy_gen
+from test_gpu_batch import _zero_tile
+
+pytestmark = pytest.mark.gpu
+
+
+def _raw_key(w, h, extra=0):
+    return bytes([0, w & 255, w >> 8, h & 255, h >> 8, 0]) + bytes(ebiv.packed_size(w, h) + extra)
+
+
+def _status(codec, pkt):
+    try:
+        codec.decode(pkt)
+        return 0
+    except ebiv.EbivError as e:
+        return e.status
+
+
+def test_bad_packets(gpu_required):
+    assert _status(ebiv.Codec(), b"") == ebiv.ErrCorrupt.status
+    assert _status(ebiv.Codec(), bytes([1])) == ebiv.ErrNoKeyframe.status
+    assert _status(ebiv.Codec(), bytes([0, 1, 0])) == ebiv.ErrCorrupt.status
+    c = ebiv.Codec()
+    assert _status(c, _raw_key(16, 16)[:6]) == ebiv.ErrCorrupt.status
+    assert _status(c, _raw_key(16, 16, 1)) == ebiv.ErrCorrupt.status
+    assert _status(c, _raw_key(16, 16)) == 0
+    assert _status(c, _raw_key(32, 32)) == ebiv.ErrDimensions.status
+    assert _status(ebiv.Codec(), bytes([0, 16, 0, 16, 0, 0x10])) == ebiv.ErrUnsupported.status
+    assert _status(ebiv.Codec(), bytes([0 | (5 << 2), 16, 0, 16, 0, 0])) == ebiv.ErrUnsupported.status
+
+
+def test_ring_cursor_and_flush(gpu_required):
+    cont, _, _ = encode_gen(64, 48, 6, ebiv.synth_frame, intra=20, gop=3)
+    pk = [p.data for p in ebiv.Reader(cont).packets()]
+    c = ebiv.Codec(3)
+    slots = [c.decode(p).ring_slot for p in pk[:4]]
+    assert slots == [0, 1, 2, 0]
+    c.flush()
+    assert c.decode(pk[3]).ring_slot == 0  # pk[3] is a key frame
+
+
+def test_rgba_matches_oracle(gpu_required):
+    spec = ebiv.SceneSpec(width=97, height=55, seed=4, sprites=2)
+    cont = ebiv.encode_scene(spec, 2, qp=22, gop=2, tiles=(1, 1), fast=True)
+    pk = [p.data for p in ebiv.Reader(cont).packets()]
+    c = ebiv.Codec()
+    for p in pk:
+        f = c.decode(p)
+        want = np.frombuffer(ebiv_oracle.rgba(f.packed(), 97, 55), np.uint8).reshape(55, 97, 4)
+        got = f.rgba()
+        assert (got == want).all()
+        assert (got[..., 3] == 255).all()
+
+
+def _zero_override_tile(pkt: bytes, tile: int) -> bytes:
+    """Zeroes one tile of a key packet's golden-override payload."""
+    b = bytearray(pkt)
+    pos = 6
+
+    def uvar(p):
+        x, s = 0, 0
+        while True:
+            c = b[p]
+            x |= (c & 0x7F) << s
+            p += 1
+            if c < 0x80:
+                return x, p
+            s += 7
+
+    keylen, pos = uvar(pos)
+    ov = pos + keylen
+    head = bytes([0x01 | (2 << 2)]) + bytes(b[ov:])  # decode the override body as an inter packet
+    zeroed = _zero_tile(head, tile)
+    return bytes(b[:ov]) + zeroed[1:]
+
+
+def test_failed_override_leaves_partial_golden(gpu_required):
+    cont, _, _ = encode_gen(64, 48, 10, noisy_gen, intra=16, gop=10, altref=4)
+    pk = [p.data for p in ebiv.Reader(cont).packets()]
+    assert ebiv.parse_frame_header(pk[0])["golden_override"]
+    bad = list(pk)
+    bad[0] = _zero_override_tile(pk[0], 0)
+    # a second, clean key with the same geometry restarts from a known state
+    seq = bad + pk
+    want = ebiv_oracle.decode_all(seq)
+    assert want[0][0] == ebiv.ErrCorrupt.status
+    c = ebiv.Codec()
+    for i, p in enumerate(seq):
+        try:
+            got = (0, c.decode(p).packed())
+        except ebiv.EbivError as e:
+            got = (e.status, None)
+        assert got[0] == want[i][0], f"frame {i}"
+        assert got[1] == want[i][1], f"frame {i} differs from the oracle"
+
+
+def test_failed_inter_frame_keeps_references(gpu_required):
+    spec = ebiv.SceneSpec(width=160, height=96, seed=8, sprites=3)
+    cont = ebiv.encode_scene(spec, 8, qp=22, gop=8, tiles=(2, 1), fast=True)
+    pk = [p.data for p in ebiv.Reader(cont).packets()]
+    pk[2] = _zero_tile(pk[2], 0)
+    want = ebiv_oracle.decode_all(pk)
+    c = ebiv.Codec()
+    for i, p in enumerate(pk):
+        try:
+            got = (0, c.decode(p).packed())
+        except ebiv.EbivError as e:
+            got = (e.status, None)
+        assert got == want[i], f"frame {i}"
