@@ -33,6 +33,21 @@ class PlaneView(C.Structure):
                 ("y_stride", C.c_int32), ("c_stride", C.c_int32), ("width", C.c_int32), ("height", C.c_int32)]
 
 
+class ServeOptions(C.Structure):
+    _fields_ = [("duration_s", C.c_double), ("frames_per_stream", C.c_int64), ("seek_prob", C.c_double),
+                ("seed", C.c_uint64), ("hbm_budget_bytes", C.c_uint64), ("max_frames_per_round", C.c_int32),
+                ("ring", C.c_int32), ("record", C.c_int32)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in ("requests", "frames", "errors", "seeks", "loops", "rounds",
+                                         "admitted_total", "admitted_peak", "waiting_at_end")] + \
+               [(k, C.c_double) for k in ("elapsed_s", "latency_p50_ms", "latency_p99_ms", "latency_max_ms",
+                                          "latency_mean_ms", "frames_per_s", "kernel_ms", "entropy_ms",
+                                          "recon_ms")] + [("key_frames", C.c_int64)] + \
+               [("peak_bytes", C.c_uint64)]
+
+
 class Frame(C.Structure):
     _fields_ = [
         ("y", C.POINTER(C.c_uint8)), ("cb", C.POINTER(C.c_uint8)), ("cr", C.POINTER(C.c_uint8)),
@@ -88,6 +103,13 @@ def lib() -> C.CDLL:
     _sig(L, "ebivgpu_batch_launches", I64, P)
     _sig(L, "ebivgpu_batch_device_bytes", C.c_uint64, P)
     _sig(L, "ebivgpu_stream_footprint", C.c_uint64, I, I, I, I)
+    # serving
+    _sig(L, "ebivgpu_server_create", I, C.POINTER(ServeOptions), PP)
+    _sig(L, "ebivgpu_server_add_stream", I, P, C.POINTER(C.c_char_p), C.POINTER(S), I, C.c_double, I)
+    _sig(L, "ebivgpu_server_run", I, P, C.POINTER(ServeStats))
+    _sig(L, "ebivgpu_server_frame_hashes", I64, P, C.POINTER(C.c_int32), C.POINTER(I64), C.POINTER(C.c_uint64), I64)
+    _sig(L, "ebivgpu_server_destroy", None, P)
+    _sig(L, "ebivgpu_frame_hash", C.c_uint64, C.c_char_p, S)
     # encoder
     _sig(L, "ebiv_encoder_default_options", None, C.POINTER(EncoderOptions))
     _sig(L, "ebiv_encoder_create", I, C.POINTER(EncoderOptions), PP)

@@ -399,13 +399,15 @@ int Engine::round(std::vector<RoundResult>* results) {
   return roundFor(ids, results);
 }
 
-int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* results) {
+int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* results,
+                     const std::vector<int>* maxFrames) {
   // ---- plan: up to `lookahead` frames per resident stream --------------------
   std::vector<Job> jobs;
   jobs.reserve(ids.size() * (size_t)lookahead_);
   std::vector<std::vector<int>> chains;  // per stream, indices into jobs in decode order
   size_t streamedBytes = 0;
-  for (int id : ids) {
+  for (size_t ii = 0; ii < ids.size(); ii++) {
+    const int id = ids[ii];
     if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) continue;
     Stream& s = *streams_[(size_t)id];
     std::vector<int> chain;
@@ -418,7 +420,8 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
       for (int b : s.outputs) busy[(size_t)b] = 1;
     };
     resetBusy();
-    const int k = s.resident ? lookahead_ : 1;
+    int k = s.resident ? lookahead_ : 1;
+    if (maxFrames && ii < maxFrames->size()) k = std::max(0, std::min(k, (*maxFrames)[ii]));
     int lastGpu = -1;  // job index of the chain's last GPU frame
     for (int step = 0; step < k; step++) {
       Job j;

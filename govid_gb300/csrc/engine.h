@@ -72,8 +72,10 @@ class Engine {
   // Decodes one packet for every active stream with work; returns the number
   // of frames attempted.  Results (one per attempted frame) are appended.
   int round(std::vector<RoundResult>* results);
-  // Same, for an explicit subset of streams.
-  int roundFor(const std::vector<int>& ids, std::vector<RoundResult>* results);
+  // Same, for an explicit subset of streams; maxFrames (optional, parallel
+  // to ids) caps each stream's frames this round below the lookahead.
+  int roundFor(const std::vector<int>& ids, std::vector<RoundResult>* results,
+               const std::vector<int>* maxFrames = nullptr);
 
   int downloadFrame(const EngineFrameView& v, uint8_t* packed, size_t cap);
   int downloadStrided(const EngineFrameView& v, uint8_t* y, int ys, uint8_t* cb, uint8_t* cr, int cs);

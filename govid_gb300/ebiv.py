@@ -291,6 +291,53 @@ class Batch:
             pass
 
 
+class Server:
+    """Serving loop: continuous batching of per-frame requests from many
+    streams with HBM-budget admission, seeks and looping (include/ebivgpu.h,
+    ebivgpu_server_*)."""
+
+    def __init__(self, duration_s: float = 10.0, frames_per_stream: int = 600, seek_prob: float = 0.05,
+                 seed: int = 1, hbm_budget_bytes: int = 120 << 30, max_frames_per_round: int = 4, ring: int = 3,
+                 record: bool = False):
+        L = _native.lib()
+        o = _native.ServeOptions(duration_s, frames_per_stream, seek_prob, seed, hbm_budget_bytes,
+                                 max_frames_per_round, ring, int(record))
+        h = C.c_void_p()
+        _check(L.ebivgpu_server_create(C.byref(o), C.byref(h)), "server")
+        self._h, self._L = h, L
+
+    def add_stream(self, packets: list[bytes], fps: float, loop: bool = False) -> None:
+        n = len(packets)
+        arr = (C.c_char_p * n)(*packets)
+        lens = (C.c_size_t * n)(*[len(p) for p in packets])
+        _check(self._L.ebivgpu_server_add_stream(self._h, arr, lens, n, float(fps), int(loop)))
+
+    def run(self) -> dict:
+        st = _native.ServeStats()
+        _check(self._L.ebivgpu_server_run(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in _native.ServeStats._fields_}
+
+    def frame_hashes(self) -> list[tuple[int, int, int]]:
+        n = self._L.ebivgpu_server_frame_hashes(self._h, None, None, None, 0)
+        s = (C.c_int32 * n)()
+        f = (C.c_int64 * n)()
+        h = (C.c_uint64 * n)()
+        self._L.ebivgpu_server_frame_hashes(self._h, s, f, h, n)
+        return list(zip(s, f, h))
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._L.ebivgpu_server_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+def frame_hash(packed: bytes) -> int:
+    return int(_native.lib().ebivgpu_frame_hash(packed, len(packed)))
+
+
 def stream_footprint(width: int, height: int, ring: int = 3, lookahead: int = 1) -> int:
     return int(_native.lib().ebivgpu_stream_footprint(width, height, ring, lookahead))
 

@@ -119,6 +119,44 @@ int64_t ebivgpu_batch_launches(ebivgpu_batch* b);
 uint64_t ebivgpu_batch_device_bytes(ebivgpu_batch* b);
 /* HBM bytes one stream of this geometry holds (frame pool + scratch). */
 uint64_t ebivgpu_stream_footprint(int width, int height, int ring, int lookahead);
+/* ---- Serving loop --------------------------------------------------------
+ * Continuous batching of per-frame requests from many streams: each stream
+ * issues requests as a Poisson process at its frame rate; every round
+ * decodes the requested frames of all streams with queued requests in one
+ * set of launches; seeks go to key frames, looping streams restart at the
+ * end; streams are admitted while their HBM footprints fit the budget and
+ * release it when they finish.  No single reference counterpart: the
+ * reference serves one Player per stream (player.go, source.go). */
+typedef struct ebivgpu_server ebivgpu_server;
+typedef struct {
+  double duration_s;           /* requests arrive during this many seconds */
+  int64_t frames_per_stream;   /* requests per stream at most */
+  double seek_prob;            /* fraction of requests that are seeks */
+  uint64_t seed;
+  uint64_t hbm_budget_bytes;   /* admission cap on frame state */
+  int32_t max_frames_per_round;/* per stream, when it fell behind */
+  int32_t ring;
+  int32_t record;              /* hash every delivered frame (testing) */
+} ebivgpu_serve_options;
+typedef struct {
+  int64_t requests, frames, errors, seeks, loops, rounds;
+  int64_t admitted_total, admitted_peak, waiting_at_end;
+  double elapsed_s, latency_p50_ms, latency_p99_ms, latency_max_ms, latency_mean_ms, frames_per_s, kernel_ms;
+  double entropy_ms, recon_ms; /* kernel_ms split: entropy stage, reconstruction stages */
+  int64_t key_frames;          /* key frames decoded (stream starts, seeks, loops) */
+  uint64_t peak_bytes;
+} ebivgpu_serve_stats;
+int ebivgpu_server_create(const ebivgpu_serve_options* o, ebivgpu_server** out);
+int ebivgpu_server_add_stream(ebivgpu_server* s, const uint8_t* const* pkts, const size_t* lens, int n, double fps,
+                              int loop);
+int ebivgpu_server_run(ebivgpu_server* s, ebivgpu_serve_stats* out);
+/* (stream index in add order, frame index, FNV-1a of the packed planes) per
+ * delivered frame when record was set; returns the total count. */
+int64_t ebivgpu_server_frame_hashes(ebivgpu_server* s, int32_t* stream, int64_t* frame, uint64_t* hash, int64_t cap);
+void ebivgpu_server_destroy(ebivgpu_server* s);
+/* FNV-1a 64 of a buffer (the hash the server records). */
+uint64_t ebivgpu_frame_hash(const uint8_t* packed, size_t n);
+
 /* Non-zero when a CUDA device is usable from this process. */
 int ebivgpu_device_available(void);
 
