@@ -110,6 +110,8 @@ def lib() -> C.CDLL:
     _sig(L, "ebivgpu_server_frame_hashes", I64, P, C.POINTER(C.c_int32), C.POINTER(I64), C.POINTER(C.c_uint64), I64)
     _sig(L, "ebivgpu_server_destroy", None, P)
     _sig(L, "ebivgpu_frame_hash", C.c_uint64, C.c_char_p, S)
+    _sig(L, "ebivgpu_decode_key_noalloc", I, C.c_char_p, S, C.c_void_p, C.c_int32, S, C.c_void_p, C.c_void_p,
+         C.c_int32, S, C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32))
     # encoder
     _sig(L, "ebiv_encoder_default_options", None, C.POINTER(EncoderOptions))
     _sig(L, "ebiv_encoder_create", I, C.POINTER(EncoderOptions), PP)

@@ -74,6 +74,7 @@ enum Status {
   kErrIO = 10,
   kErrDevice = 11,
   kErrArg = 12,
+  kErrTooLarge = 13,  // beyond the fixed scratch of ebivgpu_decode_key_noalloc
 };
 
 struct Rect4 {

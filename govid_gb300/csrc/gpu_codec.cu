@@ -213,6 +213,8 @@ const char* ebivgpu_status_string(int s) {
     case kErrIO: return "i/o error";
     case kErrDevice: return "ebivgpu: CUDA device error";
     case kErrArg: return "ebivgpu: invalid argument";
+    case kErrTooLarge:
+      return "ebivgpu: frame exceeds the no-allocation scratch (at most 3600 macroblocks and a 2 MiB packet)";
     default: return "unknown status";
   }
 }

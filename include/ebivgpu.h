@@ -41,7 +41,8 @@ enum {
   EBIV_ERR_EOF = 9,          /* io.EOF from a demuxer */
   EBIV_ERR_IO = 10,
   EBIV_ERR_DEVICE = 11,      /* CUDA failure or no usable GPU */
-  EBIV_ERR_ARG = 12          /* invalid argument at the boundary */
+  EBIV_ERR_ARG = 12,         /* invalid argument at the boundary */
+  EBIV_ERR_TOO_LARGE = 13    /* frame or packet beyond ebivgpu_decode_key_noalloc's fixed scratch */
 };
 
 typedef struct ebivgpu_codec ebivgpu_codec;
@@ -156,6 +157,36 @@ int64_t ebivgpu_server_frame_hashes(ebivgpu_server* s, int32_t* stream, int64_t*
 void ebivgpu_server_destroy(ebivgpu_server* s);
 /* FNV-1a 64 of a buffer (the hash the server records). */
 uint64_t ebivgpu_frame_hash(const uint8_t* packed, size_t n);
+
+/* ---- Key-frame decode without device allocation ---------------------------
+ * No reference counterpart: govid allocates its frame buffers on first use
+ * (ebiv/codec.go:129-153).  This entry point is for callers that must not
+ * allocate device memory on their decode path: a presentation thread with a
+ * frame deadline (cudaMalloc/cudaFree can synchronise the device), or a
+ * process whose device memory is fixed at start-up.
+ *
+ * Decodes one key-frame packet, as the first frame of a fresh stream (the
+ * result and status equal ebivgpu_decode's on a new codec), into the caller's
+ * device planes.  All scratch is one static device array of 8,461,312 bytes
+ * per device, so frames are limited to EBIVGPU_NOALLOC_MAX_MBS macroblocks
+ * (1280x720) and packets to EBIVGPU_NOALLOC_MAX_PACKET bytes; larger ones
+ * return EBIV_ERR_TOO_LARGE.  The planes must cover the macroblock-aligned
+ * frame: y_stride >= 16*ceil(W/16) and y_cap >= y_stride*16*ceil(H/16);
+ * c_stride >= 8*ceil(W/16) and c_cap >= c_stride*8*ceil(H/16).  Bytes beyond
+ * the visible W x H are scratch.  With y == NULL the call only reports W and H.
+ * Runs on cuda_stream (a cudaStream_t; NULL = the legacy default stream) and
+ * returns when the frame is decoded.  Inter frames return EBIV_ERR_NOKEYFRAME;
+ * a key frame coded as inter (it would predict from a new codec's zeroed
+ * references; the encoder never writes one) returns EBIV_ERR_UNSUPPORTED.
+ *
+ * The first call on a device resolves the scratch's address and uploads the
+ * decoder's constant tables; make it before any stream capture.  Calls that
+ * overlap in time on one device share the scratch and race: serialise them. */
+#define EBIVGPU_NOALLOC_MAX_MBS 3600
+#define EBIVGPU_NOALLOC_MAX_PACKET (2u << 20)
+int ebivgpu_decode_key_noalloc(const uint8_t* pkt, size_t n, uint8_t* y, int32_t y_stride, size_t y_cap, uint8_t* cb,
+                               uint8_t* cr, int32_t c_stride, size_t c_cap, void* cuda_stream, int32_t* width,
+                               int32_t* height);
 
 /* Non-zero when a CUDA device is usable from this process. */
 int ebivgpu_device_available(void);
