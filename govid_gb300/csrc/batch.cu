@@ -12,7 +12,7 @@
 
 namespace ebiv {
 
-void launchEntropy(const FrameDesc* frames, const int2* jobs, int njobs, cudaStream_t s);
+void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, cudaStream_t s);
 void launchInter(const FrameDesc* frames, int nframes, int maxMBs, cudaStream_t s);
 void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, cudaStream_t s);
 
@@ -519,8 +519,17 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
     const size_t oStat = al(oDesc + sizeof(FrameDesc) * nDesc, 64);
     const size_t oTab = al(oStat + sizeof(int32_t) * nDesc, 64);
     const size_t oTiles = al(oTab + sizeof(DeviceTables) * nDesc, 64);
+    // Entropy jobs: groups of up to kEntropyTilesPerJob tiles of one frame.
+    std::vector<int> tilesOf((size_t)nDesc, 0);
+    for (const Job& j : jobs) {
+      if (j.mainDesc >= 0) tilesOf[(size_t)j.mainDesc] = (int)j.main.tiles.size();
+      if (j.ovDesc >= 0) tilesOf[(size_t)j.ovDesc] = (int)j.ov.tiles.size();
+    }
+    int nEJobs = 0;
+    for (int t : tilesOf) nEJobs += (t + kEntropyTilesPerJob - 1) / kEntropyTilesPerJob;
     const size_t oJobs = al(oTiles + sizeof(TileRange) * (size_t)nTiles, 64);
-    const size_t oPkt = al(oJobs + sizeof(int2) * (size_t)nTiles, 256);
+    const size_t oEJobs = al(oJobs + sizeof(int2) * (size_t)nTiles, 64);
+    const size_t oPkt = al(oEJobs + sizeof(int4) * (size_t)nEJobs, 256);
     const size_t total = oPkt + streamedBytes;
     if (ensureStage(total)) return -1;
     uint8_t* h = hStage_;
@@ -534,17 +543,13 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
     // and each step's job ranges are contiguous.
     std::vector<int> tileFirst((size_t)nDesc, 0);
     {
-      std::vector<int> tilesOf((size_t)nDesc, 0);
-      for (const Job& j : jobs) {
-        if (j.mainDesc >= 0) tilesOf[(size_t)j.mainDesc] = (int)j.main.tiles.size();
-        if (j.ovDesc >= 0) tilesOf[(size_t)j.ovDesc] = (int)j.ov.tiles.size();
-      }
       int acc = 0;
       for (int di = 0; di < nDesc; di++) {
         tileFirst[(size_t)di] = acc;
         acc += tilesOf[(size_t)di];
       }
     }
+    std::vector<const PayloadPlan*> planOf((size_t)nDesc, nullptr);
     auto fill = [&](const Job& j, const PayloadPlan& plan, int di, int rec, int ref, int gold, bool inter, int gateDesc,
                     const Slot& sl) {
       const Stream& s = *streams_[(size_t)j.stream];
@@ -587,6 +592,7 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
         hr[tf + t] = plan.tiles[t];
         hj[tf + t] = make_int2(di, (int)t);
       }
+      planOf[(size_t)di] = &plan;
     };
     for (Job& j : jobs) {
       if (j.mainDesc < 0) continue;
@@ -597,11 +603,28 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
       if (j.ovDesc >= 0)
         fill(j, j.ov, j.ovDesc, j.ovBuf, j.work, j.work, true, j.mainDesc, s.slots.back());
     }
+    {
+      // Longest tile first, so the slowest chains start in the first wave.
+      std::vector<std::pair<uint32_t, int4>> ej;
+      ej.reserve((size_t)nEJobs);
+      for (int di = 0; di < nDesc; di++) {
+        for (int t0 = 0; t0 < tilesOf[(size_t)di]; t0 += kEntropyTilesPerJob) {
+          const int nt = std::min(kEntropyTilesPerJob, tilesOf[(size_t)di] - t0);
+          uint32_t longest = 0;
+          for (int t = t0; t < t0 + nt; t++) longest = std::max(longest, planOf[(size_t)di]->tiles[(size_t)t].length);
+          ej.push_back({longest, make_int4(di, t0, nt, 0)});
+        }
+      }
+      std::stable_sort(ej.begin(), ej.end(), [](const std::pair<uint32_t, int4>& a,
+                                                const std::pair<uint32_t, int4>& b) { return a.first > b.first; });
+      int4* he = reinterpret_cast<int4*>(h + oEJobs);
+      for (size_t k = 0; k < ej.size(); k++) he[k] = ej[k].second;
+    }
     if (cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, stream_) != cudaSuccess) return -1;
     const FrameDesc* dd = reinterpret_cast<const FrameDesc*>(d + oDesc);
     const int2* dj = reinterpret_cast<const int2*>(d + oJobs);
     if (timing_) cudaEventRecord(ev_[0], stream_);
-    launchEntropy(dd, dj, nTiles, stream_);
+    launchEntropy(dd, reinterpret_cast<const int4*>(d + oEJobs), nEJobs, stream_);
     launches_++;
     if (timing_) cudaEventRecord(ev_[1], stream_);
     for (const StepInfo& si : steps) {

@@ -1,13 +1,15 @@
 // GB300 (sm_103a) EBIV decode kernels.
 //
-// Stage A  kEntropy   one warp per tile: the tile's 4-state interleaved rANS
-//                     chain (ebiv/rans.go:270-304) drives the macroblock
-//                     grammar (ebiv/decode_intra.go:121-167,
-//                     ebiv/decode_inter.go:8-62, ebiv/residual.go:79-126,
-//                     ebiv/mv.go) and emits one MBRec per macroblock plus
-//                     sparse levels.  The warp runs the chain in lockstep;
-//                     the symbol lookup is a 17-lane ballot over the
-//                     context's cumulative starts held in shared memory.
+// Stage A  kEntropy   one warp per tile, up to four tiles of one frame per
+//                     CTA sharing the frame's symbol tables: the tile's
+//                     4-state interleaved rANS chain (ebiv/rans.go:270-304)
+//                     drives the macroblock grammar
+//                     (ebiv/decode_intra.go:121-167, ebiv/decode_inter.go:8-62,
+//                     ebiv/residual.go:79-126, ebiv/mv.go) and emits one
+//                     MBRec per macroblock plus sparse levels.  The warp runs
+//                     the chain in lockstep; a symbol costs one shared-memory
+//                     lookup (slot bucket -> symbol, start, frequency) except
+//                     in the few buckets a symbol boundary crosses.
 // Stage B1 kInterRecon one warp per macroblock of an inter frame: motion
 //                     compensation (ebiv/motioncomp.go) from the last or
 //                     golden reference plus dequantized inverse DCT residual
@@ -20,6 +22,8 @@
 // spins on memory written by another CTA.
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include "gpu_types.h"
 
 namespace ebiv {
@@ -27,11 +31,13 @@ namespace dev {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-__constant__ uint8_t cScan[3][256];   // zigzag: scan position -> row-major index
+// Per transform size and scan position: row-major index (bits 0-7) and the
+// token-context offset of the position's band, bandOf(i) * kNumPrevClass
+// (bits 8-15).
+__constant__ uint16_t cScanBand[3][256];
 __constant__ int32_t cDct[3][256];    // 2^13-scaled DCT-II basis, [k*n + i]
 __constant__ int32_t cTaps[4][4] = {{0, 64, 0, 0}, {-6, 55, 18, -3}, {-8, 40, 40, -8}, {-3, 18, 55, -6}};
 
-__device__ __forceinline__ int bandOf(int i) { return i == 0 ? 0 : i <= 2 ? 1 : i <= 8 ? 2 : i <= 20 ? 3 : 4; }
 __device__ __forceinline__ int tokenCtx(int plane, int txIdx, int band, int prevClass) {
   return plane == kPlaneLuma ? ctxTokenBase + (txIdx * kNumBands + band) * kNumPrevClass + prevClass
                              : ctxTokenBase + kLumaTokenCtx + band * kNumPrevClass + prevClass;
@@ -47,77 +53,106 @@ __device__ __forceinline__ int16_t clampMV(int v) {
 // ---------------------------------------------------------------------------
 // Stage A: entropy decode
 // ---------------------------------------------------------------------------
-// Per-warp symbol tables.  sym[c*16+s] packs the cumulative start (low 16
-// bits) and frequency (high 16) of symbol s in context c.  lut[c*64+b] is the
-// symbol whose range holds slot b*64 — the decoder starts there and walks
-// forward at most a few entries; 0xFF marks an unused context.
-struct WarpTables {
+// Symbol tables, built once per CTA for the frame whose tiles the CTA
+// decodes.  bucket[c*64+b] describes the symbol s of context c whose range
+// holds slot b*64: start (bits 0-11), frequency (12-24), s (25-28), a flag
+// (29) when a later symbol starts inside the bucket (the decoder then walks
+// sym[]), and a flag (30) for an unused context, whose entry decodes as the
+// identity so the chain stays well defined after the error.  sym[c*16+s]
+// packs start | frequency << 16 for the walk.
+constexpr uint32_t kBImpure = 1u << 29, kBUnused = 1u << 30;
+struct EntropyTables {
+  uint32_t bucket[kNumContexts * 64];
   uint32_t sym[kNumContexts * 16];
-  uint8_t lut[kNumContexts * 64];
 };
 constexpr int kRowMax = 128;  // tiles at most this many macroblocks wide keep their rows in shared memory
 struct WarpRows {
-  uint32_t mv[2][kRowMax];   // packed motion vectors of the row above / the current row
-  int16_t lvl[2][kRowMax];   // intra dependency levels (-1: not intra)
-  uint32_t rec[12];          // the macroblock record being assembled
+  uint32_t mv[2][kRowMax];  // packed motion vectors of the row above / the current row
+  int16_t lvl[2][kRowMax];  // intra dependency levels (-1: not intra)
 };
 
-__device__ __forceinline__ void buildWarpTables(WarpTables& T, const DeviceTables& src, int lane) {
-  for (int i = lane; i < kNumContexts * 16; i += 32) {
+__device__ __forceinline__ void buildTables(EntropyTables& T, const DeviceTables& src, int tid, int nthreads) {
+  for (int i = tid; i < kNumContexts * 16; i += nthreads) {
     const int c = i >> 4, sidx = i & 15;
     const uint32_t st = src.start[c][sidx], nx = src.start[c][sidx + 1];
     T.sym[i] = (st == 0xFFFFu || nx == 0xFFFFu) ? 0xFFFFu : (st | ((nx - st) << 16));
   }
-  for (int i = lane; i < kNumContexts * 64; i += 32) T.lut[i] = 0xFF;
-  __syncwarp();
+  for (int i = tid; i < kNumContexts * 64; i += nthreads) T.bucket[i] = (kM << 12) | kBUnused;
+  __syncthreads();
   // Each (context, symbol) pair fills the buckets whose first slot it covers.
-  for (int i = lane; i < kNumContexts * 16; i += 32) {
+  for (int i = tid; i < kNumContexts * 16; i += nthreads) {
     const int c = i >> 4, sidx = i & 15;
     if (!src.used[c]) continue;
     const uint32_t st = src.start[c][sidx], nx = src.start[c][sidx + 1];
     if (st == 0xFFFFu || nx == 0xFFFFu || nx <= st) continue;
-    for (uint32_t b = (st + 63) >> 6; b < 64 && (b << 6) < nx; b++) T.lut[c * 64 + b] = (uint8_t)sidx;
+    for (uint32_t b = (st + 63) >> 6; b < 64 && (b << 6) < nx; b++)
+      T.bucket[c * 64 + b] = st | ((nx - st) << 12) | ((uint32_t)sidx << 25) | (nx < ((b + 1) << 6) ? kBImpure : 0u);
   }
-  __syncwarp();
+  __syncthreads();
 }
 
 // A tile's rANS decoder (ebiv/rans.go:222-304).  All fields are warp-uniform;
 // the two next stream bytes are prefetched so renormalisation rarely waits.
+// After the first error every symbol decodes as 0.
 struct Chain {
   const uint8_t* buf;
   int32_t pos;
   uint32_t x0, x1, x2, x3;  // states in use order: x0 decodes the next symbol
   uint32_t b1, b2;          // buf[pos-1], buf[pos-2] when present
   int32_t err;
-  const WarpTables* t;
+  const EntropyTables* t;
 
   __device__ __forceinline__ uint32_t byteAt(int i) const { return i >= 0 ? (uint32_t)__ldg(buf + i) : 0u; }
 
   __device__ __forceinline__ int sym(int ctx) {
     if (err) return 0;
-    const uint32_t slot = x0 & (kM - 1);
-    int s = t->lut[ctx * 64 + (slot >> 6)];
-    if (s == 0xFF) {
-      err = kErrCorrupt;  // symbol decoded from an unused context
-      return 0;
-    }
-    uint32_t w = t->sym[ctx * 16 + s];
-    while (slot >= (w & 0xFFFFu) + (w >> 16)) w = t->sym[ctx * 16 + (++s)];
-    uint32_t x = (w >> 16) * (x0 >> kScaleBits) + slot - (w & 0xFFFFu);
-    while (x < kLower) {
-      if (pos == 0) {
-        err = kErrCorrupt;  // stream underrun
+    const uint32_t x = x0;
+    const uint32_t slot = x & (kM - 1);
+    const uint32_t e = t->bucket[ctx * 64 + (slot >> 6)];
+    int s = (int)((e >> 25) & 15u);
+    uint32_t start = e & 0xFFFu, freq = (e >> 12) & 0x1FFFu;
+    if (e & (kBImpure | kBUnused)) {
+      if (e & kBUnused) {
+        err = kErrCorrupt;  // symbol decoded from an unused context
         return 0;
       }
-      pos--;
-      x = (x << 8) | b1;
-      b1 = b2;
-      b2 = byteAt(pos - 2);
+      while (slot >= start + freq) {
+        const uint32_t w = t->sym[ctx * 16 + (++s)];
+        start = w & 0xFFFFu;
+        freq = w >> 16;
+      }
+    }
+    uint32_t xn = freq * (x >> kScaleBits) + slot - start;
+    if (xn < kLower) {
+      if (pos >= 2 && xn >= (kLower >> 16)) {
+        if (xn < (kLower >> 8)) {  // two bytes
+          xn = (xn << 16) | (b1 << 8) | b2;
+          pos -= 2;
+          b1 = byteAt(pos - 1);
+          b2 = byteAt(pos - 2);
+        } else {  // one byte
+          xn = (xn << 8) | b1;
+          pos -= 1;
+          b1 = b2;
+          b2 = byteAt(pos - 2);
+        }
+      } else {
+        while (xn < kLower) {
+          if (pos == 0) {
+            err = kErrCorrupt;  // stream underrun
+            return 0;
+          }
+          pos--;
+          xn = (xn << 8) | b1;
+          b1 = b2;
+          b2 = byteAt(pos - 2);
+        }
+      }
     }
     x0 = x1;
     x1 = x2;
     x2 = x3;
-    x3 = x;
+    x3 = xn;
     return s;
   }
   __device__ __forceinline__ uint32_t rawBits(int n) {
@@ -138,44 +173,46 @@ struct Chain {
 };
 
 // decodeBlock (ebiv/residual.go:79-126): writes the block's nonzero levels as
-// packed entries after a count word; lane 0 stores.  Returns the count.
-__device__ __forceinline__ int entropyBlock(Chain& d, int plane, int txIdx, int n, uint32_t* region, int lane) {
-  const uint8_t* scan = cScan[n == 4 ? 0 : (n == 8 ? 1 : 2)];  // scan follows the block size
-  const int total = n * n;
-  const int ctxBase = plane == kPlaneLuma ? ctxTokenBase + txIdx * kNumBands * kNumPrevClass
-                                          : ctxTokenBase + kLumaTokenCtx;
+// packed entries after a count word; lane 0 stores.  ctxBase selects the
+// token contexts of the plane and transform size.  Returns the count.
+__device__ __forceinline__ int entropyBlock(Chain& d, int ctxBase, int sz, uint32_t* region, int lane) {
+  const uint16_t* sb = cScanBand[sz];
+  const int total = 16 << (2 * sz);
   int first = -1, last = -1, count = 0;
   int32_t sumAbs = 0;
   int prevClass = 0;
   uint32_t firstPos = 0;
   int32_t firstMag = 0;
+  uint32_t cur = sb[0];
   for (int i = 0; i < total; i++) {
-    const int t = d.sym(ctxBase + bandOf(i) * kNumPrevClass + prevClass);
+    const uint32_t nxt = i + 1 < total ? sb[i + 1] : 0u;  // next position's entry, loaded early
+    const int t = d.sym(ctxBase + (int)(cur >> 8) + prevClass);
     if (t == tEOB) break;
-    if (t == tZero) {
+    if (t != tZero) {
+      int mag;
+      if (t == tEscape) {
+        mag = 5 + (int)d.classValue(ctxEscClass);
+        prevClass = 2;
+      } else {
+        mag = t;
+        prevClass = mag == 1 ? 1 : 2;
+      }
+      sumAbs = wadd(sumAbs, mag);
+      const uint32_t pos = cur & 0xFFu;
+      if (first < 0) {
+        first = i;
+        firstPos = pos;
+        firstMag = mag;
+      } else {
+        if (d.sym(ctxSign) == 1) mag = -mag;
+        if (lane == 0) region[1 + count] = pos | ((uint32_t)mag << 8);
+      }
+      count++;
+      last = i;
+    } else {
       prevClass = 0;
-      continue;
     }
-    int mag;
-    if (t == tEscape) {
-      mag = 5 + (int)d.classValue(ctxEscClass);
-      prevClass = 2;
-    } else {
-      mag = t;
-      prevClass = mag == 1 ? 1 : 2;
-    }
-    sumAbs = wadd(sumAbs, mag);
-    const uint32_t pos = scan[i];
-    if (first < 0) {
-      first = i;
-      firstPos = pos;
-      firstMag = mag;
-    } else {
-      if (d.sym(ctxSign) == 1) mag = -mag;
-      if (lane == 0) region[1 + count] = pos | ((uint32_t)mag << 8);
-    }
-    count++;
-    last = i;
+    cur = nxt;
   }
   if (first >= 0) {
     const bool neg = (last - first >= kSDHMinSpan) ? (sumAbs & 1) == 1 : d.sym(ctxSign) == 1;
@@ -199,117 +236,91 @@ __device__ __forceinline__ uint32_t packMV(int x, int y) { return (uint32_t)(uin
 __device__ __forceinline__ int mvX(uint32_t v) { return (int16_t)(v & 0xFFFFu); }
 __device__ __forceinline__ int mvY(uint32_t v) { return (int16_t)(v >> 16); }
 
-// Tile context: bounds, neighbour rows, record staging.
-struct TileCtx {
-  Chain d;
-  int lane;
-  int x0, x1, y0, y1;  // tile bounds in macroblocks
-  int mbCols;
-  bool wide;           // rows live in global memory
-  WarpRows* rows;
-  uint32_t* gmv;       // wide-tile fallback: one packed vector per macroblock
-  int16_t* glv;        // wide-tile fallback: one level per macroblock
-
-  __device__ __forceinline__ uint32_t mvAt(int mbx, int mby) const {
-    return wide ? gmv[mby * mbCols + mbx] : rows->mv[(mby - y0) & 1][mbx - x0];
+// The macroblock record being assembled, in registers (see MBRec: word 0
+// mode|ref<<8|part<<16|cbp<<24, 1 tx|cmode<<8, 2-5 vectors, 6-9 luma modes,
+// 10 nzmask, 11 wmask).
+struct Rec {
+  uint32_t w0, w1, mv0, mv1, mv2, mv3, lm0, lm1, lm2, lm3, nz, wm;
+  __device__ __forceinline__ void clear() { w0 = w1 = mv0 = mv1 = mv2 = mv3 = lm0 = lm1 = lm2 = lm3 = nz = wm = 0; }
+  __device__ __forceinline__ void lumaMode(int k, uint32_t m) {
+    const uint32_t v = m << ((k & 3) * 8);
+    const int w = k >> 2;
+    if (w == 0) lm0 |= v;
+    else if (w == 1) lm1 |= v;
+    else if (w == 2) lm2 |= v;
+    else lm3 |= v;
   }
-  __device__ __forceinline__ int lvAt(int mbx, int mby) const {
-    return wide ? glv[mby * mbCols + mbx] : rows->lvl[(mby - y0) & 1][mbx - x0];
+  __device__ __forceinline__ void setMV(int i, uint32_t v) {
+    if (i == 0) mv0 = v;
+    else if (i == 1) mv1 = v;
+    else if (i == 2) mv2 = v;
+    else mv3 = v;
   }
-  __device__ __forceinline__ void setMV(int mbx, int mby, uint32_t v, int lv) {
-    if (lane == 0) {
-      if (wide) {
-        gmv[mby * mbCols + mbx] = v;
-        glv[mby * mbCols + mbx] = (int16_t)lv;
-      } else {
-        rows->mv[(mby - y0) & 1][mbx - x0] = v;
-        rows->lvl[(mby - y0) & 1][mbx - x0] = (int16_t)lv;
-      }
-    }
-  }
-  // predictMV — ebiv/mv.go:21-52 (neighbours within the tile)
-  __device__ __forceinline__ uint32_t predictMV(int mbx, int mby) const {
-    const bool aOK = mbx > x0, bOK = mby > y0;
-    uint32_t a = 0, bv = 0, c = 0;
-    bool cOK = false;
-    if (aOK) a = mvAt(mbx - 1, mby);
-    if (bOK) {
-      bv = mvAt(mbx, mby - 1);
-      if (mbx + 1 < x1) {
-        c = mvAt(mbx + 1, mby - 1);
-        cOK = true;
-      } else if (aOK) {
-        c = mvAt(mbx - 1, mby - 1);
-        cOK = true;
-      }
-    }
-    if (!aOK && !bOK && !cOK) return 0;
-    if (aOK && !bOK && !cOK) return a;
-    if (!aOK && bOK && !cOK) return bv;
-    return packMV(median3((int16_t)mvX(a), (int16_t)mvX(bv), (int16_t)mvX(c)),
-                  median3((int16_t)mvY(a), (int16_t)mvY(bv), (int16_t)mvY(c)));
-  }
-  // Intra dependency level of an intra macroblock at (mbx, mby).
-  __device__ __forceinline__ int intraLevel(int mbx, int mby) const {
-    int m = -1;
-    if (mbx > x0) m = max(m, lvAt(mbx - 1, mby));
-    if (mby > y0) {
-      m = max(m, lvAt(mbx, mby - 1));
-      if (mbx > x0) m = max(m, lvAt(mbx - 1, mby - 1));
-      if (mbx + 1 < x1) m = max(m, lvAt(mbx + 1, mby - 1));
-    }
-    return m + 1;
+  // Lanes 0-2 store the 48-byte record as three 16-byte words.
+  __device__ __forceinline__ void store(MBRec* dst, int lane) const {
+    uint4 v;
+    if (lane == 0) v = make_uint4(w0, w1, mv0, mv1);
+    else if (lane == 1) v = make_uint4(mv2, mv3, lm0, lm1);
+    else v = make_uint4(lm2, lm3, nz, wm);
+    if (lane < 3) reinterpret_cast<uint4*>(dst)[lane] = v;
   }
 };
 
-// Record words (see MBRec): 0 mode|ref<<8|part<<16|cbp<<24, 1 tx|cmode<<8,
-// 2-5 mv[0..3], 6-9 luma modes, 10 nzmask, 11 wmask.  Lane 0 writes fields
-// into the warp's staging copy; lanes 0-11 store it.
-__device__ __forceinline__ void recSet(TileCtx& tc, int word, uint32_t v) {
-  if (tc.lane == 0) tc.rows->rec[word] = v;
-}
-__device__ __forceinline__ void recOr(TileCtx& tc, int word, uint32_t v) {
-  if (tc.lane == 0) tc.rows->rec[word] |= v;
-}
-
-// The coded blocks of one macroblock, decoded by a single inlined block
-// decoder in bitstream order.  kind: 0 luma block preceded by its intra mode,
-// 1 luma block, 2 chroma Cb (preceded by the chroma intra mode when intra),
-// 3 chroma Cr.
-struct BlockList {
-  int count;
-  int tx;
-  bool intra;
-  uint8_t kind[18];
+// Neighbourhood of the macroblock being decoded: availability within the
+// tile, the left neighbour's vector/level (registers) and the row above.
+struct Nbr {
+  bool aOK, bOK, arOK;
+  uint32_t mvA, mvB, mvC;  // left, above, above-right (or above-left)
+  bool cOK;
 };
 
-// Decodes the listed blocks; returns how many completed before an error and
+// predictMV — ebiv/mv.go:21-52 (neighbours within the tile)
+__device__ __forceinline__ uint32_t predictMV(const Nbr& n) {
+  if (!n.aOK && !n.bOK && !n.cOK) return 0;
+  if (n.aOK && !n.bOK && !n.cOK) return n.mvA;
+  if (!n.aOK && n.bOK && !n.cOK) return n.mvB;
+  return packMV(median3((int16_t)mvX(n.mvA), (int16_t)mvX(n.mvB), (int16_t)mvX(n.mvC)),
+                median3((int16_t)mvY(n.mvA), (int16_t)mvY(n.mvB), (int16_t)mvY(n.mvC)));
+}
+
+// The coded blocks of one macroblock in bitstream order: nLuma luma blocks
+// (each preceded by its intra mode when intra), then Cb (preceded by the
+// chroma intra mode when intra) and Cr when present.
+struct BlockPlan {
+  int nLuma, tx;
+  bool intra, cb, cr;
+};
+
+// The one block loop of the kernel (a single inlined copy keeps the code
+// small).  Returns how many blocks completed before an error; *nzOut gets
 // the nonzero mask (bit k luma block k, 16 Cb, 17 Cr).
-__device__ __forceinline__ int entropyBlocks(TileCtx& tc, const BlockList& bl, uint32_t* coef, uint32_t* nzOut) {
-  Chain& d = tc.d;
-  const int n = 4 << bl.tx;
-  uint32_t nz = 0;
+__device__ __forceinline__ int entropyBlocks(Chain& d, Rec& r, const BlockPlan& p, uint32_t* coef, int lane,
+                                             uint32_t* nzOut) {
+  const int nEnt = p.nLuma + (p.cb ? 1 : 0) + (p.cr ? 1 : 0);
+  const int bw = (16 << (2 * p.tx)) + 1;  // words per luma block region
+  const int lumaBase = ctxTokenBase + p.tx * kNumBands * kNumPrevClass;
   int done = 0;
-  int luma = 0;
-  for (int e = 0; e < bl.count; e++) {
-    const int kind = bl.kind[e];
-    int plane = kPlaneLuma, bn = n, txi = bl.tx;
+  uint32_t nz = 0;
+#pragma unroll 1
+  for (int e = 0; e < nEnt; e++) {
+    int ctxBase, sz;
     uint32_t* region;
     uint32_t bit;
-    if (kind <= 1) {
-      if (kind == 0) recOr(tc, 6 + (luma >> 2), (uint32_t)d.sym(ctxLumaMode) << ((luma & 3) * 8));
-      region = coef + luma * (n * n + 1);
-      bit = 1u << luma;
-      luma++;
+    if (e < p.nLuma) {
+      if (p.intra) r.lumaMode(e, (uint32_t)d.sym(ctxLumaMode));
+      ctxBase = lumaBase;
+      sz = p.tx;
+      region = coef + e * bw;
+      bit = 1u << e;
     } else {
-      if (kind == 2 && bl.intra) recOr(tc, 1, (uint32_t)d.sym(ctxChromaMode) << 8);
-      plane = kPlaneChroma;
-      bn = 8;
-      txi = 0;
-      region = coef + (kind == 2 ? kCoefCb : kCoefCr);
-      bit = kind == 2 ? (1u << 16) : (1u << 17);
+      const bool isCb = p.cb && e == p.nLuma;
+      if (isCb && p.intra) r.w1 |= (uint32_t)d.sym(ctxChromaMode) << 8;
+      ctxBase = ctxTokenBase + kLumaTokenCtx;
+      sz = 1;
+      region = coef + (isCb ? kCoefCb : kCoefCr);
+      bit = isCb ? (1u << 16) : (1u << 17);
     }
-    const int cnt = entropyBlock(d, plane, txi, bn, region, tc.lane);
+    const int cnt = entropyBlock(d, ctxBase, sz, region, lane);
     if (d.err) break;
     if (cnt) nz |= bit;
     done++;
@@ -318,112 +329,122 @@ __device__ __forceinline__ int entropyBlocks(TileCtx& tc, const BlockList& bl, u
   return done;
 }
 
-// Intra macroblock symbols (decodeLumaMB + decodeChromaMB,
-// ebiv/decode_intra.go:137-187).  Returns the write mask.
-__device__ __forceinline__ uint32_t entropyIntraMB(TileCtx& tc, uint32_t* coef) {
-  Chain& d = tc.d;
+// Intra macroblock header (decodeLumaMB, ebiv/decode_intra.go:137-150): the
+// transform size; the blocks follow.
+__device__ __forceinline__ void intraHeader(Chain& d, Rec& r, BlockPlan* p) {
   int tx = d.sym(ctxTxSize);
   if (tx >= 3) tx = 0;  // alphabet size 3: unreachable
-  const int nb = 16 >> (2 * tx);
-  BlockList bl;
-  bl.tx = tx;
-  bl.intra = true;
-  bl.count = nb + 2;
-  for (int k = 0; k < nb; k++) bl.kind[k] = 0;
-  bl.kind[nb] = 2;
-  bl.kind[nb + 1] = 3;
-  recSet(tc, 0, kRecIntra);
-  recSet(tc, 1, (uint32_t)tx);
-  uint32_t nz;
-  const int done = d.err ? 0 : entropyBlocks(tc, bl, coef, &nz);
-  if (d.err && done == 0) nz = 0;
-  recSet(tc, 10, nz);
-  uint32_t w = (1u << min(done, nb)) - 1;
-  if (done > nb) w |= 1u << 16;
-  if (done > nb + 1) w |= 1u << 17;
-  return w;
+  r.w0 = kRecIntra;
+  r.w1 = (uint32_t)tx;
+  p->tx = tx;
+  p->nLuma = 16 >> (2 * tx);
+  p->intra = p->cb = p->cr = true;
 }
 
-// Inter-frame macroblock symbols (decodeInterMB + reconInterMB grammar,
-// ebiv/decode_inter.go:8-118).  Returns the write mask.
-__device__ __forceinline__ uint32_t entropyInterMB(TileCtx& tc, int mbx, int mby, uint32_t* coef, bool* intra) {
-  Chain& d = tc.d;
+// Inter-frame macroblock header (decodeInterMB, ebiv/decode_inter.go:8-62):
+// mode, reference, partition, vectors, coded-block pattern, transform size.
+// Returns 0 when the macroblock is complete without blocks (*wOut holds its
+// write mask), 1 when the blocks of *p follow.  *mvOut is the vector
+// neighbours predict from.
+__device__ __forceinline__ int interHeader(Chain& d, Rec& r, const Nbr& n, BlockPlan* p, bool* intra,
+                                           uint32_t* mvOut, uint32_t* wOut) {
   const int mode = d.sym(ctxMBMode);
+  *mvOut = 0;
+  *wOut = 0;
   if (mode == mbSkip) {
-    const uint32_t p = tc.predictMV(mbx, mby);
-    tc.setMV(mbx, mby, p, -1);
-    recSet(tc, 0, kRecSkip);
-    recSet(tc, 2, p);
-    return kWriteAll;
+    const uint32_t pv = predictMV(n);
+    *mvOut = pv;
+    r.w0 = kRecSkip;
+    r.mv0 = pv;
+    *wOut = kWriteAll;
+    return 0;
   }
   if (mode == mbIntra) {
     *intra = true;
-    return entropyIntraMB(tc, coef);  // the caller records the zero vector and level
+    intraHeader(d, r, p);
+    return d.err ? 0 : 1;
   }
   if (mode != mbInter) {
     d.err = kErrCorrupt;
     return 0;
   }
   const int refSel = d.sym(ctxRef);
-  uint32_t pred = tc.predictMV(mbx, mby);
+  uint32_t pred = predictMV(n);
   if (refSel == refGolden) pred = 0;
   int part = d.sym(ctxPart);
   if (part >= kNumPartModes) part = 0;  // alphabet size 4: unreachable
   const int np = part == partWhole ? 1 : (part == part8x8 ? 4 : 2);
   uint32_t mv0 = 0;
+#pragma unroll 1
   for (int i = 0; i < np; i++) {
     const uint32_t pp = i > 0 ? mv0 : pred;
-    const int dx = d.mvComponent(ctxMVClassX);
-    const int vx = clampMV(mvX(pp) + dx);
-    const int dy = d.mvComponent(ctxMVClassY);
-    const int vy = clampMV(mvY(pp) + dy);
+    int vx = 0, vy = 0;
+#pragma unroll 1
+    for (int c = 0; c < 2; c++) {
+      const int dv = d.mvComponent(c ? ctxMVClassY : ctxMVClassX);
+      if (c == 0) vx = clampMV(mvX(pp) + dv);
+      else vy = clampMV(mvY(pp) + dv);
+    }
     const uint32_t v = packMV(vx, vy);
     if (i == 0) mv0 = v;
-    recSet(tc, 2 + i, v);
+    r.setMV(i, v);
   }
   if (d.err) return 0;
-  tc.setMV(mbx, mby, refSel == refGolden ? 0u : mv0, -1);
+  *mvOut = refSel == refGolden ? 0u : mv0;
   const int cbp = d.sym(ctxCBP);
-  recSet(tc, 0, kRecInter | ((uint32_t)refSel << 8) | ((uint32_t)part << 16) | ((uint32_t)cbp << 24));
+  r.w0 = kRecInter | ((uint32_t)refSel << 8) | ((uint32_t)part << 16) | ((uint32_t)cbp << 24);
   if (d.err) return 0;
-  BlockList bl;
-  bl.intra = false;
-  bl.tx = 0;
-  bl.count = 0;
-  int nb = 0;
+  int tx = 0, nb = 0;
   if (cbp & cbpLuma) {
-    int tx = d.sym(ctxTxSize);
+    tx = d.sym(ctxTxSize);
     if (tx >= 3) tx = 0;
     if (d.err) return 0;
-    recSet(tc, 1, (uint32_t)tx);
-    bl.tx = tx;
+    r.w1 = (uint32_t)tx;
     nb = 16 >> (2 * tx);
-    for (int k = 0; k < nb; k++) bl.kind[bl.count++] = 1;
   }
-  const int cbEntry = (cbp & cbpCb) ? bl.count : -1;
-  if (cbp & cbpCb) bl.kind[bl.count++] = 2;
-  const int crEntry = (cbp & cbpCr) ? bl.count : -1;
-  if (cbp & cbpCr) bl.kind[bl.count++] = 3;
-  uint32_t nz = 0;
-  const int done = entropyBlocks(tc, bl, coef, &nz);
-  recSet(tc, 10, nz);
-  if (done < nb) return (1u << done) - 1;  // a coded luma block failed: nothing else is written
-  uint32_t w = 0xFFFFu;                    // coded luma complete, or motion-compensated luma
+  p->tx = tx;
+  p->nLuma = nb;
+  p->intra = false;
+  p->cb = (cbp & cbpCb) != 0;
+  p->cr = (cbp & cbpCr) != 0;
+  return 1;
+}
+
+// Write mask after the blocks (decodeLumaMB/decodeChromaMB and
+// reconInterMB, ebiv/decode_intra.go:150-187, ebiv/decode_inter.go:63-118):
+// an intra macroblock keeps the blocks completed before an error; an inter
+// macroblock whose coded luma failed writes only the luma blocks decoded.
+__device__ __forceinline__ uint32_t writeMask(const BlockPlan& p, int done) {
+  const int nb = p.nLuma;
+  if (p.intra) {
+    uint32_t w = (1u << min(done, nb)) - 1;
+    if (done > nb) w |= 1u << 16;
+    if (done > nb + 1) w |= 1u << 17;
+    return w;
+  }
+  if (done < nb) return (1u << done) - 1;
+  const int cbEntry = p.cb ? nb : -1;
+  const int crEntry = p.cr ? nb + (p.cb ? 1 : 0) : -1;
+  uint32_t w = 0xFFFFu;  // coded luma complete, or motion-compensated luma
   if (cbEntry < 0 || done > cbEntry) w |= 1u << 16;
   if (crEntry < 0 || done > crEntry) w |= 1u << 17;
   return w;
 }
 
-constexpr int kEntropyWarps = 4;
+constexpr int kEntropyWarps = kEntropyTilesPerJob;
 
-__global__ void __launch_bounds__(32 * kEntropyWarps) kEntropy(const FrameDesc* frames, const int2* jobs, int njobs) {
-  __shared__ WarpTables sT[kEntropyWarps];
+// One CTA per entropy job: up to kEntropyWarps tiles of one frame, one warp
+// per tile, sharing the frame's symbol tables.
+__global__ void __launch_bounds__(32 * kEntropyWarps, 4) kEntropy(const FrameDesc* frames, const int4* jobs, int njobs) {
+  __shared__ EntropyTables sT;
   __shared__ WarpRows sR[kEntropyWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int j = blockIdx.x * kEntropyWarps + warp;
-  if (j >= njobs) return;
-  const FrameDesc* fp = frames + jobs[j].x;
-  const int tile = jobs[j].y;
+  if (blockIdx.x >= njobs) return;
+  const int4 job = jobs[blockIdx.x];
+  const FrameDesc* fp = frames + job.x;
+  buildTables(sT, *fp->tables, threadIdx.x, blockDim.x);
+  if (warp >= job.z) return;  // no barrier follows
+  const int tile = job.y + warp;
   // Descriptor fields into registers: the kernel's global stores cannot alias them then.
   const int mbCols = fp->mbCols;
   const int inter = fp->inter;
@@ -433,26 +454,19 @@ __global__ void __launch_bounds__(32 * kEntropyWarps) kEntropy(const FrameDesc* 
   TileStat* const tstat = fp->tileStat;
   int32_t* const status = fp->status;
   const TileRange tr = fp->tiles[tile];
-  buildWarpTables(sT[warp], *fp->tables, lane);
+  const int x0 = tr.mbX0, x1 = tr.mbX1, y0 = tr.mbY0, y1 = tr.mbY1;
+  const bool wide = (x1 - x0) > kRowMax;
+  uint32_t* const gmv = reinterpret_cast<uint32_t*>(fp->mvgrid);
+  int16_t* const glv = fp->lvgrid;
+  WarpRows& rows = sR[warp];
 
-  TileCtx tc;
-  tc.lane = lane;
-  tc.x0 = tr.mbX0;
-  tc.x1 = tr.mbX1;
-  tc.y0 = tr.mbY0;
-  tc.y1 = tr.mbY1;
-  tc.mbCols = mbCols;
-  tc.rows = &sR[warp];
-  tc.wide = (tc.x1 - tc.x0) > kRowMax;
-  tc.gmv = reinterpret_cast<uint32_t*>(fp->mvgrid);
-  tc.glv = fp->lvgrid;
-  Chain& d = tc.d;
+  Chain d;
   d.buf = fp->pkt + tr.offset;
   d.pos = (int32_t)tr.length;
   d.err = 0;
-  d.t = &sT[warp];
-  const int tw = tc.x1 - tc.x0;
-  const int total = tw * (tc.y1 - tc.y0);
+  d.t = &sT;
+  const int tw = x1 - x0;
+  const int total = tw * (y1 - y0);
   int done = 0, intraCount = 0, maxLevel = -1;
   if (tr.length < (uint32_t)(kStates * 4)) {
     d.err = kErrCorrupt;  // tile stream too short to initialise rANS
@@ -469,44 +483,92 @@ __global__ void __launch_bounds__(32 * kEntropyWarps) kEntropy(const FrameDesc* 
     d.x3 = st[3];
     d.b1 = d.byteAt(d.pos - 1);
     d.b2 = d.byteAt(d.pos - 2);
-    int mbx = tc.x0, mby = tc.y0;
-    for (; done < total; done++) {
-      const int idx = mby * mbCols + mbx;
-      if (lane < 12) tc.rows->rec[lane] = 0;
-      __syncwarp();
-      uint32_t* coef = coefBase + (size_t)idx * kCoefPerMB;
-      bool intra = !inter;
-      uint32_t w;
-      if (inter) {
-        w = entropyInterMB(tc, mbx, mby, coef, &intra);
+    for (int mby = y0; mby < y1 && !d.err; mby++) {
+      // Rows as pointers indexed by the frame column: shared memory for
+      // tiles up to kRowMax macroblocks wide, the frame grid otherwise.
+      uint32_t* mvCur;
+      const uint32_t* mvUp;
+      int16_t* lvCur;
+      const int16_t* lvUp;
+      if (wide) {
+        mvCur = gmv + (size_t)mby * mbCols;
+        mvUp = mvCur - mbCols;
+        lvCur = glv + (size_t)mby * mbCols;
+        lvUp = lvCur - mbCols;
       } else {
-        w = entropyIntraMB(tc, coef);
+        const int r = (mby - y0) & 1;
+        mvCur = rows.mv[r] - x0;
+        mvUp = rows.mv[r ^ 1] - x0;
+        lvCur = rows.lvl[r] - x0;
+        lvUp = rows.lvl[r ^ 1] - x0;
       }
-      if (intra) {
-        const int lv = tc.intraLevel(mbx, mby);
-        tc.setMV(mbx, mby, 0u, w ? lv : -1);
-        if (w) {
+      const bool bOK = mby > y0;
+      uint32_t mvLeft = 0;
+      int lvLeft = -1;
+      for (int mbx = x0; mbx < x1; mbx++) {
+        const int idx = mby * mbCols + mbx;
+        Nbr n;
+        n.aOK = mbx > x0;
+        n.bOK = bOK;
+        n.arOK = bOK && mbx + 1 < x1;
+        n.cOK = n.arOK || (bOK && n.aOK);
+        n.mvA = mvLeft;
+        n.mvB = 0;
+        n.mvC = 0;
+        if (inter && bOK) {
+          n.mvB = mvUp[mbx];
+          if (n.cOK) n.mvC = mvUp[n.arOK ? mbx + 1 : mbx - 1];
+        }
+        uint32_t* coef = coefBase + (size_t)idx * kCoefPerMB;
+        Rec r;
+        r.clear();
+        bool intra = !inter;
+        uint32_t mv = 0, w = 0;
+        BlockPlan p;
+        int blocks;
+        if (inter) {
+          blocks = interHeader(d, r, n, &p, &intra, &mv, &w);
+        } else {
+          intraHeader(d, r, &p);
+          blocks = d.err ? 0 : 1;
+        }
+        if (blocks) {
+          uint32_t nz;
+          const int nd = entropyBlocks(d, r, p, coef, lane, &nz);
+          r.nz = nz;
+          w = writeMask(p, nd);
+        }
+        int lv = -1;
+        if (intra && w) {
+          // Intra dependency level: one more than the highest intra neighbour.
+          int m = n.aOK ? lvLeft : -1;
+          if (bOK) {
+            m = max(m, (int)lvUp[mbx]);
+            if (n.aOK) m = max(m, (int)lvUp[mbx - 1]);
+            if (n.arOK) m = max(m, (int)lvUp[mbx + 1]);
+          }
+          lv = m + 1;
           if (lane == 0) intraList[tr.mbBase + intraCount] = (uint32_t)idx | ((uint32_t)lv << kLevelShift);
           intraCount++;
           maxLevel = max(maxLevel, lv);
         }
-      }
-      recSet(tc, 11, w);
-      __syncwarp();
-      if (lane < 12) reinterpret_cast<uint32_t*>(recs + idx)[lane] = tc.rows->rec[lane];
-      if (d.err) {
+        if (lane == 0) {
+          mvCur[mbx] = mv;
+          lvCur[mbx] = (int16_t)lv;
+        }
+        mvLeft = mv;
+        lvLeft = lv;
+        r.wm = w;
+        r.store(recs + idx, lane);
         done++;
-        break;
+        if (d.err) break;
       }
-      if (++mbx == tc.x1) {
-        mbx = tc.x0;
-        mby++;
-      }
+      __syncwarp();  // the row just written is read as the row above
     }
   }
   // Macroblocks the tile never reached are left untouched by reconstruction.
   for (int k = done + lane; k < total; k += 32) {
-    MBRec* r = recs + (size_t)(tc.y0 + k / tw) * mbCols + tc.x0 + k % tw;
+    MBRec* r = recs + (size_t)(y0 + k / tw) * mbCols + x0 + k % tw;
     r->mode = kRecNone;
     r->wmask = 0;
   }
@@ -905,19 +967,22 @@ __global__ void __launch_bounds__(32 * kIntraWarps) kIntraRecon(const FrameDesc*
 // Launch wrappers
 // ---------------------------------------------------------------------------
 int uploadCodingTables(const int* scan4, const int* scan8, const int* scan16, const int32_t* dct) {
-  uint8_t s[3][256];
-  for (int i = 0; i < 16; i++) s[0][i] = (uint8_t)scan4[i];
-  for (int i = 0; i < 64; i++) s[1][i] = (uint8_t)scan8[i];
-  for (int i = 0; i < 256; i++) s[2][i] = (uint8_t)scan16[i];
-  if (cudaMemcpyToSymbol(dev::cScan, s, sizeof(s)) != cudaSuccess) return kErrDevice;
+  uint16_t s[3][256];
+  std::memset(s, 0, sizeof(s));
+  const int* scans[3] = {scan4, scan8, scan16};
+  for (int k = 0; k < 3; k++)
+    for (int i = 0; i < (16 << (2 * k)); i++) {
+      const int band = bandOf(i);
+      s[k][i] = (uint16_t)((uint32_t)scans[k][i] | ((uint32_t)(band * kNumPrevClass) << 8));
+    }
+  if (cudaMemcpyToSymbol(dev::cScanBand, s, sizeof(s)) != cudaSuccess) return kErrDevice;
   if (cudaMemcpyToSymbol(dev::cDct, dct, sizeof(int32_t) * 3 * 256) != cudaSuccess) return kErrDevice;
   return kOK;
 }
 
-void launchEntropy(const FrameDesc* frames, const int2* jobs, int njobs, cudaStream_t s) {
+void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, cudaStream_t s) {
   if (njobs <= 0) return;
-  const int blocks = (njobs + dev::kEntropyWarps - 1) / dev::kEntropyWarps;
-  dev::kEntropy<<<blocks, 32 * dev::kEntropyWarps, 0, s>>>(frames, jobs, njobs);
+  dev::kEntropy<<<njobs, 32 * dev::kEntropyWarps, 0, s>>>(frames, jobs, njobs);
 }
 
 void launchInter(const FrameDesc* frames, int nframes, int maxMBs, cudaStream_t s) {

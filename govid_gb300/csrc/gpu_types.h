@@ -43,6 +43,11 @@ constexpr int kCoefCr = 337;
 constexpr int kCoefPerMB = 408;
 constexpr uint32_t kWriteAll = 0x3FFFFu;
 
+// The entropy kernel decodes up to this many tiles of one frame per CTA
+// (one warp each), sharing the frame's symbol tables.  A job is
+// int4{descriptor, first tile, tile count, 0}.
+constexpr int kEntropyTilesPerJob = 4;
+
 struct TileStat {
   int32_t err;         // 0 or an ebiv status
   int32_t intraCount;  // intra macroblocks reconstructed in this tile

@@ -17,6 +17,7 @@
 // every call uploads as zero.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -30,7 +31,7 @@
 
 namespace ebiv {
 
-void launchEntropy(const FrameDesc* frames, const int2* jobs, int njobs, cudaStream_t s);
+void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, cudaStream_t s);
 void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, cudaStream_t s);
 
 namespace {
@@ -45,7 +46,9 @@ constexpr size_t kOffStatus = a256(kOffDesc + 2 * sizeof(FrameDesc));
 constexpr size_t kOffTables = a256(kOffStatus + 2 * sizeof(int32_t));
 constexpr size_t kOffTiles = a256(kOffTables + 2 * sizeof(DeviceTables));
 constexpr size_t kOffJobs = a256(kOffTiles + 2 * (size_t)kNAMaxMBs * sizeof(TileRange));
-constexpr size_t kOffRec = a256(kOffJobs + 2 * (size_t)kNAMaxMBs * sizeof(int2));  // end of the uploaded head
+constexpr size_t kNAMaxEJobs = (kNAMaxMBs + kEntropyTilesPerJob - 1) / kEntropyTilesPerJob;
+constexpr size_t kOffEJobs = a256(kOffJobs + 2 * (size_t)kNAMaxMBs * sizeof(int2));
+constexpr size_t kOffRec = a256(kOffEJobs + 2 * kNAMaxEJobs * sizeof(int4));  // end of the uploaded head
 constexpr size_t kOffCoef = a256(kOffRec + (size_t)kNAMaxMBs * sizeof(MBRec));
 constexpr size_t kOffMV = a256(kOffCoef + (size_t)kNAMaxMBs * kCoefPerMB * sizeof(uint32_t));
 constexpr size_t kOffLV = a256(kOffMV + (size_t)kNAMaxMBs * 2 * sizeof(int16_t));
@@ -199,6 +202,10 @@ extern "C" int ebivgpu_decode_key_noalloc(const uint8_t* pkt, size_t n, uint8_t*
       tr[t] = p.tiles[t];
       jb[t] = make_int2(w, (int)t);
     }
+    int4* ej = reinterpret_cast<int4*>(head.data() + kOffEJobs) + (size_t)w * kNAMaxEJobs;
+    const int nt = (int)p.tiles.size();
+    for (int t0 = 0; t0 < nt; t0 += kEntropyTilesPerJob)
+      ej[t0 / kEntropyTilesPerJob] = make_int4(w, t0, std::min(kEntropyTilesPerJob, nt - t0), 0);
   }
   int32_t status[2] = {0, 0};
   if (cudaMemcpyAsync(d, head.data(), head.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
@@ -206,10 +213,12 @@ extern "C" int ebivgpu_decode_key_noalloc(const uint8_t* pkt, size_t n, uint8_t*
     return kErrDevice;
   const FrameDesc* dd = reinterpret_cast<const FrameDesc*>(d + kOffDesc);
   const int2* dj = reinterpret_cast<const int2*>(d + kOffJobs);
+  const int4* de = reinterpret_cast<const int4*>(d + kOffEJobs);
   const int nt0 = (int)plan[0].tiles.size();
-  launchEntropy(dd, dj, nt0, s);
+  auto groups = [](int nt) { return (nt + kEntropyTilesPerJob - 1) / kEntropyTilesPerJob; };
+  launchEntropy(dd, de, groups(nt0), s);
   launchIntra(dd, dj, nt0, s);
-  if (withOv) launchEntropy(dd, dj + kNAMaxMBs, (int)plan[1].tiles.size(), s);  // after the key's recon
+  if (withOv) launchEntropy(dd, de + kNAMaxEJobs, groups((int)plan[1].tiles.size()), s);  // after the key's recon
   if (cudaMemcpyAsync(status, d + kOffStatus, sizeof(status), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess)
     return kErrDevice;
