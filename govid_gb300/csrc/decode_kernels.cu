@@ -35,7 +35,10 @@ constexpr unsigned kFull = 0xffffffffu;
 // token-context offset of the position's band, bandOf(i) * kNumPrevClass
 // (bits 8-15).
 __constant__ uint16_t cScanBand[3][256];
-__constant__ int32_t cDct[3][256];    // 2^13-scaled DCT-II basis, [k*n + i]
+// 2^13-scaled DCT-II basis, [k*n + i], per transform size.  Global memory:
+// the transforms read it with a different index in every lane, which the
+// L1 path serves in one pass and the constant cache would serialise.
+__device__ int32_t gDct[3][256];
 __constant__ int32_t cTaps[4][4] = {{0, 64, 0, 0}, {-6, 55, 18, -3}, {-8, 40, 40, -8}, {-3, 18, 55, -6}};
 
 __device__ __forceinline__ int tokenCtx(int plane, int txIdx, int band, int prevClass) {
@@ -584,37 +587,60 @@ __global__ void __launch_bounds__(32 * kEntropyWarps, 4) kEntropy(const FrameDes
 }
 
 // ---------------------------------------------------------------------------
-// Dequantization + inverse DCT of one block (warp-cooperative)
+// Dequantization + inverse DCT of a whole macroblock (warp-cooperative)
 // ---------------------------------------------------------------------------
-// Writes the n x n residual into out[r*outStride + c].  dense and tmp are
-// per-warp shared scratch of n*n words.
-__device__ void idctBlock(const uint32_t* region, int n, int32_t qdc, int32_t qac, int32_t* dense, int32_t* tmp,
-                          int32_t* out, int outStride, int lane) {
-  const int nn = n * n;
-  const int tx = n == 4 ? 0 : (n == 8 ? 1 : 2);
-  for (int i = lane; i < nn; i += 32) dense[i] = 0;
+// Every coded block of the macroblock at once (ebiv/quant.go:72-80,
+// ebiv/transform.go:129-194): bit k of mask selects luma block k of the
+// tx-sized grid, bits 16/17 the Cb/Cr 8x8 blocks.  dense and tmp are
+// per-warp scratch of 384 words; on return dense holds the luma residual
+// (16x16 raster) in words 0-255 and the Cb and Cr residuals (8x8 raster) in
+// 256-319 and 320-383, zero at the positions of unselected blocks.
+__device__ void mbResidual(const uint32_t* coef, int tx, uint32_t mask, int32_t qdc, int32_t qac, int32_t* dense,
+                           int32_t* tmp, int lane) {
+  const int n = 4 << tx, nn = n * n, per = 4 >> tx, nb = per * per;
+  for (int i = lane; i < 384; i += 32) dense[i] = 0;
   __syncwarp();
-  const int count = (int)region[0];
-  for (int e = lane; e < count; e += 32) {
-    const uint32_t v = region[1 + e];
-    const int pos = (int)(v & 0xFF);
-    const int32_t lvl = (int32_t)v >> 8;
-    dense[pos] = wmul(lvl, pos == 0 ? qdc : qac);
+  // Scatter the sparse levels: luma block b at dense[b*nn], Cb at 256, Cr at 320.
+  for (int b = 0; b < nb + 2; b++) {
+    const bool luma = b < nb;
+    if (!((mask >> (luma ? b : 16 + b - nb)) & 1)) continue;
+    const uint32_t* region = coef + (luma ? b * (nn + 1) : (b == nb ? kCoefCb : kCoefCr));
+    int32_t* d = dense + (luma ? b * nn : 256 + (b - nb) * 64);
+    const int count = (int)region[0];
+    for (int e = lane; e < count; e += 32) {
+      const uint32_t v = region[1 + e];
+      const int pos = (int)(v & 0xFF);
+      d[pos] = wmul((int32_t)v >> 8, pos == 0 ? qdc : qac);
+    }
   }
   __syncwarp();
-  const int32_t* c = cDct[tx];
-  for (int o = lane; o < nn; o += 32) {
-    const int i = o / n, l = o - i * n;
+  // Columns: tmp[b][i][l] = sum_k c[k][i] * dense[b][k][l].
+  for (int o = lane; o < 384; o += 32) {
+    const bool luma = o < 256;
+    const int bn = luma ? n : 8, base = luma ? (o / nn) * nn : 256 + ((o - 256) >> 6) * 64;
+    const int q = o - base, i = q / bn, l = q - i * bn;
+    const int32_t* c = gDct[luma ? tx : 1];
     int64_t acc = 0;
-    for (int k = 0; k < n; k++) acc += (int64_t)c[k * n + i] * (int64_t)dense[k * n + l];
+    for (int k = 0; k < bn; k++) acc += (int64_t)__ldg(c + k * bn + i) * (int64_t)dense[base + k * bn + l];
     tmp[o] = (int32_t)((acc + 4096) >> 13);
   }
   __syncwarp();
-  for (int o = lane; o < nn; o += 32) {
-    const int i = o / n, m = o - i * n;
+  // Rows: out[i][m] = sum_l c[l][m] * tmp[b][i][l], into dense (read only
+  // by the column pass, which is complete).
+  for (int o = lane; o < 384; o += 32) {
+    const bool luma = o < 256;
+    const int bn = luma ? n : 8, base = luma ? (o / nn) * nn : 256 + ((o - 256) >> 6) * 64;
+    const int q = o - base, i = q / bn, m = q - i * bn;
+    const int32_t* c = gDct[luma ? tx : 1];
     int64_t acc = 0;
-    for (int l = 0; l < n; l++) acc += (int64_t)c[l * n + m] * (int64_t)tmp[i * n + l];
-    out[i * outStride + m] = (int32_t)((acc + 4096) >> 13);
+    for (int l = 0; l < bn; l++) acc += (int64_t)__ldg(c + l * bn + m) * (int64_t)tmp[base + i * bn + l];
+    const int32_t v = (int32_t)((acc + 4096) >> 13);
+    if (luma) {
+      const int b = o / nn, bx = (b % per) * n, by = (b / per) * n;
+      dense[(by + i) * 16 + bx + m] = v;
+    } else {
+      dense[o] = v;
+    }
   }
   __syncwarp();
 }
@@ -667,9 +693,8 @@ __device__ __forceinline__ int partIndex(int part, int x, int y) {  // luma coor
 constexpr int kInterWarps = 4;
 
 struct InterScratch {
-  int32_t res[256];
-  int32_t dense[256];
-  int32_t tmp[256];
+  int32_t res[384];  // levels, then residuals (mbResidual)
+  int32_t tmp[384];
 };
 
 __global__ void __launch_bounds__(32 * kInterWarps) kInterRecon(const FrameDesc* frames) {
@@ -695,6 +720,14 @@ __global__ void __launch_bounds__(32 * kInterWarps) kInterRecon(const FrameDesc*
   const int part = mode == kRecInter ? r.part : partWhole;
   const int cbp = mode == kRecInter ? r.cbp : 0;
 
+  // Residuals of the coded blocks that are written, all at once.
+  uint32_t resMask = 0;
+  if (cbp & cbpLuma) resMask |= r.nzmask & wm & 0xFFFFu;
+  if (cbp & cbpCb) resMask |= r.nzmask & wm & (1u << 16);
+  if (cbp & cbpCr) resMask |= r.nzmask & wm & (1u << 17);
+  if (resMask)
+    mbResidual(f.coef + (size_t)idx * kCoefPerMB, r.tx, resMask, f.qdc, f.qac, S.res, S.tmp, lane);
+
   // Luma: lane -> row lane/2, 8 columns.
   {
     const int row = lane >> 1, c0 = (lane & 1) * 8;
@@ -705,33 +738,17 @@ __global__ void __launch_bounds__(32 * kInterWarps) kInterRecon(const FrameDesc*
     int pred[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) pred[k] = lumaSample(refp[0], f.strideY, f.padW, f.padH, sx + k, sy, fx, fy);
-    const bool coded = (cbp & cbpLuma) != 0;
-    const int tx = r.tx, n = 4 << tx, per = 4 >> tx;
-    if (coded) {
-      const int nb = per * per;
-      for (int k = 0; k < nb; k++) {
-        if (!((wm >> k) & 1)) continue;
-        const int bx = (k % per) * n, by = (k / per) * n;
-        if ((r.nzmask >> k) & 1) {
-          idctBlock(f.coef + (size_t)idx * kCoefPerMB + k * (n * n + 1), n, f.qdc, f.qac, S.dense, S.tmp,
-                    S.res + by * 16 + bx, 16, lane);
-        } else {
-          for (int i = lane; i < n * n; i += 32) S.res[(by + i / n) * 16 + bx + i % n] = 0;
-          __syncwarp();
-        }
-      }
-    }
+    const int n = 4 << r.tx, per = 4 >> r.tx;
     uint8_t* out = f.rec[0] + (size_t)(mby * 16 + row) * f.strideY + mbx * 16 + c0;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
       const int c = c0 + k;
       const int blk = (row / n) * per + c / n;
       if (!((wm >> blk) & 1)) continue;
-      const int v = coded ? clampByteD(wadd(pred[k], S.res[row * 16 + c])) : pred[k];
+      const int v = resMask ? clampByteD(wadd(pred[k], S.res[row * 16 + c])) : pred[k];
       out[k] = (uint8_t)v;
     }
   }
-  __syncwarp();
   // Chroma: lane -> row lane/4, 2 columns; Cb then Cr.
 #pragma unroll
   for (int pl = 0; pl < 2; pl++) {
@@ -744,15 +761,9 @@ __global__ void __launch_bounds__(32 * kInterWarps) kInterRecon(const FrameDesc*
     const int sx = mbx * 8 + c0 + (mvx >> 3), sy = mby * 8 + row + (mvy >> 3);
     int p0 = chromaSample(refp[1 + pl], f.strideC, f.padCW, f.padCH, sx, sy, fx, fy);
     int p1 = chromaSample(refp[1 + pl], f.strideC, f.padCW, f.padCH, sx + 1, sy, fx, fy);
-    const bool coded = (cbp & (cbpCb << pl)) != 0;
-    if (coded) {
-      if (r.nzmask & bit) {
-        idctBlock(f.coef + (size_t)idx * kCoefPerMB + (pl ? kCoefCr : kCoefCb), 8, f.qdc, f.qac, S.dense, S.tmp,
-                  S.res, 8, lane);
-        p0 = clampByteD(wadd(p0, S.res[row * 8 + c0]));
-        p1 = clampByteD(wadd(p1, S.res[row * 8 + c0 + 1]));
-        __syncwarp();
-      }
+    if (resMask & bit) {
+      p0 = clampByteD(wadd(p0, S.res[256 + pl * 64 + row * 8 + c0]));
+      p1 = clampByteD(wadd(p1, S.res[256 + pl * 64 + row * 8 + c0 + 1]));
     }
     uint8_t* out = f.rec[1 + pl] + (size_t)(mby * 8 + row) * f.strideC + mbx * 8 + c0;
     out[0] = (uint8_t)p0;
@@ -765,28 +776,36 @@ __global__ void __launch_bounds__(32 * kInterWarps) kInterRecon(const FrameDesc*
 // ---------------------------------------------------------------------------
 constexpr int kIntraWarps = 8;
 
+// Per-warp scratch of the intra stage.  The macroblock being reconstructed
+// lives in a working area in shared memory together with the samples its
+// prediction may read: area row 0 is the row above the macroblock (from one
+// left of it to 31 right of its left edge: above-left corner, above,
+// above-right), column 0 the column to its left; chroma likewise (9 x 9).
+constexpr int kAreaW = 48;
 struct IntraScratch {
   int32_t ref[4 * 16 + 1];
-  int32_t res[256];
-  int32_t dense[256];
-  int32_t tmp[256];
+  int32_t res[384];  // levels, then residuals (mbResidual)
+  int32_t tmp[384];
+  uint8_t areaY[17 * kAreaW];
+  uint8_t areaC[2][9 * 16];
 };
 
 // The reference sample array of predictIntra after substituteRefs, in
 // closed form: ref[0..2n-1] left column bottom-to-top, ref[2n] corner,
-// ref[2n+1..4n] top then top-right.
-__device__ __forceinline__ int32_t refValue(int i, int n, bool avAbove, bool avLeft, bool avAR, const uint8_t* p,
-                                            int stride, int x0, int y0) {
+// ref[2n+1..4n] top then top-right.  (x0, y0) are the block's coordinates
+// in the working area a (row stride as).
+__device__ __forceinline__ int32_t refValue(int i, int n, bool avAbove, bool avLeft, bool avAR, const uint8_t* a,
+                                            int as, int x0, int y0) {
   const int corner = 2 * n;
-  auto L = [&](int r) -> int32_t { return p[(size_t)(y0 + r) * stride + x0 - 1]; };
-  auto Tp = [&](int j) -> int32_t { return p[(size_t)(y0 - 1) * stride + x0 + j]; };
+  auto L = [&](int r) -> int32_t { return a[(y0 + r) * as + x0 - 1]; };
+  auto Tp = [&](int j) -> int32_t { return a[(y0 - 1) * as + x0 + j]; };
   if (!avLeft && !avAbove) return kDCPred;
   if (i < corner) {
     const int row = 2 * n - 1 - i;
     return avLeft ? L(row < n ? row : n - 1) : Tp(0);
   }
   if (i == corner) {
-    if (avLeft && avAbove) return p[(size_t)(y0 - 1) * stride + x0 - 1];
+    if (avLeft && avAbove) return a[(y0 - 1) * as + x0 - 1];
     return avLeft ? L(0) : Tp(0);
   }
   const int j = i - corner - 1;
@@ -794,11 +813,14 @@ __device__ __forceinline__ int32_t refValue(int i, int n, bool avAbove, bool avL
   return L(0);
 }
 
-// Predicts and reconstructs one n x n block at (x0,y0) of plane p.
-__device__ void intraBlock(IntraScratch& S, uint8_t* p, int stride, int x0, int y0, int n, int mode, bool avAbove,
-                           bool avLeft, bool avAR, bool hasRes, int lane) {
+// Predicts and reconstructs one n x n block (predictIntra,
+// ebiv/predict.go:131-219) at area coordinates (ax, ay) of working area a,
+// writing each sample to the area and to plane p at (px, py).
+__device__ void intraBlock(IntraScratch& S, uint8_t* a, int as, int ax, int ay, uint8_t* p, int stride, int px,
+                           int py, int n, int mode, bool avAbove, bool avLeft, bool avAR, const int32_t* res,
+                           int resStride, int lane) {
   const int corner = 2 * n;
-  for (int i = lane; i <= 4 * n; i += 32) S.ref[i] = refValue(i, n, avAbove, avLeft, avAR, p, stride, x0, y0);
+  for (int i = lane; i <= 4 * n; i += 32) S.ref[i] = refValue(i, n, avAbove, avLeft, avAR, a, as, ax, ay);
   __syncwarp();
   int32_t dc = 0;
   if (mode == modeDC) {
@@ -818,9 +840,7 @@ __device__ void intraBlock(IntraScratch& S, uint8_t* p, int stride, int x0, int 
     default: break;
   }
   const int nn = n * n;
-  int32_t vals[8];
-  int cnt = 0;
-  for (int o = lane; o < nn; o += 32, cnt++) {
+  for (int o = lane; o < nn; o += 32) {
     const int r = o / n, c = o - r * n;
     int32_t v;
     switch (mode) {
@@ -829,8 +849,8 @@ __device__ void intraBlock(IntraScratch& S, uint8_t* p, int stride, int x0, int 
       case modeTM: v = clampByteD(S.ref[corner + 1 + c] + S.ref[corner - 1 - r] - S.ref[corner]); break;
       case modeDC: v = dc; break;
       default: {
-        const int a = vertical ? r : c, b = vertical ? c : r;
-        const int pos = (a + 1) * angle;
+        const int aa = vertical ? r : c, b = vertical ? c : r;
+        const int pos = (aa + 1) * angle;
         const int idx = pos >> 5, fact = pos & 31;
         auto ext = [&](int k) -> int32_t {
           if (k >= 0) {
@@ -843,15 +863,9 @@ __device__ void intraBlock(IntraScratch& S, uint8_t* p, int stride, int x0, int 
         v = ((32 - fact) * ext(b + idx + 1) + fact * ext(b + idx + 2) + 16) >> 5;
       }
     }
-    if (hasRes) v = clampByteD(wadd(v, S.res[r * n + c]));
-    else v = clampByteD(v);
-    vals[cnt] = v;
-  }
-  __syncwarp();  // every lane has read its neighbours before anyone writes
-  cnt = 0;
-  for (int o = lane; o < nn; o += 32, cnt++) {
-    const int r = o / n, c = o - r * n;
-    p[(size_t)(y0 + r) * stride + x0 + c] = (uint8_t)vals[cnt];
+    v = res ? clampByteD(wadd(v, res[r * resStride + c])) : clampByteD(v);
+    a[(ay + r) * as + ax + c] = (uint8_t)v;  // the block's reference array is already in S.ref
+    p[(size_t)(py + r) * stride + px + c] = (uint8_t)v;
   }
   __syncwarp();
 }
@@ -864,17 +878,38 @@ __device__ void intraMB(const FrameDesc& f, IntraScratch& S, int mbx, int mby, i
   if (!wm) return;
   const int tx = r.tx, n = 4 << tx, per = 4 >> tx, nb = per * per;
   const int tileLeft = tx0 * 16, tileTop = ty0 * 16, tileRight = tx1 * 16;
-  const int mbTop = mby * 16, mbRight = (mbx + 1) * 16;
-  const uint32_t* coef = f.coef + (size_t)idx * kCoefPerMB;
+  const int mbLeft = mbx * 16, mbTop = mby * 16, mbRight = mbLeft + 16;
+  const uint32_t resMask = r.nzmask & wm;
+  if (resMask)
+    mbResidual(f.coef + (size_t)idx * kCoefPerMB, tx, resMask, f.qdc, f.qac, S.res, S.tmp, lane);
+  // Working areas: the row above and the column to the left, where they
+  // lie inside the tile (nothing outside it is ever predicted from).
+  {
+    const uint8_t* Y = f.rec[0];
+    const bool up = mbTop > tileTop, left = mbLeft > tileLeft;
+    for (int i = lane; i < 33; i += 32) {
+      const int x = mbLeft - 1 + i;
+      if (up && x >= tileLeft && x < tileRight) S.areaY[i] = Y[(size_t)(mbTop - 1) * f.strideY + x];
+    }
+    if (left && lane < 16) S.areaY[(1 + lane) * kAreaW] = Y[(size_t)(mbTop + lane) * f.strideY + mbLeft - 1];
+    const int cl = mbx * 8, ct = mby * 8;
+    for (int pl = 0; pl < 2; pl++) {
+      const uint8_t* C = f.rec[1 + pl];
+      if (up && lane < 9 && (lane > 0 || left)) S.areaC[pl][lane] = C[(size_t)(ct - 1) * f.strideC + cl - 1 + lane];
+      if (left && lane < 8) S.areaC[pl][(1 + lane) * 16] = C[(size_t)(ct + lane) * f.strideC + cl - 1];
+    }
+    __syncwarp();
+  }
   for (int k = 0; k < nb; k++) {
     if (!((wm >> k) & 1)) break;
-    const int x0 = mbx * 16 + (k % per) * n, y0 = mby * 16 + (k / per) * n;
+    const int bx = (k % per) * n, by = (k / per) * n;
+    const int x0 = mbLeft + bx, y0 = mbTop + by;
     const bool avAbove = y0 > tileTop, avLeft = x0 > tileLeft;
     bool avAR = false;
     if (!(y0 <= tileTop || x0 + 2 * n > tileRight)) avAR = (y0 == mbTop) ? true : (x0 + 2 * n <= mbRight);
     const bool hasRes = (r.nzmask >> k) & 1;
-    if (hasRes) idctBlock(coef + k * (n * n + 1), n, f.qdc, f.qac, S.dense, S.tmp, S.res, n, lane);
-    intraBlock(S, f.rec[0], f.strideY, x0, y0, n, r.lmode[k], avAbove, avLeft, avAR, hasRes, lane);
+    intraBlock(S, S.areaY, kAreaW, 1 + bx, 1 + by, f.rec[0], f.strideY, x0, y0, n, r.lmode[k], avAbove, avLeft,
+               avAR, hasRes ? S.res + by * 16 + bx : nullptr, 16, lane);
   }
   const int cx0 = mbx * 8, cy0 = mby * 8;
   const bool cAbove = cy0 > ty0 * 8, cLeft = cx0 > tx0 * 8;
@@ -882,19 +917,19 @@ __device__ void intraMB(const FrameDesc& f, IntraScratch& S, int mbx, int mby, i
     const uint32_t bit = 1u << (16 + pl);
     if (!(wm & bit)) break;
     const bool hasRes = (r.nzmask & bit) != 0;
-    if (hasRes) idctBlock(coef + (pl ? kCoefCr : kCoefCb), 8, f.qdc, f.qac, S.dense, S.tmp, S.res, 8, lane);
-    intraBlock(S, f.rec[1 + pl], f.strideC, cx0, cy0, 8, r.cmode, cAbove, cLeft, false, hasRes, lane);
+    intraBlock(S, S.areaC[pl], 16, 1, 1, f.rec[1 + pl], f.strideC, cx0, cy0, 8, r.cmode, cAbove, cLeft, false,
+               hasRes ? S.res + 256 + pl * 64 : nullptr, 8, lane);
   }
 }
 
-constexpr int kLevelBuckets = 2048;
+constexpr int kLevelBuckets = 1024;  // tiles with more intra levels take the scan path
 
 // One CTA per tile.  The tile's intra macroblocks (listed by the entropy
 // stage with their dependency levels) are counting-sorted by level, then each
 // level is reconstructed in parallel with a CTA barrier between levels.  Key
 // frames get the classic wavefront (level = x + 2y); inter frames with a few
 // isolated intra macroblocks take one or two levels.
-__global__ void __launch_bounds__(32 * kIntraWarps) kIntraRecon(const FrameDesc* frames, const int2* jobs, int njobs) {
+__global__ void __launch_bounds__(32 * kIntraWarps, 1) kIntraRecon(const FrameDesc* frames, const int2* jobs, int njobs) {
   __shared__ IntraScratch sS[kIntraWarps];
   __shared__ int sStart[kLevelBuckets + 1];
   __shared__ int sCur[kLevelBuckets];
@@ -976,7 +1011,7 @@ int uploadCodingTables(const int* scan4, const int* scan8, const int* scan16, co
       s[k][i] = (uint16_t)((uint32_t)scans[k][i] | ((uint32_t)(band * kNumPrevClass) << 8));
     }
   if (cudaMemcpyToSymbol(dev::cScanBand, s, sizeof(s)) != cudaSuccess) return kErrDevice;
-  if (cudaMemcpyToSymbol(dev::cDct, dct, sizeof(int32_t) * 3 * 256) != cudaSuccess) return kErrDevice;
+  if (cudaMemcpyToSymbol(dev::gDct, dct, sizeof(int32_t) * 3 * 256) != cudaSuccess) return kErrDevice;
   return kOK;
 }
 
