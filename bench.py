@@ -539,7 +539,7 @@ def main():
     ap.add_argument("--frames", type=int, default=FRAMES)
     ap.add_argument("--mix-frames", type=int, default=120)
     ap.add_argument("--mix-distinct", type=int, default=1)
-    ap.add_argument("--lookahead", type=int, default=8)
+    ap.add_argument("--lookahead", type=int, default=32)
     ap.add_argument("--mix-lookahead", type=int, default=4)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serve", action="store_true")

@@ -600,17 +600,49 @@ __device__ void mbResidual(const uint32_t* coef, int tx, uint32_t mask, int32_t 
   const int n = 4 << tx, nn = n * n, per = 4 >> tx, nb = per * per;
   for (int i = lane; i < 384; i += 32) dense[i] = 0;
   __syncwarp();
-  // Scatter the sparse levels: luma block b at dense[b*nn], Cb at 256, Cr at 320.
-  for (int b = 0; b < nb + 2; b++) {
-    const bool luma = b < nb;
-    if (!((mask >> (luma ? b : 16 + b - nb)) & 1)) continue;
-    const uint32_t* region = coef + (luma ? b * (nn + 1) : (b == nb ? kCoefCb : kCoefCr));
-    int32_t* d = dense + (luma ? b * nn : 256 + (b - nb) * 64);
-    const int count = (int)region[0];
-    for (int e = lane; e < count; e += 32) {
-      const uint32_t v = region[1 + e];
-      const int pos = (int)(v & 0xFF);
-      d[pos] = wmul((int32_t)v >> 8, pos == 0 ? qdc : qac);
+  // Scatter the sparse levels (luma block b at dense[b*nn], Cb at 256, Cr at
+  // 320).  Lane b reads block b's count; the entries of all blocks are then
+  // fetched as one flattened list, up to four per lane in flight.
+  const int nEnt = nb + 2;
+  int myCount = 0;
+  if (lane < nEnt) {
+    const bool luma = lane < nb;
+    if ((mask >> (luma ? lane : 16 + lane - nb)) & 1)
+      myCount = (int)coef[luma ? lane * (nn + 1) : (lane == nb ? kCoefCb : kCoefCr)];
+  }
+  int incl = myCount;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int total = __shfl_sync(kFull, incl, 31);
+  const int excl = incl - myCount;
+  for (int t0 = 0; t0 < total; t0 += 128) {
+    uint32_t val[4];
+    int dst[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int t = t0 + u * 32 + lane;
+      int ob = 0, oe = 0;
+      for (int b = 0; b < nEnt; b++) {  // owning block: last nonempty block starting at or before t
+        const int eb = __shfl_sync(kFull, excl, b), cb = __shfl_sync(kFull, myCount, b);
+        if (cb > 0 && eb <= t) {
+          ob = b;
+          oe = eb;
+        }
+      }
+      const bool luma = ob < nb;
+      dst[u] = -1;
+      if (t < total) {
+        val[u] = coef[(luma ? ob * (nn + 1) : (ob == nb ? kCoefCb : kCoefCr)) + 1 + (t - oe)];
+        dst[u] = luma ? ob * nn : 256 + (ob - nb) * 64;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      if (dst[u] < 0) continue;
+      const int pos = (int)(val[u] & 0xFF);
+      dense[dst[u] + pos] = wmul((int32_t)val[u] >> 8, pos == 0 ? qdc : qac);
     }
   }
   __syncwarp();
@@ -688,6 +720,64 @@ __device__ __forceinline__ int partIndex(int part, int x, int y) {  // luma coor
 }
 
 // ---------------------------------------------------------------------------
+// Register copies for the reconstruction kernels.  Their byte stores to the
+// planes may alias any other memory as far as the compiler knows, so fields
+// read through the descriptor or record pointers would be re-loaded after
+// every store; these copies are read once.
+// ---------------------------------------------------------------------------
+struct ReconView {
+  uint8_t* rec[3];
+  const uint8_t* ref[3];
+  const uint8_t* gold[3];
+  int strideY, strideC, padW, padH, padCW, padCH, mbCols;
+  int32_t qdc, qac;
+  const MBRec* mbrec;
+  const uint32_t* coef;
+  __device__ __forceinline__ void load(const FrameDesc& f) {
+    for (int k = 0; k < 3; k++) {
+      rec[k] = f.rec[k];
+      ref[k] = f.ref[k];
+      gold[k] = f.gold[k];
+    }
+    strideY = f.strideY;
+    strideC = f.strideC;
+    padW = f.padW;
+    padH = f.padH;
+    padCW = f.padCW;
+    padCH = f.padCH;
+    mbCols = f.mbCols;
+    qdc = f.qdc;
+    qac = f.qac;
+    mbrec = f.mbrec;
+    coef = f.coef;
+  }
+};
+
+// A macroblock record as three 16-byte words (see MBRec).
+struct RecRegs {
+  uint4 a, b, c;  // words 0-3, 4-7, 8-11
+  __device__ __forceinline__ void load(const MBRec* p) {
+    const uint4* q = reinterpret_cast<const uint4*>(p);
+    a = q[0];
+    b = q[1];
+    c = q[2];
+  }
+  __device__ __forceinline__ int mode() const { return (int)(a.x & 0xFF); }
+  __device__ __forceinline__ int ref() const { return (int)((a.x >> 8) & 0xFF); }
+  __device__ __forceinline__ int part() const { return (int)((a.x >> 16) & 0xFF); }
+  __device__ __forceinline__ int cbp() const { return (int)(a.x >> 24); }
+  __device__ __forceinline__ int tx() const { return (int)(a.y & 0xFF); }
+  __device__ __forceinline__ int cmode() const { return (int)((a.y >> 8) & 0xFF); }
+  __device__ __forceinline__ uint32_t mv(int i) const { return i == 0 ? a.z : (i == 1 ? a.w : (i == 2 ? b.x : b.y)); }
+  __device__ __forceinline__ int lmode(int k) const {
+    const uint32_t w = k < 8 ? (k < 4 ? b.z : b.w) : (k < 12 ? c.x : c.y);
+    return (int)((w >> ((k & 3) * 8)) & 0xFF);
+  }
+  __device__ __forceinline__ uint32_t nzmask() const { return c.z; }
+  __device__ __forceinline__ uint32_t wmask() const { return c.w; }
+};
+
+// ---------------------------------------------------------------------------
 // Stage B1: inter macroblock reconstruction
 // ---------------------------------------------------------------------------
 constexpr int kInterWarps = 4;
@@ -708,38 +798,42 @@ __global__ void __launch_bounds__(32 * kInterWarps) kInterRecon(const FrameDesc*
   if (!f.inter) return;
   const int idx = blockIdx.x * kInterWarps + warp;
   if (idx >= f.mbCols * f.mbRows) return;
-  const MBRec& r = f.mbrec[idx];
-  const int mode = r.mode;
+  ReconView v;
+  v.load(f);
+  RecRegs r;
+  r.load(v.mbrec + idx);
+  const int mode = r.mode();
   if (mode != kRecSkip && mode != kRecInter) return;
-  const uint32_t wm = r.wmask;
+  const uint32_t wm = r.wmask();
   if (!wm) return;
   InterScratch& S = sS[warp];
-  const int mbx = idx % f.mbCols, mby = idx / f.mbCols;
-  const bool golden = mode == kRecInter && r.ref == refGolden;
-  const uint8_t* const* refp = golden ? f.gold : f.ref;
-  const int part = mode == kRecInter ? r.part : partWhole;
-  const int cbp = mode == kRecInter ? r.cbp : 0;
+  const int mbx = idx % v.mbCols, mby = idx / v.mbCols;
+  const bool golden = mode == kRecInter && r.ref() == refGolden;
+  const uint8_t* const* refp = golden ? v.gold : v.ref;
+  const int part = mode == kRecInter ? r.part() : partWhole;
+  const int cbp = mode == kRecInter ? r.cbp() : 0;
+  const uint32_t nzm = r.nzmask();
+  const int tx = r.tx();
 
   // Residuals of the coded blocks that are written, all at once.
   uint32_t resMask = 0;
-  if (cbp & cbpLuma) resMask |= r.nzmask & wm & 0xFFFFu;
-  if (cbp & cbpCb) resMask |= r.nzmask & wm & (1u << 16);
-  if (cbp & cbpCr) resMask |= r.nzmask & wm & (1u << 17);
-  if (resMask)
-    mbResidual(f.coef + (size_t)idx * kCoefPerMB, r.tx, resMask, f.qdc, f.qac, S.res, S.tmp, lane);
+  if (cbp & cbpLuma) resMask |= nzm & wm & 0xFFFFu;
+  if (cbp & cbpCb) resMask |= nzm & wm & (1u << 16);
+  if (cbp & cbpCr) resMask |= nzm & wm & (1u << 17);
+  if (resMask) mbResidual(v.coef + (size_t)idx * kCoefPerMB, tx, resMask, v.qdc, v.qac, S.res, S.tmp, lane);
 
   // Luma: lane -> row lane/2, 8 columns.
   {
     const int row = lane >> 1, c0 = (lane & 1) * 8;
-    const int pi = partIndex(part, c0, row);
-    const int mvx = r.mv[pi][0], mvy = r.mv[pi][1];
+    const uint32_t m = r.mv(partIndex(part, c0, row));
+    const int mvx = (int16_t)(m & 0xFFFFu), mvy = (int16_t)(m >> 16);
     const int fx = mvx & 3, fy = mvy & 3;
     const int sx = mbx * 16 + c0 + (mvx >> 2), sy = mby * 16 + row + (mvy >> 2);
     int pred[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) pred[k] = lumaSample(refp[0], f.strideY, f.padW, f.padH, sx + k, sy, fx, fy);
-    const int n = 4 << r.tx, per = 4 >> r.tx;
-    uint8_t* out = f.rec[0] + (size_t)(mby * 16 + row) * f.strideY + mbx * 16 + c0;
+    for (int k = 0; k < 8; k++) pred[k] = lumaSample(refp[0], v.strideY, v.padW, v.padH, sx + k, sy, fx, fy);
+    const int n = 4 << tx, per = 4 >> tx;
+    uint8_t* out = v.rec[0] + (size_t)(mby * 16 + row) * v.strideY + mbx * 16 + c0;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
       const int c = c0 + k;
@@ -755,17 +849,17 @@ __global__ void __launch_bounds__(32 * kInterWarps) kInterRecon(const FrameDesc*
     const uint32_t bit = 1u << (16 + pl);
     if (!(wm & bit)) continue;
     const int row = lane >> 2, c0 = (lane & 3) * 2;
-    const int pi = partIndex(part, c0 * 2, row * 2);
-    const int mvx = r.mv[pi][0], mvy = r.mv[pi][1];
+    const uint32_t m = r.mv(partIndex(part, c0 * 2, row * 2));
+    const int mvx = (int16_t)(m & 0xFFFFu), mvy = (int16_t)(m >> 16);
     const int fx = mvx & 7, fy = mvy & 7;
     const int sx = mbx * 8 + c0 + (mvx >> 3), sy = mby * 8 + row + (mvy >> 3);
-    int p0 = chromaSample(refp[1 + pl], f.strideC, f.padCW, f.padCH, sx, sy, fx, fy);
-    int p1 = chromaSample(refp[1 + pl], f.strideC, f.padCW, f.padCH, sx + 1, sy, fx, fy);
+    int p0 = chromaSample(refp[1 + pl], v.strideC, v.padCW, v.padCH, sx, sy, fx, fy);
+    int p1 = chromaSample(refp[1 + pl], v.strideC, v.padCW, v.padCH, sx + 1, sy, fx, fy);
     if (resMask & bit) {
       p0 = clampByteD(wadd(p0, S.res[256 + pl * 64 + row * 8 + c0]));
       p1 = clampByteD(wadd(p1, S.res[256 + pl * 64 + row * 8 + c0 + 1]));
     }
-    uint8_t* out = f.rec[1 + pl] + (size_t)(mby * 8 + row) * f.strideC + mbx * 8 + c0;
+    uint8_t* out = v.rec[1 + pl] + (size_t)(mby * 8 + row) * v.strideC + mbx * 8 + c0;
     out[0] = (uint8_t)p0;
     out[1] = (uint8_t)p1;
   }
@@ -870,33 +964,35 @@ __device__ void intraBlock(IntraScratch& S, uint8_t* a, int as, int ax, int ay, 
   __syncwarp();
 }
 
-__device__ void intraMB(const FrameDesc& f, IntraScratch& S, int mbx, int mby, int tx0, int tx1, int ty0, int lane) {
+__device__ void intraMB(const ReconView& f, IntraScratch& S, int mbx, int mby, int tx0, int tx1, int ty0, int lane) {
   const int idx = mby * f.mbCols + mbx;
-  const MBRec& r = f.mbrec[idx];
-  if (r.mode != kRecIntra) return;
-  const uint32_t wm = r.wmask;
+  RecRegs r;
+  r.load(f.mbrec + idx);
+  if (r.mode() != kRecIntra) return;
+  const uint32_t wm = r.wmask();
   if (!wm) return;
-  const int tx = r.tx, n = 4 << tx, per = 4 >> tx, nb = per * per;
+  const uint32_t nzm = r.nzmask();
+  const int tx = r.tx(), n = 4 << tx, per = 4 >> tx, nb = per * per;
   const int tileLeft = tx0 * 16, tileTop = ty0 * 16, tileRight = tx1 * 16;
   const int mbLeft = mbx * 16, mbTop = mby * 16, mbRight = mbLeft + 16;
-  const uint32_t resMask = r.nzmask & wm;
-  if (resMask)
-    mbResidual(f.coef + (size_t)idx * kCoefPerMB, tx, resMask, f.qdc, f.qac, S.res, S.tmp, lane);
+  uint8_t* const Y = f.rec[0];
+  const int ys = f.strideY, cs = f.strideC;
+  const uint32_t resMask = nzm & wm;
+  if (resMask) mbResidual(f.coef + (size_t)idx * kCoefPerMB, tx, resMask, f.qdc, f.qac, S.res, S.tmp, lane);
   // Working areas: the row above and the column to the left, where they
   // lie inside the tile (nothing outside it is ever predicted from).
+  const bool up = mbTop > tileTop, left = mbLeft > tileLeft;
   {
-    const uint8_t* Y = f.rec[0];
-    const bool up = mbTop > tileTop, left = mbLeft > tileLeft;
     for (int i = lane; i < 33; i += 32) {
       const int x = mbLeft - 1 + i;
-      if (up && x >= tileLeft && x < tileRight) S.areaY[i] = Y[(size_t)(mbTop - 1) * f.strideY + x];
+      if (up && x >= tileLeft && x < tileRight) S.areaY[i] = Y[(size_t)(mbTop - 1) * ys + x];
     }
-    if (left && lane < 16) S.areaY[(1 + lane) * kAreaW] = Y[(size_t)(mbTop + lane) * f.strideY + mbLeft - 1];
+    if (left && lane < 16) S.areaY[(1 + lane) * kAreaW] = Y[(size_t)(mbTop + lane) * ys + mbLeft - 1];
     const int cl = mbx * 8, ct = mby * 8;
     for (int pl = 0; pl < 2; pl++) {
       const uint8_t* C = f.rec[1 + pl];
-      if (up && lane < 9 && (lane > 0 || left)) S.areaC[pl][lane] = C[(size_t)(ct - 1) * f.strideC + cl - 1 + lane];
-      if (left && lane < 8) S.areaC[pl][(1 + lane) * 16] = C[(size_t)(ct + lane) * f.strideC + cl - 1];
+      if (up && lane < 9 && (lane > 0 || left)) S.areaC[pl][lane] = C[(size_t)(ct - 1) * cs + cl - 1 + lane];
+      if (left && lane < 8) S.areaC[pl][(1 + lane) * 16] = C[(size_t)(ct + lane) * cs + cl - 1];
     }
     __syncwarp();
   }
@@ -907,17 +1003,17 @@ __device__ void intraMB(const FrameDesc& f, IntraScratch& S, int mbx, int mby, i
     const bool avAbove = y0 > tileTop, avLeft = x0 > tileLeft;
     bool avAR = false;
     if (!(y0 <= tileTop || x0 + 2 * n > tileRight)) avAR = (y0 == mbTop) ? true : (x0 + 2 * n <= mbRight);
-    const bool hasRes = (r.nzmask >> k) & 1;
-    intraBlock(S, S.areaY, kAreaW, 1 + bx, 1 + by, f.rec[0], f.strideY, x0, y0, n, r.lmode[k], avAbove, avLeft,
-               avAR, hasRes ? S.res + by * 16 + bx : nullptr, 16, lane);
+    const bool hasRes = (nzm >> k) & 1;
+    intraBlock(S, S.areaY, kAreaW, 1 + bx, 1 + by, Y, ys, x0, y0, n, r.lmode(k), avAbove, avLeft, avAR,
+               hasRes ? S.res + by * 16 + bx : nullptr, 16, lane);
   }
   const int cx0 = mbx * 8, cy0 = mby * 8;
-  const bool cAbove = cy0 > ty0 * 8, cLeft = cx0 > tx0 * 8;
+  const int cmode = r.cmode();
   for (int pl = 0; pl < 2; pl++) {
     const uint32_t bit = 1u << (16 + pl);
     if (!(wm & bit)) break;
-    const bool hasRes = (r.nzmask & bit) != 0;
-    intraBlock(S, S.areaC[pl], 16, 1, 1, f.rec[1 + pl], f.strideC, cx0, cy0, 8, r.cmode, cAbove, cLeft, false,
+    const bool hasRes = (nzm & bit) != 0;
+    intraBlock(S, S.areaC[pl], 16, 1, 1, f.rec[1 + pl], cs, cx0, cy0, 8, cmode, up, left, false,
                hasRes ? S.res + 256 + pl * 64 : nullptr, 8, lane);
   }
 }
@@ -949,9 +1045,11 @@ __global__ void __launch_bounds__(32 * kIntraWarps, 1) kIntraRecon(const FrameDe
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, tid = threadIdx.x;
   const uint32_t* list = f.intraList + tr.mbBase;
   uint32_t* sorted = f.intraSorted + tr.mbBase;
+  ReconView view;
+  view.load(f);
   auto runMB = [&](uint32_t e) {
     const int idx = (int)(e & kIndexMask);
-    intraMB(f, sS[warp], idx % f.mbCols, idx / f.mbCols, tr.mbX0, tr.mbX1, tr.mbY0, lane);
+    intraMB(view, sS[warp], idx % view.mbCols, idx / view.mbCols, tr.mbX0, tr.mbX1, tr.mbY0, lane);
   };
   if (L <= kLevelBuckets) {
     for (int l = tid; l <= L; l += blockDim.x) sStart[l] = 0;
