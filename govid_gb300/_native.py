@@ -24,7 +24,7 @@ class EncoderOptions(C.Structure):
         ("auto_tiles", C.c_int32), ("altref_window", C.c_int32),
         ("fast_encode", C.c_int32), ("threads", C.c_int32),
         ("search", C.c_int32), ("exhaustive_range", C.c_int32),
-        ("keep_recon", C.c_int32),
+        ("keep_recon", C.c_int32), ("proposed_fallback_sad", C.c_int32),
     ]
 
 
@@ -110,6 +110,23 @@ def lib() -> C.CDLL:
     _sig(L, "ebivgpu_server_frame_hashes", I64, P, C.POINTER(C.c_int32), C.POINTER(I64), C.POINTER(C.c_uint64), I64)
     _sig(L, "ebivgpu_server_destroy", None, P)
     _sig(L, "ebivgpu_frame_hash", C.c_uint64, C.c_char_p, S)
+    # learned motion-vector proposer
+    F32P, I16P = C.POINTER(C.c_float), C.POINTER(C.c_int16)
+    _sig(L, "ebiv_mvnet_create", I, I, I, I, I, C.c_uint64, PP)
+    _sig(L, "ebiv_mvnet_destroy", None, P)
+    _sig(L, "ebiv_mvnet_param_count", I)
+    _sig(L, "ebiv_mvnet_get_params", I, P, F32P)
+    _sig(L, "ebiv_mvnet_set_params", I, P, F32P)
+    _sig(L, "ebiv_mvnet_exhaustive", I, P, U8P, U8P, I, I, I16P, C.POINTER(C.c_int32))
+    _sig(L, "ebiv_mvnet_add_pair", I, P, U8P, U8P, I, I16P)
+    _sig(L, "ebiv_mvnet_pairs", I, P)
+    _sig(L, "ebiv_mvnet_set_input", I, P, I, U8P, U8P, I, I16P)
+    _sig(L, "ebiv_mvnet_gather", I, P, C.POINTER(C.c_int32), I)
+    _sig(L, "ebiv_mvnet_gradients", I, P, I, F32P, F32P)
+    _sig(L, "ebiv_mvnet_train_step", I, P, I, C.c_float, F32P)
+    _sig(L, "ebiv_mvnet_head", I, P, I, F32P)
+    _sig(L, "ebiv_mvnet_propose", I, P, U8P, U8P, I, I16P)
+    _sig(L, "ebiv_encoder_set_mvnet", I, P, P)
     _sig(L, "ebivgpu_decode_key_noalloc", I, C.c_char_p, S, C.c_void_p, C.c_int32, S, C.c_void_p, C.c_void_p,
          C.c_int32, S, C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32))
     # encoder
@@ -121,6 +138,7 @@ def lib() -> C.CDLL:
     _sig(L, "ebiv_encoder_recon", I, P, I, U8P, S)
     _sig(L, "ebiv_encoder_recon_count", I, P)
     _sig(L, "ebiv_encoder_sad_evaluations", C.c_uint64, P)
+    _sig(L, "ebiv_encoder_search_fallbacks", C.c_uint64, P)
     _sig(L, "ebiv_encoder_set_candidates", I, P, C.POINTER(C.c_int16), I, I, I)
     _sig(L, "ebiv_encoder_destroy", None, P)
     # reader

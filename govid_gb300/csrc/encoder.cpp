@@ -772,6 +772,7 @@ struct TileEncoder {
   BlockScratch sc;
   TokStream lumaToks, cbToks, crToks;
   uint64_t sadCount = 0;
+  uint64_t fallbacks = 0;  // proposed searches decided by the exhaustive search
   explicit TileEncoder(FrameEncoder* f) : fe(f) {}
 
   int rdBits(const std::vector<Tok>& toks) const;
@@ -821,8 +822,10 @@ struct FrameEncoder {
   WorkerPool* pool = nullptr;
   SearchMode search = SearchMode::Diamond;
   int exhaustiveRange = 16;
+  int fallbackSAD = 0;
   const MVProposer* proposer = nullptr;
   std::atomic<uint64_t> sadCount{0};
+  std::atomic<uint64_t> fallbacks{0};
 
   // newFrameEncoder — ebiv/encode_intra.go:89-118
   FrameEncoder(const Geometry& geo, const PackedImage& img, const Frame* r, const Frame* gold, int qp, int tc, int tr)
@@ -853,6 +856,7 @@ struct FrameEncoder {
       else
         te.encodeIntraTile(streams[(size_t)i], b);
       sadCount += te.sadCount;
+      fallbacks += te.fallbacks;
     };
     if (pool)
       pool->run(grid.count(), fn);
@@ -1314,8 +1318,7 @@ MotionVector TileEncoder::search(const Frame* ref, int mbx, int mby, int px, int
     case SearchMode::Exhaustive:
       return searchExhaustive(ref, mbx, mby, px, py, pw, ph, pred);
     case SearchMode::Proposed:
-      if (fe->proposer && ref == fe->ref && pw == kMB && ph == kMB)
-        return searchProposed(ref, mbx, mby, px, py, pw, ph, pred);
+      if (fe->proposer && ref == fe->ref) return searchProposed(ref, mbx, mby, px, py, pw, ph, pred);
       return searchMVRect(ref, mbx, mby, px, py, pw, ph, pred);
     default:
       return searchMVRect(ref, mbx, mby, px, py, pw, ph, pred);
@@ -1383,8 +1386,12 @@ MotionVector TileEncoder::searchExhaustive(const Frame* ref, int mbx, int mby, i
   return best;
 }
 
-// Candidate search: the proposer's full-pel candidates plus zero and the
-// predictor, a one-pixel full-pel polish, then half/quarter-pel refinement.
+// Candidate search: zero, the predictor and the proposer's full-pel
+// candidates for the macroblock (used for every partition of it), each
+// candidate with its one-pixel full-pel neighbourhood (the proposals are
+// 2-pixel bins), a one-pixel polish around the best, then the same
+// half/quarter-pel refinement as the diamond.  When the best SAD stays above
+// fallbackSAD per 256 pixels the exhaustive search decides instead.
 MotionVector TileEncoder::searchProposed(const Frame* ref, int mbx, int mby, int px, int py, int pw, int ph,
                                          MotionVector pred) {
   MotionVector best;
@@ -1399,11 +1406,19 @@ MotionVector TileEncoder::searchProposed(const Frame* ref, int mbx, int mby, int
   consider(pred);
   MotionVector cands[32];
   const int nc = fe->proposer->candidates(mbx, mby, cands, 32);
-  for (int i = 0; i < nc; i++) consider({clampMV(cands[i].x), clampMV(cands[i].y)});
+  for (int i = 0; i < nc; i++) {
+    const int cx = cands[i].x & ~3, cy = cands[i].y & ~3;
+    for (int dy = -1; dy <= 1; dy++)
+      for (int dx = -1; dx <= 1; dx++) consider({clampMV(cx + dx * 4), clampMV(cy + dy * 4)});
+  }
   {
     const int bx = best.x & ~3, by = best.y & ~3;
     for (int dy = -1; dy <= 1; dy++)
       for (int dx = -1; dx <= 1; dx++) consider({clampMV(bx + dx * 4), clampMV(by + dy * 4)});
+  }
+  if (fe->fallbackSAD > 0 && bestSAD * 256 > (int64_t)fe->fallbackSAD * pw * ph) {
+    fallbacks++;
+    return searchExhaustive(ref, mbx, mby, px, py, pw, ph, pred);
   }
   const int subs[2] = {2, 1};
   for (int sub : subs) {
@@ -1469,6 +1484,7 @@ struct Encoder::Impl {
   bool closed = false;
   int err = kOK;
   uint64_t sads = 0;
+  uint64_t fallbacks = 0;
 
   int writeFrame(const std::vector<uint8_t>& payload, bool key) {  // Writer.WriteFrame
     if (err) return err;
@@ -1521,6 +1537,7 @@ Encoder::Encoder(const EncoderOptions& o) : impl_(new Impl()), opt_(o) {
 Encoder::~Encoder() = default;
 
 uint64_t Encoder::sadEvaluations() const { return impl_->sads; }
+uint64_t Encoder::searchFallbacks() const { return impl_->fallbacks; }
 
 namespace {
 std::vector<uint8_t> frameHeaderBytes(int type, int coding, const Geometry& g, bool override_) {
@@ -1659,12 +1676,14 @@ int Encoder::flushGOP() {
     fe.pool = m.pool.get();
     fe.search = opt_.search;
     fe.exhaustiveRange = opt_.exhaustiveRange;
+    fe.fallbackSAD = opt_.proposedFallbackSAD;
     fe.proposer = proposer_;
     if (inter && proposer_ && opt_.search == SearchMode::Proposed)
       proposer_->prepare(fe.src->yb.data(), ref->yb.data(), m.geo.padW(), m.geo.padH());
     fe.encode(inter, !opt_.fastEncode);
     std::vector<uint8_t> payload = fe.finish(opt_.qp, prev, freqs);
     m.sads += fe.sadCount.load();
+    m.fallbacks += fe.fallbacks.load();
     rec->reset(fe.rec.release());
     return payload;
   };

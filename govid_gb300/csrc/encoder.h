@@ -65,6 +65,7 @@ struct EncoderOptions {
   int threads = 1;                 // host threads for tile fan-out
   SearchMode search = SearchMode::Diamond;
   int exhaustiveRange = 16;        // full-pel search radius for Exhaustive
+  int proposedFallbackSAD = 0;     // Proposed: exhaustive search when the best SAD per 256 px exceeds this (0 = never)
   bool keepRecon = false;          // keep each written frame's reconstruction
 };
 
@@ -79,6 +80,7 @@ class Encoder {
   void setProposer(MVProposer* p) { proposer_ = p; }
   // Motion search statistics accumulated over the encode (SAD evaluations).
   uint64_t sadEvaluations() const;
+  uint64_t searchFallbacks() const;  // proposed searches handed to the exhaustive search
   int frameCount() const { return accepted_; }
   // Reconstructions (visible region) of the frames written so far, in
   // container order, when keepRecon was set.

@@ -37,6 +37,11 @@ struct ebiv_encoder {
     }
   } proposer;
 };
+namespace ebiv {
+Encoder* encoderOf(ebiv_encoder* e) { return e ? e->enc.get() : nullptr; }
+const EncoderOptions* encoderOptionsOf(ebiv_encoder* e) { return e ? &e->opt : nullptr; }
+}  // namespace ebiv
+
 struct ebiv_reader {
   Reader r;
 };
@@ -66,6 +71,7 @@ EncoderOptions toOptions(const ebiv_encoder_options* o) {
   e.threads = o->threads;
   e.search = (SearchMode)o->search;
   e.exhaustiveRange = o->exhaustive_range > 0 ? o->exhaustive_range : 16;
+  e.proposedFallbackSAD = o->proposed_fallback_sad > 0 ? o->proposed_fallback_sad : 0;
   e.keepRecon = o->keep_recon != 0;
   return e;
 }
@@ -158,6 +164,8 @@ int ebiv_encoder_recon(ebiv_encoder* e, int index, uint8_t* packed, size_t cap) 
 int ebiv_encoder_recon_count(ebiv_encoder* e) { return e ? (int)e->enc->recons().size() : 0; }
 
 uint64_t ebiv_encoder_sad_evaluations(ebiv_encoder* e) { return e ? e->enc->sadEvaluations() : 0; }
+
+uint64_t ebiv_encoder_search_fallbacks(ebiv_encoder* e) { return e ? e->enc->searchFallbacks() : 0; }
 
 int ebiv_encoder_set_candidates(ebiv_encoder* e, const int16_t* mv, int frames, int mbs, int k) {
   if (!e || !mv || frames < 0 || mbs <= 0 || k <= 0) return kErrArg;

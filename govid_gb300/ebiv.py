@@ -474,7 +474,8 @@ class Encoder:
 
     def __init__(self, cfg: Config, intra: int | None = None, gop: int = 1, tiles: tuple[int, int] | None = None,
                  auto_tiles: int = 0, altref: int = 0, fast: bool = False, threads: int = 1,
-                 search: str = "diamond", exhaustive_range: int = 16, keep_recon: bool = False):
+                 search: str = "diamond", exhaustive_range: int = 16, keep_recon: bool = False,
+                 fallback_sad: int = 0):
         L = _native.lib()
         o = _native.EncoderOptions()
         L.ebiv_encoder_default_options(C.byref(o))
@@ -493,6 +494,7 @@ class Encoder:
         o.search = {"diamond": 0, "exhaustive": 1, "proposed": 2}[search]
         o.exhaustive_range = int(exhaustive_range)
         o.keep_recon = int(bool(keep_recon))
+        o.proposed_fallback_sad = int(fallback_sad)
         h = C.c_void_p()
         _check(L.ebiv_encoder_create(C.byref(o), C.byref(h)), "NewEncoder")
         self._h, self._L, self.cfg = h, L, cfg
@@ -526,6 +528,9 @@ class Encoder:
 
     def sad_evaluations(self) -> int:
         return int(self._L.ebiv_encoder_sad_evaluations(self._h))
+
+    def search_fallbacks(self) -> int:
+        return int(self._L.ebiv_encoder_search_fallbacks(self._h))
 
     def set_candidates(self, mv: np.ndarray) -> None:
         """mv: int16 (frames, mbs, k, 2) quarter-pel candidates for search='proposed'."""

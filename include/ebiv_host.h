@@ -46,6 +46,7 @@ typedef struct {
   int32_t search;                         /* 0 diamond, 1 exhaustive, 2 proposed */
   int32_t exhaustive_range;               /* full-pel radius for search=1 */
   int32_t keep_recon;                     /* keep reconstructions */
+  int32_t proposed_fallback_sad;          /* search=2: exhaustive when best SAD per 256 px exceeds this (0 never) */
 } ebiv_encoder_options;
 
 void ebiv_encoder_default_options(ebiv_encoder_options* o);
@@ -58,6 +59,8 @@ int ebiv_encoder_output(ebiv_encoder* e, const uint8_t** data, size_t* n);
 int ebiv_encoder_recon(ebiv_encoder* e, int index, uint8_t* packed, size_t cap);
 int ebiv_encoder_recon_count(ebiv_encoder* e);
 uint64_t ebiv_encoder_sad_evaluations(ebiv_encoder* e);
+/* Proposed searches (search=2) the exhaustive search decided. */
+uint64_t ebiv_encoder_search_fallbacks(ebiv_encoder* e);
 /* Installs candidate motion vectors per macroblock for search=2: a table of
  * frames*mbs*k (x,y) int16 pairs in quarter pixels, frame-major, consumed in
  * inter-frame order. */
