@@ -350,6 +350,12 @@ def run_gpu(args):
             out["batched"] = run_batched(args)
         if not args.no_serve:
             out["serving"] = run_serve(args)
+        if not args.no_mv:
+            from govid_gb300 import eval_mvnet
+
+            r = eval_mvnet.compare(1920, 1080, nframes=args.mv_frames, qp=22, log=None)
+            r["note"] = "encoder on the host cores; the proposer's net runs on this GPU"
+            out["learned_mv"] = r
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(pkts, args.cpu_seconds)
         out["clocks"] = ck.summary()
@@ -543,6 +549,8 @@ def main():
     ap.add_argument("--mix-lookahead", type=int, default=4)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-mv", action="store_true")
+    ap.add_argument("--mv-frames", type=int, default=16)
     ap.add_argument("--serve-streams", type=int, default=256)
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--serve-max-frames", type=int, default=2)

@@ -139,6 +139,8 @@ def lib() -> C.CDLL:
     _sig(L, "ebiv_encoder_recon_count", I, P)
     _sig(L, "ebiv_encoder_sad_evaluations", C.c_uint64, P)
     _sig(L, "ebiv_encoder_search_fallbacks", C.c_uint64, P)
+    _sig(L, "ebiv_encoder_search_seconds", C.c_double, P)
+    _sig(L, "ebiv_encoder_propose_seconds", C.c_double, P)
     _sig(L, "ebiv_encoder_set_candidates", I, P, C.POINTER(C.c_int16), I, I, I)
     _sig(L, "ebiv_encoder_destroy", None, P)
     # reader

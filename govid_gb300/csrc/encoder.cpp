@@ -8,6 +8,7 @@
 #include "encoder.h"
 
 #include <algorithm>
+#include <chrono>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -773,6 +774,7 @@ struct TileEncoder {
   TokStream lumaToks, cbToks, crToks;
   uint64_t sadCount = 0;
   uint64_t fallbacks = 0;  // proposed searches decided by the exhaustive search
+  uint64_t searchNs = 0;   // thread time spent in motion search
   explicit TileEncoder(FrameEncoder* f) : fe(f) {}
 
   int rdBits(const std::vector<Tok>& toks) const;
@@ -800,6 +802,7 @@ struct TileEncoder {
   MotionVector searchExhaustive(const Frame* ref, int mbx, int mby, int px, int py, int pw, int ph, MotionVector pred);
   MotionVector searchProposed(const Frame* ref, int mbx, int mby, int px, int py, int pw, int ph, MotionVector pred);
   MotionVector search(const Frame* ref, int mbx, int mby, int px, int py, int pw, int ph, MotionVector pred);
+  MotionVector searchOnce(const Frame* ref, int mbx, int mby, int px, int py, int pw, int ph, MotionVector pred);
   int64_t rectSAD(const Frame* ref, int mbx, int mby, int px, int py, int pw, int ph, MotionVector mv);
 };
 
@@ -826,6 +829,7 @@ struct FrameEncoder {
   const MVProposer* proposer = nullptr;
   std::atomic<uint64_t> sadCount{0};
   std::atomic<uint64_t> fallbacks{0};
+  std::atomic<uint64_t> searchNs{0};
 
   // newFrameEncoder — ebiv/encode_intra.go:89-118
   FrameEncoder(const Geometry& geo, const PackedImage& img, const Frame* r, const Frame* gold, int qp, int tc, int tr)
@@ -857,6 +861,7 @@ struct FrameEncoder {
         te.encodeIntraTile(streams[(size_t)i], b);
       sadCount += te.sadCount;
       fallbacks += te.fallbacks;
+      searchNs += te.searchNs;
     };
     if (pool)
       pool->run(grid.count(), fn);
@@ -1314,6 +1319,15 @@ int64_t TileEncoder::codeInterLuma(TokStream& s, int mbx, int mby, const int32_t
 
 MotionVector TileEncoder::search(const Frame* ref, int mbx, int mby, int px, int py, int pw, int ph,
                                  MotionVector pred) {
+  const auto t0 = std::chrono::steady_clock::now();
+  const MotionVector m = searchOnce(ref, mbx, mby, px, py, pw, ph, pred);
+  searchNs += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0)
+                  .count();
+  return m;
+}
+
+MotionVector TileEncoder::searchOnce(const Frame* ref, int mbx, int mby, int px, int py, int pw, int ph,
+                                     MotionVector pred) {
   switch (fe->search) {
     case SearchMode::Exhaustive:
       return searchExhaustive(ref, mbx, mby, px, py, pw, ph, pred);
@@ -1406,10 +1420,21 @@ MotionVector TileEncoder::searchProposed(const Frame* ref, int mbx, int mby, int
   consider(pred);
   MotionVector cands[32];
   const int nc = fe->proposer->candidates(mbx, mby, cands, 32);
+  // Neighbourhoods of adjacent bins overlap: evaluate each position once.
+  uint32_t seen[9 * 32];
+  int nSeen = 0;
   for (int i = 0; i < nc; i++) {
     const int cx = cands[i].x & ~3, cy = cands[i].y & ~3;
     for (int dy = -1; dy <= 1; dy++)
-      for (int dx = -1; dx <= 1; dx++) consider({clampMV(cx + dx * 4), clampMV(cy + dy * 4)});
+      for (int dx = -1; dx <= 1; dx++) {
+        const MotionVector m{clampMV(cx + dx * 4), clampMV(cy + dy * 4)};
+        const uint32_t key = (uint32_t)(uint16_t)m.x | ((uint32_t)(uint16_t)m.y << 16);
+        bool dup = false;
+        for (int k = 0; k < nSeen && !dup; k++) dup = seen[k] == key;
+        if (dup) continue;
+        seen[nSeen++] = key;
+        consider(m);
+      }
   }
   {
     const int bx = best.x & ~3, by = best.y & ~3;
@@ -1485,6 +1510,8 @@ struct Encoder::Impl {
   int err = kOK;
   uint64_t sads = 0;
   uint64_t fallbacks = 0;
+  uint64_t searchNs = 0;   // summed thread time in motion search
+  uint64_t proposeNs = 0;  // wall time of the proposer's per-frame preparation
 
   int writeFrame(const std::vector<uint8_t>& payload, bool key) {  // Writer.WriteFrame
     if (err) return err;
@@ -1538,6 +1565,8 @@ Encoder::~Encoder() = default;
 
 uint64_t Encoder::sadEvaluations() const { return impl_->sads; }
 uint64_t Encoder::searchFallbacks() const { return impl_->fallbacks; }
+double Encoder::searchSeconds() const { return (double)impl_->searchNs * 1e-9; }
+double Encoder::proposeSeconds() const { return (double)impl_->proposeNs * 1e-9; }
 
 namespace {
 std::vector<uint8_t> frameHeaderBytes(int type, int coding, const Geometry& g, bool override_) {
@@ -1678,12 +1707,17 @@ int Encoder::flushGOP() {
     fe.exhaustiveRange = opt_.exhaustiveRange;
     fe.fallbackSAD = opt_.proposedFallbackSAD;
     fe.proposer = proposer_;
-    if (inter && proposer_ && opt_.search == SearchMode::Proposed)
+    if (inter && proposer_ && opt_.search == SearchMode::Proposed) {
+      const auto t0 = std::chrono::steady_clock::now();
       proposer_->prepare(fe.src->yb.data(), ref->yb.data(), m.geo.padW(), m.geo.padH());
+      m.proposeNs += (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0)
+                         .count();
+    }
     fe.encode(inter, !opt_.fastEncode);
     std::vector<uint8_t> payload = fe.finish(opt_.qp, prev, freqs);
     m.sads += fe.sadCount.load();
     m.fallbacks += fe.fallbacks.load();
+    m.searchNs += fe.searchNs.load();
     rec->reset(fe.rec.release());
     return payload;
   };

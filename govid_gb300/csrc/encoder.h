@@ -81,6 +81,8 @@ class Encoder {
   // Motion search statistics accumulated over the encode (SAD evaluations).
   uint64_t sadEvaluations() const;
   uint64_t searchFallbacks() const;  // proposed searches handed to the exhaustive search
+  double searchSeconds() const;      // thread seconds in motion search (summed over tile threads)
+  double proposeSeconds() const;     // wall seconds of the proposer's per-frame preparation
   int frameCount() const { return accepted_; }
   // Reconstructions (visible region) of the frames written so far, in
   // container order, when keepRecon was set.

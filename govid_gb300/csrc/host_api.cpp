@@ -167,6 +167,10 @@ uint64_t ebiv_encoder_sad_evaluations(ebiv_encoder* e) { return e ? e->enc->sadE
 
 uint64_t ebiv_encoder_search_fallbacks(ebiv_encoder* e) { return e ? e->enc->searchFallbacks() : 0; }
 
+double ebiv_encoder_search_seconds(ebiv_encoder* e) { return e ? e->enc->searchSeconds() : 0.0; }
+
+double ebiv_encoder_propose_seconds(ebiv_encoder* e) { return e ? e->enc->proposeSeconds() : 0.0; }
+
 int ebiv_encoder_set_candidates(ebiv_encoder* e, const int16_t* mv, int frames, int mbs, int k) {
   if (!e || !mv || frames < 0 || mbs <= 0 || k <= 0) return kErrArg;
   e->proposer.mv.assign(mv, mv + (size_t)frames * mbs * k * 2);

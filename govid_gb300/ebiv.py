@@ -532,6 +532,14 @@ class Encoder:
     def search_fallbacks(self) -> int:
         return int(self._L.ebiv_encoder_search_fallbacks(self._h))
 
+    def search_seconds(self) -> float:
+        """Thread seconds in motion search, summed over tile threads."""
+        return float(self._L.ebiv_encoder_search_seconds(self._h))
+
+    def propose_seconds(self) -> float:
+        """Wall seconds the proposer spent preparing candidates (search='proposed')."""
+        return float(self._L.ebiv_encoder_propose_seconds(self._h))
+
     def set_candidates(self, mv: np.ndarray) -> None:
         """mv: int16 (frames, mbs, k, 2) quarter-pel candidates for search='proposed'."""
         a = np.ascontiguousarray(mv, dtype=np.int16)

@@ -61,6 +61,10 @@ int ebiv_encoder_recon_count(ebiv_encoder* e);
 uint64_t ebiv_encoder_sad_evaluations(ebiv_encoder* e);
 /* Proposed searches (search=2) the exhaustive search decided. */
 uint64_t ebiv_encoder_search_fallbacks(ebiv_encoder* e);
+/* Thread seconds spent in motion search (summed over tile threads) and wall
+ * seconds of the proposer's per-frame preparation (search=2). */
+double ebiv_encoder_search_seconds(ebiv_encoder* e);
+double ebiv_encoder_propose_seconds(ebiv_encoder* e);
 /* Installs candidate motion vectors per macroblock for search=2: a table of
  * frames*mbs*k (x,y) int16 pairs in quarter pixels, frame-major, consumed in
  * inter-frame order. */
