@@ -245,23 +245,16 @@ def run_gpu(args):
     alg = algorithmic_bytes(pkts, W, H)
 
     # ---- value: packets resident in HBM, device frame pool output ----
-    b = ebiv.Batch(lookahead=args.lookahead)
+    b = ebiv.Batch(lookahead=args.lookahead, pipeline=not args.no_pipeline)
     sid = b.add_stream(pkts, ring=3)
 
     def one_pass(lat=None):
         b.seek(sid, 0)
         done = 0
-        while True:
-            t = time.perf_counter()
-            res = b.round()
-            if not res:
-                break
-            if lat is not None:
-                lat.append(time.perf_counter() - t)
-            for r in res:
-                if r.status != 0:
-                    raise RuntimeError(f"decode failed at frame {r.frame_index}: {r.status}")
-            done += len(res)
+        for r in all_rounds(b, lat):
+            if r.status != 0:
+                raise RuntimeError(f"decode failed at frame {r.frame_index}: {r.status}")
+            done += 1
         return done
 
     for _ in range(args.warmup):
@@ -332,7 +325,7 @@ def run_gpu(args):
         "data": "synthetic (seeded sprite scene encoded by this repo's EBIV encoder)",
         "config": {"workload": f"EBIV decode, 1 stream {W}x{H} {n} frames q22 gop60 tiles 4x3 (fast encode)",
                    "frames_per_step": n, "packet_bytes_per_step": h2d, "l2": "flushed between steps",
-                   "lookahead_frames": args.lookahead,
+                   "lookahead_frames": args.lookahead, "pipelined_rounds": not args.no_pipeline,
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e, 2), "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "latency_ms": {"p50": round(1000 * statistics.median(lat), 3) if lat else None,
@@ -364,6 +357,21 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def all_rounds(b, lat=None):
+    """Every result of a batch until its streams are exhausted.  A pipelined
+    round returns the previous round's results, so stop after two empty
+    rounds and collect the one in flight.  lat gets each call's wall time."""
+    empty = 0
+    while empty < 2:
+        t = time.perf_counter()
+        res = b.round()
+        if lat is not None and res:
+            lat.append(time.perf_counter() - t)
+        empty = empty + 1 if not res else 0
+        yield from res
+    yield from b.drain()
+
+
 def run_batched(args):
     """64 mixed streams in rounds vs the same streams one stream per launch."""
     import torch
@@ -375,7 +383,7 @@ def run_batched(args):
     log(f"[bench] mix content ready in {time.time() - t0:.1f}s")
     eq1080 = sum(algorithmic_bytes([p.data for p in ebiv.Reader(c).packets()], w, h)
                  for w, h, c in streams)
-    b = ebiv.Batch(lookahead=args.mix_lookahead)
+    b = ebiv.Batch(lookahead=args.mix_lookahead, pipeline=not args.no_pipeline)
     single_b = ebiv.Batch(lookahead=1)
     ids, single_ids = [], []
     totals = 0
@@ -390,6 +398,7 @@ def run_batched(args):
     for sid in ids:
         b.seek(sid, 0)
     b.round()
+    b.drain()
     for sid in ids:
         b.seek(sid, 0)
     flush_l2()
@@ -398,16 +407,10 @@ def run_batched(args):
     b.timing(1)
     ts = time.perf_counter()
     frames = 0
-    while True:
-        t = time.perf_counter()
-        res = b.round()
-        if not res:
-            break
-        lat.append(time.perf_counter() - t)
-        frames += len(res)
-        bad = [r for r in res if r.status != 0]
-        if bad:
-            raise RuntimeError(f"batched decode failed: {bad[0]}")
+    for r in all_rounds(b, lat):
+        frames += 1
+        if r.status != 0:
+            raise RuntimeError(f"batched decode failed: {r}")
     torch.cuda.synchronize()
     te = time.perf_counter()
     kernel_ms, _, _ = b.timing(-1)
@@ -434,7 +437,7 @@ def run_batched(args):
     hbm = eq1080 / (kernel_ms / 1000) / 1e9 if kernel_ms > 0 else 0.0
     return {
         "streams": len(streams), "distinct_bitstreams": len({id(c) for _, _, c in streams}),
-        "lookahead_frames": args.mix_lookahead,
+        "lookahead_frames": args.mix_lookahead, "pipelined_rounds": not args.no_pipeline,
         "frames_per_stream": args.mix_frames, "frames": frames,
         "frames_per_s": round(batched_fps, 2),
         "frames_1080p_equiv_per_s": round(batched_fps * (px / totals) / (W * H), 2),
@@ -548,6 +551,7 @@ def main():
     ap.add_argument("--lookahead", type=int, default=32)
     ap.add_argument("--mix-lookahead", type=int, default=4)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-pipeline", action="store_true", help="synchronous rounds (no entropy/recon overlap)")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-mv", action="store_true")
     ap.add_argument("--mv-frames", type=int, default=16)

@@ -74,6 +74,14 @@ struct Engine::Stream {
   std::vector<Slot> slots;
   size_t mbs = 0;
   size_t bytes = 0;
+  // Pipelined rounds: references after the newest planned round (valid while
+  // hasProv), pool buffers claimed per round parity, and an epoch bumped at
+  // every rollback (jobs planned under an older epoch are discarded).
+  bool hasProv = false;
+  int pRef = -1, pGolden = -1;
+  int64_t lastRound = 0;
+  int64_t epoch = 0;
+  std::vector<int> roundBufs[2];
 
   uint8_t* plane(int b, int k) const {
     return pool[(size_t)b] + (k == 0 ? 0 : yBytes + (size_t)(k - 1) * cBytes);
@@ -104,22 +112,54 @@ struct Engine::Job {
   PayloadPlan main, ov;
   TableHistory hMain;    // table history after the main payload was planned
   TableHistory hBefore;  // table history before this frame was planned
+  TableHistory hAfter;   // table history after this frame (and its override) was planned
   int step = 0, slot = -1;
   int mainDesc = -1, ovDesc = -1;
   int gateDesc = -1;  // descriptor whose status gates this frame (-1: none)
   size_t stageOff = 0;
+  int64_t epoch = 0;  // the stream's epoch when planned
 };
 
-Engine::Engine() {}
+struct Engine::StepInfo {
+  int mainFirst = 0, mainCount = 0, ovFirst = 0, ovCount = 0;
+  int jobFirst = 0, jobCount = 0, ovJobFirst = 0, ovJobCount = 0;
+  int maxInterMBs = 0, maxOvMBs = 0;
+};
+
+struct Engine::Round {
+  int64_t id = 0;
+  int parity = 0;
+  std::vector<Job> jobs;
+  std::vector<std::vector<int>> chains;  // per stream, indices into jobs in decode order
+  std::vector<StepInfo> steps;
+  int nDesc = 0, nTiles = 0, nEJobs = 0;
+  size_t oDesc = 0, oStat = 0, oJobs = 0, oEJobs = 0;
+  bool launched = false;  // entropy launched; statuses pending
+  void clear() {
+    jobs.clear();
+    chains.clear();
+    steps.clear();
+    nDesc = nTiles = nEJobs = 0;
+    launched = false;
+  }
+};
+
+Engine::Engine() : rounds_(new Round[2]) {}
 
 Engine::~Engine() {
+  if (streamE_) cudaStreamSynchronize(streamE_);
   if (stream_) cudaStreamSynchronize(stream_);
   for (auto& s : streams_)
     if (s) s->release();
-  if (dStage_) cudaFree(dStage_);
-  if (hStage_) cudaFreeHost(hStage_);
-  for (auto& e : ev_)
-    if (e) cudaEventDestroy(e);
+  for (int p = 0; p < 2; p++) {
+    if (dStage_[p]) cudaFree(dStage_[p]);
+    if (hStage_[p]) cudaFreeHost(hStage_[p]);
+    if (hStatus_[p]) cudaFreeHost(hStatus_[p]);
+    for (auto& e : ev_[p])
+      if (e) cudaEventDestroy(e);
+  }
+  if (dOne_) cudaFree(dOne_);
+  if (ownStreamE_ && streamE_) cudaStreamDestroy(streamE_);
   if (ownStream_ && stream_) cudaStreamDestroy(stream_);
 }
 
@@ -130,8 +170,13 @@ int Engine::init(cudaStream_t s) {
     if (cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking) != cudaSuccess) return kErrDevice;
     ownStream_ = true;
   }
-  for (auto& e : ev_)
-    if (cudaEventCreate(&e) != cudaSuccess) return kErrDevice;
+  for (auto& row : ev_)
+    for (auto& e : row)
+      if (cudaEventCreate(&e) != cudaSuccess) return kErrDevice;
+  int32_t one = 1;
+  if (cudaMalloc(&dOne_, sizeof(int32_t)) != cudaSuccess ||
+      cudaMemcpy(dOne_, &one, sizeof(one), cudaMemcpyHostToDevice) != cudaSuccess)
+    return kErrDevice;
   return ensureDeviceTables();
 }
 
@@ -143,11 +188,17 @@ int Engine::setLookahead(int k) {
   return kOK;
 }
 
-size_t Engine::footprint(int w, int h, int ring, int lookahead) {
+// Frame buffers per stream: the ring's outputs plus a round's, the two
+// references, and the buffers a round claims; a pipelined engine holds two
+// rounds' worth of claims.
+int Engine::poolSize(int ring, int k, bool pipelined) { return pipelined ? ring + 3 * k + 4 : ring + 2 * k + 3; }
+
+size_t Engine::footprint(int w, int h, int ring, int lookahead, bool pipelined) {
   const Geometry g = Geometry::of(w, h);
   const size_t yb = (size_t)stride64(g.padW()) * g.padH(), cb = (size_t)stride64(g.padCW()) * g.padCH();
   const size_t mbs = (size_t)g.mbCols * g.mbRows;
-  return (size_t)(ring + 2 * lookahead + 3) * (yb + 2 * cb) + (size_t)(lookahead + 1) * Slot::bytes(mbs);
+  return (size_t)poolSize(ring, lookahead, pipelined) * (yb + 2 * cb) +
+         (size_t)(pipelined ? 2 : 1) * (lookahead + 1) * Slot::bytes(mbs);
 }
 
 int Engine::addResidentStream(const uint8_t* const* pkts, const size_t* lens, int n, int ring, int* id) {
@@ -176,6 +227,7 @@ int Engine::addResidentStream(const uint8_t* const* pkts, const size_t* lens, in
 }
 
 int Engine::addStreamingStream(int ring, int* id) {
+  if (pipelined_) return kErrArg;  // pipelined rounds keep packets resident
   std::unique_ptr<Stream> s(new (std::nothrow) Stream());
   if (!s) return kErrArg;
   s->ring = ring >= 2 ? ring : 3;
@@ -215,6 +267,7 @@ int Engine::setActive(int id, bool active) {
 
 int Engine::removeStream(int id) {
   if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) return kErrArg;
+  if (streamE_) cudaStreamSynchronize(streamE_);
   cudaStreamSynchronize(stream_);
   deviceBytes_ -= streams_[(size_t)id]->bytes;
   streams_[(size_t)id]->release();
@@ -233,7 +286,7 @@ int Engine::configure(Stream& s, int w, int h) {
   s.cBytes = (size_t)s.strideC * s.geo.padCH();
   s.bufBytes = s.yBytes + 2 * s.cBytes;
   const int k = s.resident ? lookahead_ : 1;
-  const int P = s.ring + 2 * k + 3;
+  const int P = poolSize(s.ring, k, pipelined_);
   for (int i = 0; i < P; i++) {
     uint8_t* p = nullptr;
     if (cudaMalloc(&p, s.bufBytes) != cudaSuccess) return kErrDevice;
@@ -244,30 +297,47 @@ int Engine::configure(Stream& s, int w, int h) {
   s.ref = 0;
   s.golden = 1;
   s.mbs = (size_t)s.geo.mbCols * s.geo.mbRows;
-  s.slots.resize((size_t)k + 1);
-  for (auto& sl : s.slots)
-    if (!sl.alloc(s.mbs)) return kErrDevice;
-  const size_t b = (size_t)P * s.bufBytes + (size_t)(k + 1) * Slot::bytes(s.mbs);
+  // Slots: one per frame step and one for an override, per round parity.
+  // Job slots index lookahead_ + 1 per parity; streaming streams use slot 0
+  // and the override slot.
+  const int perParity = lookahead_ + 1;
+  s.slots.resize((size_t)(pipelined_ ? 2 : 1) * perParity);
+  for (size_t i = 0; i < s.slots.size(); i++) {
+    const int within = (int)(i % (size_t)perParity);
+    if ((within < k || within == perParity - 1) && !s.slots[i].alloc(s.mbs)) return kErrDevice;
+  }
+  const size_t b = (size_t)P * s.bufBytes + (size_t)(pipelined_ ? 2 : 1) * (k + 1) * Slot::bytes(s.mbs);
   s.bytes += b;
   deviceBytes_ += b;
   s.ready = true;
   return kOK;
 }
 
-int Engine::ensureStage(size_t bytes) {
-  if (bytes <= stageCap_) return kOK;
+// Staging for round parity P (host pinned + device).  The other parity's
+// round may be in flight; it never touches these buffers.
+int Engine::ensureStage(int P, size_t bytes) {
+  if (bytes <= stageCap_[P]) return kOK;
   const size_t cap = al(bytes + bytes / 2, 1 << 20);
-  if (dStage_) {
-    cudaStreamSynchronize(stream_);
-    cudaFree(dStage_);
-  }
-  if (hStage_) cudaFreeHost(hStage_);
-  dStage_ = nullptr;
-  hStage_ = nullptr;
-  stageCap_ = 0;
-  if (cudaMalloc(&dStage_, cap) != cudaSuccess) return kErrDevice;
-  if (cudaMallocHost(&hStage_, cap) != cudaSuccess) return kErrDevice;
-  stageCap_ = cap;
+  if (dStage_[P]) cudaFree(dStage_[P]);  // synchronises the device
+  if (hStage_[P]) cudaFreeHost(hStage_[P]);
+  dStage_[P] = nullptr;
+  hStage_[P] = nullptr;
+  stageCap_[P] = 0;
+  if (cudaMalloc(&dStage_[P], cap) != cudaSuccess) return kErrDevice;
+  if (cudaMallocHost(&hStage_[P], cap) != cudaSuccess) return kErrDevice;
+  stageCap_[P] = cap;
+  return kOK;
+}
+
+// Pinned host words the round's frame statuses are read back into.
+int Engine::ensureStatus(int P, int n) {
+  if (n <= statusCap_[P]) return kOK;
+  const int cap = std::max(n * 2, 256);
+  if (hStatus_[P]) cudaFreeHost(hStatus_[P]);
+  hStatus_[P] = nullptr;
+  statusCap_[P] = 0;
+  if (cudaMallocHost(&hStatus_[P], sizeof(int32_t) * (size_t)cap) != cudaSuccess) return kErrDevice;
+  statusCap_[P] = cap;
   return kOK;
 }
 
@@ -345,7 +415,7 @@ int Engine::planFrame(Stream& s, Job& j, std::vector<char>& busy) {
   return kOK;
 }
 
-void Engine::finishFrame(Stream& s, Job& j, const int32_t* st, std::vector<RoundResult>* results) {
+int Engine::finishFrame(Stream& s, Job& j, const int32_t* st, std::vector<RoundResult>* results) {
   RoundResult r;
   r.stream = s.id;
   r.frameIndex = j.pktIndex;
@@ -389,6 +459,7 @@ void Engine::finishFrame(Stream& s, Job& j, const int32_t* st, std::vector<Round
   }
   r.status = status;
   if (results) results->push_back(r);
+  return status;
 }
 
 int Engine::round(std::vector<RoundResult>* results) {
@@ -399,34 +470,58 @@ int Engine::round(std::vector<RoundResult>* results) {
   return roundFor(ids, results);
 }
 
-int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* results,
-                     const std::vector<int>* maxFrames) {
-  // ---- plan: up to `lookahead` frames per resident stream --------------------
-  std::vector<Job> jobs;
+// ---------------------------------------------------------------------------
+// A round: plan + entropy launch, reconstruction launch, collect.  Run back
+// to back (the synchronous engine) or overlapped with the neighbouring rounds
+// (the pipelined engine: round N+1 is planned and its entropy stage runs on
+// the entropy stream while round N reconstructs on the engine's stream; round
+// N+1's reconstruction is launched once round N has been collected, so a
+// stream whose round-N chain failed has its round-N+1 frames skipped and
+// re-planned).
+// ---------------------------------------------------------------------------
+int Engine::setPipelined(bool on) {
+  for (auto& s : streams_)
+    if (s) return kErrArg;  // pool and slot counts depend on it
+  if (on && !streamE_) {
+    if (cudaStreamCreateWithFlags(&streamE_, cudaStreamNonBlocking) != cudaSuccess) return kErrDevice;
+    ownStreamE_ = true;
+  }
+  pipelined_ = on;
+  return kOK;
+}
+
+int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFrames, Round& R) {
+  R.clear();
+  R.id = ++roundSeq_;
+  const int P = R.parity;
+  std::vector<Job>& jobs = R.jobs;
   jobs.reserve(ids.size() * (size_t)lookahead_);
-  std::vector<std::vector<int>> chains;  // per stream, indices into jobs in decode order
   size_t streamedBytes = 0;
+  cudaStream_t se = entropyStream();
   for (size_t ii = 0; ii < ids.size(); ii++) {
     const int id = ids[ii];
     if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) continue;
     Stream& s = *streams_[(size_t)id];
     std::vector<int> chain;
     std::vector<char> busy;
-    int provRef = s.ref, provGolden = s.golden;
-    auto resetBusy = [&] {
-      busy.assign(s.pool.size(), 0);
-      if (provRef >= 0) busy[(size_t)provRef] = 1;
-      if (provGolden >= 0) busy[(size_t)provGolden] = 1;
-      for (int b : s.outputs) busy[(size_t)b] = 1;
-    };
-    resetBusy();
+    // Start from the provisional references after the stream's in-flight
+    // round, when it has one.
+    int provRef = s.hasProv ? s.pRef : s.ref, provGolden = s.hasProv ? s.pGolden : s.golden;
+    busy.assign(s.pool.size(), 0);
+    if (provRef >= 0) busy[(size_t)provRef] = 1;
+    if (provGolden >= 0) busy[(size_t)provGolden] = 1;
+    for (int b : s.outputs) busy[(size_t)b] = 1;
+    for (int b : s.roundBufs[P ^ 1]) busy[(size_t)b] = 1;
+    s.roundBufs[P].clear();
     int k = s.resident ? lookahead_ : 1;
     if (maxFrames && ii < maxFrames->size()) k = std::max(0, std::min(k, (*maxFrames)[ii]));
+    const int slotBase = P * (lookahead_ + 1);
     int lastGpu = -1;  // job index of the chain's last GPU frame
     for (int step = 0; step < k; step++) {
       Job j;
       j.stream = id;
       j.step = step;
+      j.epoch = s.epoch;
       if (s.resident) {
         if (s.next >= (int64_t)s.hostPkts.size()) break;
         j.pktIndex = s.next;
@@ -439,15 +534,19 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
         j.hPkt = s.pendingPkt.data();
         j.n = s.pendingPkt.size();
         j.pktIndex = s.next++;
+        s.pending = false;
       }
       j.ref = provRef;
       j.golden = provGolden;
-      j.slot = step;
-      if (step > 0) j.hBefore = s.hist;
+      j.slot = slotBase + step;
+      j.hBefore = s.hist;
       planFrame(s, j, busy);
+      j.hAfter = s.hist;
       // (configure may have allocated the pool: references start as the zeroed buffers)
       if (j.ref < 0) j.ref = s.ref;
       if (j.golden < 0) j.golden = s.golden;
+      if (j.work >= 0) s.roundBufs[P].push_back(j.work);
+      if (j.ovBuf >= 0) s.roundBufs[P].push_back(j.ovBuf);
       if (j.status == kOK && j.gpu) {
         j.gateDesc = lastGpu;  // resolved to a descriptor index below
         if (!s.resident) {
@@ -463,9 +562,16 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
       jobs.push_back(std::move(j));
       if (stop) break;
     }
-    if (!chain.empty()) chains.push_back(std::move(chain));
+    if (!chain.empty()) {
+      R.chains.push_back(std::move(chain));
+      s.pRef = provRef;
+      s.pGolden = provGolden;
+      s.hasProv = true;
+      s.lastRound = R.id;
+    }
   }
-  // Raw frames: scatter the packed planes into their pool buffer.
+  // Raw frames: scatter the packed planes into their pool buffer (engine
+  // stream: after the previous round's reconstruction, before this one's).
   for (Job& j : jobs) {
     if (j.status != kOK || j.fh.coding != kCodingRaw) continue;
     Stream& s = *streams_[(size_t)j.stream];
@@ -483,15 +589,10 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
   int maxStep = -1;
   for (const Job& j : jobs)
     if (j.status == kOK && j.gpu) maxStep = std::max(maxStep, j.step);
-  struct StepInfo {
-    int mainFirst = 0, mainCount = 0, ovFirst = 0, ovCount = 0;
-    int jobFirst = 0, jobCount = 0, ovJobFirst = 0, ovJobCount = 0;
-    int maxInterMBs = 0, maxOvMBs = 0;
-  };
-  std::vector<StepInfo> steps((size_t)(maxStep + 1));
+  R.steps.assign((size_t)(maxStep + 1), StepInfo{});
   int nDesc = 0, nTiles = 0;
   for (int st = 0; st <= maxStep; st++) {
-    StepInfo& si = steps[(size_t)st];
+    StepInfo& si = R.steps[(size_t)st];
     si.mainFirst = nDesc;
     si.jobFirst = nTiles;
     for (Job& j : jobs) {
@@ -513,171 +614,273 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
       si.maxOvMBs = std::max(si.maxOvMBs, (int)streams_[(size_t)j.stream]->mbs);
     }
   }
-  std::vector<int32_t> statuses((size_t)std::max(nDesc, 1), 0);
-  if (nDesc > 0) {
-    const size_t oDesc = 0;
-    const size_t oStat = al(oDesc + sizeof(FrameDesc) * nDesc, 64);
-    const size_t oTab = al(oStat + sizeof(int32_t) * nDesc, 64);
-    const size_t oTiles = al(oTab + sizeof(DeviceTables) * nDesc, 64);
-    // Entropy jobs: groups of up to kEntropyTilesPerJob tiles of one frame.
-    std::vector<int> tilesOf((size_t)nDesc, 0);
-    for (const Job& j : jobs) {
-      if (j.mainDesc >= 0) tilesOf[(size_t)j.mainDesc] = (int)j.main.tiles.size();
-      if (j.ovDesc >= 0) tilesOf[(size_t)j.ovDesc] = (int)j.ov.tiles.size();
-    }
-    int nEJobs = 0;
-    for (int t : tilesOf) nEJobs += (t + kEntropyTilesPerJob - 1) / kEntropyTilesPerJob;
-    const size_t oJobs = al(oTiles + sizeof(TileRange) * (size_t)nTiles, 64);
-    const size_t oEJobs = al(oJobs + sizeof(int2) * (size_t)nTiles, 64);
-    const size_t oPkt = al(oEJobs + sizeof(int4) * (size_t)nEJobs, 256);
-    const size_t total = oPkt + streamedBytes;
-    if (ensureStage(total)) return -1;
-    uint8_t* h = hStage_;
-    uint8_t* d = dStage_;
-    FrameDesc* hd = reinterpret_cast<FrameDesc*>(h + oDesc);
-    int32_t* hs = reinterpret_cast<int32_t*>(h + oStat);
-    DeviceTables* ht = reinterpret_cast<DeviceTables*>(h + oTab);
-    TileRange* hr = reinterpret_cast<TileRange*>(h + oTiles);
-    int2* hj = reinterpret_cast<int2*>(h + oJobs);
-    // Tile jobs are laid out in descriptor order, so each descriptor's tiles
-    // and each step's job ranges are contiguous.
-    std::vector<int> tileFirst((size_t)nDesc, 0);
-    {
-      int acc = 0;
-      for (int di = 0; di < nDesc; di++) {
-        tileFirst[(size_t)di] = acc;
-        acc += tilesOf[(size_t)di];
-      }
-    }
-    std::vector<const PayloadPlan*> planOf((size_t)nDesc, nullptr);
-    auto fill = [&](const Job& j, const PayloadPlan& plan, int di, int rec, int ref, int gold, bool inter, int gateDesc,
-                    const Slot& sl) {
-      const Stream& s = *streams_[(size_t)j.stream];
-      FrameDesc& fd = hd[di];
-      std::memset(&fd, 0, sizeof(fd));
-      for (int k = 0; k < 3; k++) {
-        fd.rec[k] = s.plane(rec, k);
-        fd.ref[k] = s.plane(ref, k);
-        fd.gold[k] = s.plane(gold, k);
-      }
-      fd.strideY = s.strideY;
-      fd.strideC = s.strideC;
-      fd.padW = s.geo.padW();
-      fd.padH = s.geo.padH();
-      fd.padCW = s.geo.padCW();
-      fd.padCH = s.geo.padCH();
-      fd.mbCols = s.geo.mbCols;
-      fd.mbRows = s.geo.mbRows;
-      fd.inter = inter ? 1 : 0;
-      const Quant q = quantFor(plan.qp);
-      fd.qdc = q.dc;
-      fd.qac = q.ac;
-      fd.tileCount = (int)plan.tiles.size();
-      fd.pkt = j.dPkt ? j.dPkt : d + oPkt + j.stageOff;
-      fd.tables = reinterpret_cast<const DeviceTables*>(d + oTab) + di;
-      const int tf = tileFirst[(size_t)di];
-      fd.tiles = reinterpret_cast<const TileRange*>(d + oTiles) + tf;
-      fd.mbrec = sl.rec;
-      fd.coef = sl.coef;
-      fd.mvgrid = sl.mv;
-      fd.lvgrid = sl.lv;
-      fd.intraList = sl.intra;
-      fd.intraSorted = sl.intra + s.mbs;
-      fd.tileStat = sl.ts;
-      fd.status = reinterpret_cast<int32_t*>(d + oStat) + di;
-      fd.gate = gateDesc >= 0 ? reinterpret_cast<const int32_t*>(d + oStat) + gateDesc : nullptr;
-      hs[di] = 0;
-      ht[di] = plan.tables;
-      for (size_t t = 0; t < plan.tiles.size(); t++) {
-        hr[tf + t] = plan.tiles[t];
-        hj[tf + t] = make_int2(di, (int)t);
-      }
-      planOf[(size_t)di] = &plan;
-    };
-    for (Job& j : jobs) {
-      if (j.mainDesc < 0) continue;
-      Stream& s = *streams_[(size_t)j.stream];
-      const int gate = j.gateDesc >= 0 ? jobs[(size_t)j.gateDesc].mainDesc : -1;
-      fill(j, j.main, j.mainDesc, j.work, j.ref, j.golden, j.fh.coding == kCodingInter, gate, s.slots[(size_t)j.slot]);
-      if (!s.resident) std::memcpy(h + oPkt + j.stageOff, j.hPkt, j.n);
-      if (j.ovDesc >= 0)
-        fill(j, j.ov, j.ovDesc, j.ovBuf, j.work, j.work, true, j.mainDesc, s.slots.back());
-    }
-    {
-      // Longest tile first, so the slowest chains start in the first wave.
-      std::vector<std::pair<uint32_t, int4>> ej;
-      ej.reserve((size_t)nEJobs);
-      for (int di = 0; di < nDesc; di++) {
-        for (int t0 = 0; t0 < tilesOf[(size_t)di]; t0 += kEntropyTilesPerJob) {
-          const int nt = std::min(kEntropyTilesPerJob, tilesOf[(size_t)di] - t0);
-          uint32_t longest = 0;
-          for (int t = t0; t < t0 + nt; t++) longest = std::max(longest, planOf[(size_t)di]->tiles[(size_t)t].length);
-          ej.push_back({longest, make_int4(di, t0, nt, 0)});
-        }
-      }
-      std::stable_sort(ej.begin(), ej.end(), [](const std::pair<uint32_t, int4>& a,
-                                                const std::pair<uint32_t, int4>& b) { return a.first > b.first; });
-      int4* he = reinterpret_cast<int4*>(h + oEJobs);
-      for (size_t k = 0; k < ej.size(); k++) he[k] = ej[k].second;
-    }
-    if (cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, stream_) != cudaSuccess) return -1;
-    const FrameDesc* dd = reinterpret_cast<const FrameDesc*>(d + oDesc);
-    const int2* dj = reinterpret_cast<const int2*>(d + oJobs);
-    if (timing_) cudaEventRecord(ev_[0], stream_);
-    launchEntropy(dd, reinterpret_cast<const int4*>(d + oEJobs), nEJobs, stream_);
-    launches_++;
-    if (timing_) cudaEventRecord(ev_[1], stream_);
-    for (const StepInfo& si : steps) {
-      if (si.maxInterMBs > 0) {
-        launchInter(dd + si.mainFirst, si.mainCount, si.maxInterMBs, stream_);
-        launches_++;
-      }
-      if (si.jobCount > 0) {
-        launchIntra(dd, dj + si.jobFirst, si.jobCount, stream_);
-        launches_++;
-      }
-      if (si.ovCount > 0) {
-        launchInter(dd + si.ovFirst, si.ovCount, si.maxOvMBs, stream_);
-        launchIntra(dd, dj + si.ovJobFirst, si.ovJobCount, stream_);
-        launches_ += 2;
-      }
-    }
-    if (timing_) cudaEventRecord(ev_[2], stream_);
-    if (cudaMemcpyAsync(statuses.data(), d + oStat, sizeof(int32_t) * nDesc, cudaMemcpyDeviceToHost, stream_) !=
-        cudaSuccess)
-      return -1;
+  R.nDesc = nDesc;
+  R.nTiles = nTiles;
+  if (nDesc == 0) return kOK;
+  // Entropy jobs: groups of up to kEntropyTilesPerJob tiles of one frame.
+  std::vector<int> tilesOf((size_t)nDesc, 0);
+  for (const Job& j : jobs) {
+    if (j.mainDesc >= 0) tilesOf[(size_t)j.mainDesc] = (int)j.main.tiles.size();
+    if (j.ovDesc >= 0) tilesOf[(size_t)j.ovDesc] = (int)j.ov.tiles.size();
   }
+  int nEJobs = 0;
+  for (int t : tilesOf) nEJobs += (t + kEntropyTilesPerJob - 1) / kEntropyTilesPerJob;
+  R.nEJobs = nEJobs;
+  R.oDesc = 0;
+  R.oStat = al(R.oDesc + sizeof(FrameDesc) * nDesc, 64);
+  const size_t oTab = al(R.oStat + sizeof(int32_t) * nDesc, 64);
+  const size_t oTiles = al(oTab + sizeof(DeviceTables) * nDesc, 64);
+  R.oJobs = al(oTiles + sizeof(TileRange) * (size_t)nTiles, 64);
+  R.oEJobs = al(R.oJobs + sizeof(int2) * (size_t)nTiles, 64);
+  const size_t oPkt = al(R.oEJobs + sizeof(int4) * (size_t)nEJobs, 256);
+  const size_t total = oPkt + streamedBytes;
+  if (ensureStage(P, total) || ensureStatus(P, nDesc)) return -1;
+  uint8_t* h = hStage_[P];
+  uint8_t* d = dStage_[P];
+  FrameDesc* hd = reinterpret_cast<FrameDesc*>(h + R.oDesc);
+  int32_t* hs = reinterpret_cast<int32_t*>(h + R.oStat);
+  DeviceTables* ht = reinterpret_cast<DeviceTables*>(h + oTab);
+  TileRange* hr = reinterpret_cast<TileRange*>(h + oTiles);
+  int2* hj = reinterpret_cast<int2*>(h + R.oJobs);
+  // Tile jobs are laid out in descriptor order, so each descriptor's tiles
+  // and each step's job ranges are contiguous.
+  std::vector<int> tileFirst((size_t)nDesc, 0);
+  {
+    int acc = 0;
+    for (int di = 0; di < nDesc; di++) {
+      tileFirst[(size_t)di] = acc;
+      acc += tilesOf[(size_t)di];
+    }
+  }
+  std::vector<const PayloadPlan*> planOf((size_t)nDesc, nullptr);
+  auto fill = [&](const Job& j, const PayloadPlan& plan, int di, int rec, int ref, int gold, bool inter, int gateDesc,
+                  const Slot& sl) {
+    const Stream& s = *streams_[(size_t)j.stream];
+    FrameDesc& fd = hd[di];
+    std::memset(&fd, 0, sizeof(fd));
+    for (int k = 0; k < 3; k++) {
+      fd.rec[k] = s.plane(rec, k);
+      fd.ref[k] = s.plane(ref, k);
+      fd.gold[k] = s.plane(gold, k);
+    }
+    fd.strideY = s.strideY;
+    fd.strideC = s.strideC;
+    fd.padW = s.geo.padW();
+    fd.padH = s.geo.padH();
+    fd.padCW = s.geo.padCW();
+    fd.padCH = s.geo.padCH();
+    fd.mbCols = s.geo.mbCols;
+    fd.mbRows = s.geo.mbRows;
+    fd.inter = inter ? 1 : 0;
+    const Quant q = quantFor(plan.qp);
+    fd.qdc = q.dc;
+    fd.qac = q.ac;
+    fd.tileCount = (int)plan.tiles.size();
+    fd.pkt = j.dPkt ? j.dPkt : d + oPkt + j.stageOff;
+    fd.tables = reinterpret_cast<const DeviceTables*>(d + oTab) + di;
+    const int tf = tileFirst[(size_t)di];
+    fd.tiles = reinterpret_cast<const TileRange*>(d + oTiles) + tf;
+    fd.mbrec = sl.rec;
+    fd.coef = sl.coef;
+    fd.mvgrid = sl.mv;
+    fd.lvgrid = sl.lv;
+    fd.intraList = sl.intra;
+    fd.intraSorted = sl.intra + s.mbs;
+    fd.tileStat = sl.ts;
+    fd.status = reinterpret_cast<int32_t*>(d + R.oStat) + di;
+    fd.gate = gateDesc >= 0 ? reinterpret_cast<const int32_t*>(d + R.oStat) + gateDesc : nullptr;
+    hs[di] = 0;
+    ht[di] = plan.tables;
+    for (size_t t = 0; t < plan.tiles.size(); t++) {
+      hr[tf + t] = plan.tiles[t];
+      hj[tf + t] = make_int2(di, (int)t);
+    }
+    planOf[(size_t)di] = &plan;
+  };
+  for (Job& j : jobs) {
+    if (j.mainDesc < 0) continue;
+    Stream& s = *streams_[(size_t)j.stream];
+    const int gate = j.gateDesc >= 0 ? jobs[(size_t)j.gateDesc].mainDesc : -1;
+    const int ovSlot = P * (lookahead_ + 1) + lookahead_;
+    fill(j, j.main, j.mainDesc, j.work, j.ref, j.golden, j.fh.coding == kCodingInter, gate, s.slots[(size_t)j.slot]);
+    if (!s.resident) std::memcpy(h + oPkt + j.stageOff, j.hPkt, j.n);
+    if (j.ovDesc >= 0) fill(j, j.ov, j.ovDesc, j.ovBuf, j.work, j.work, true, j.mainDesc, s.slots[(size_t)ovSlot]);
+  }
+  {
+    // Longest tile first, so the slowest chains start in the first wave.
+    std::vector<std::pair<uint32_t, int4>> ej;
+    ej.reserve((size_t)nEJobs);
+    for (int di = 0; di < nDesc; di++) {
+      for (int t0 = 0; t0 < tilesOf[(size_t)di]; t0 += kEntropyTilesPerJob) {
+        const int nt = std::min(kEntropyTilesPerJob, tilesOf[(size_t)di] - t0);
+        uint32_t longest = 0;
+        for (int t = t0; t < t0 + nt; t++) longest = std::max(longest, planOf[(size_t)di]->tiles[(size_t)t].length);
+        ej.push_back({longest, make_int4(di, t0, nt, 0)});
+      }
+    }
+    std::stable_sort(ej.begin(), ej.end(), [](const std::pair<uint32_t, int4>& a,
+                                              const std::pair<uint32_t, int4>& b) { return a.first > b.first; });
+    int4* he = reinterpret_cast<int4*>(h + R.oEJobs);
+    for (size_t k = 0; k < ej.size(); k++) he[k] = ej[k].second;
+  }
+  if (cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, se) != cudaSuccess) return -1;
+  const FrameDesc* dd = reinterpret_cast<const FrameDesc*>(d + R.oDesc);
+  if (timing_) cudaEventRecord(ev_[P][0], se);
+  launchEntropy(dd, reinterpret_cast<const int4*>(d + R.oEJobs), nEJobs, se);
+  launches_++;
+  cudaEventRecord(ev_[P][1], se);  // entropy done: the reconstruction waits on it
+  R.launched = true;
+  return kOK;
+}
+
+int Engine::launchRecon(Round& R) {
+  if (!R.launched) return kOK;
+  const int P = R.parity;
+  uint8_t* h = hStage_[P];
+  uint8_t* d = dStage_[P];
+  // Frames of streams rolled back since planning: point their gate at a word
+  // that is always set, so the reconstruction skips them.
+  for (Job& j : R.jobs) {
+    const Stream* s = j.stream >= 0 && j.stream < (int)streams_.size() ? streams_[(size_t)j.stream].get() : nullptr;
+    if (s && j.epoch == s->epoch) continue;
+    for (int di : {j.mainDesc, j.ovDesc}) {
+      if (di < 0) continue;
+      FrameDesc* hd = reinterpret_cast<FrameDesc*>(h + R.oDesc) + di;
+      hd->gate = dOne_;
+      FrameDesc* ddi = reinterpret_cast<FrameDesc*>(d + R.oDesc) + di;
+      if (cudaMemcpyAsync(&ddi->gate, &hd->gate, sizeof(hd->gate), cudaMemcpyHostToDevice, stream_) != cudaSuccess)
+        return -1;
+    }
+  }
+  if (cudaStreamWaitEvent(stream_, ev_[P][1], 0) != cudaSuccess) return -1;
+  const FrameDesc* dd = reinterpret_cast<const FrameDesc*>(d + R.oDesc);
+  const int2* dj = reinterpret_cast<const int2*>(d + R.oJobs);
+  if (timing_) cudaEventRecord(ev_[P][2], stream_);
+  for (const StepInfo& si : R.steps) {
+    if (si.maxInterMBs > 0) {
+      launchInter(dd + si.mainFirst, si.mainCount, si.maxInterMBs, stream_);
+      launches_++;
+    }
+    if (si.jobCount > 0) {
+      launchIntra(dd, dj + si.jobFirst, si.jobCount, stream_);
+      launches_++;
+    }
+    if (si.ovCount > 0) {
+      launchInter(dd + si.ovFirst, si.ovCount, si.maxOvMBs, stream_);
+      launchIntra(dd, dj + si.ovJobFirst, si.ovJobCount, stream_);
+      launches_ += 2;
+    }
+  }
+  if (timing_) cudaEventRecord(ev_[P][3], stream_);
+  if (cudaMemcpyAsync(hStatus_[P], d + R.oStat, sizeof(int32_t) * R.nDesc, cudaMemcpyDeviceToHost, stream_) !=
+      cudaSuccess)
+    return -1;
+  return kOK;
+}
+
+int Engine::collectRound(Round& R, std::vector<RoundResult>* results) {
+  const int P = R.parity;
+  const bool gpu = R.nDesc > 0;
+  std::vector<int32_t> statuses((size_t)std::max(R.nDesc, 1), 0);
   if (cudaStreamSynchronize(stream_) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
-    for (Job& j : jobs)
+    for (Job& j : R.jobs)
       if (j.status == kOK) j.status = kErrDevice;
+  } else if (gpu) {
+    std::memcpy(statuses.data(), hStatus_[P], sizeof(int32_t) * R.nDesc);
   }
-  if (timing_ && nDesc > 0) {
+  if (timing_ && gpu) {
     float a = 0, b = 0;
-    cudaEventElapsedTime(&a, ev_[0], ev_[1]);
-    cudaEventElapsedTime(&b, ev_[1], ev_[2]);
+    cudaEventElapsedTime(&a, ev_[P][0], ev_[P][1]);
+    cudaEventElapsedTime(&b, ev_[P][2], ev_[P][3]);
     entropyMs_ += a;
     reconMs_ += b;
     kernelMs_ += a + b;
   }
   // ---- commit each stream's chain in order; roll back at the first skipped frame
   int attempted = 0;
-  for (const auto& chain : chains) {
-    Stream& s = *streams_[(size_t)jobs[(size_t)chain[0]].stream];
+  for (const auto& chain : R.chains) {
+    const int id = R.jobs[(size_t)chain[0]].stream;
+    if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) continue;  // removed meanwhile
+    Stream& s = *streams_[(size_t)id];
+    s.roundBufs[P].clear();
+    if (R.jobs[(size_t)chain[0]].epoch != s.epoch) continue;  // planned before a rollback: discarded
+    // A newer round of this stream was planned on top of this chain's
+    // outcome; commit this chain as if it were the newest.
+    const bool newer = s.lastRound > R.id;
+    TableHistory newest;
+    if (newer) {
+      newest = s.hist;
+      s.hist = R.jobs[(size_t)chain.back()].hAfter;
+    }
+    bool rolledBack = false, failed = false;
     for (size_t c = 0; c < chain.size(); c++) {
-      Job& j = jobs[(size_t)chain[c]];
+      Job& j = R.jobs[(size_t)chain[c]];
       if (j.mainDesc >= 0 && statuses[(size_t)j.mainDesc] == kSkipped) {
-        // The frame this one depended on failed: re-plan from here next round
-        // with the table history as it stood before this frame was planned.
+        // The frame this one depended on failed: re-plan from here with the
+        // table history as it stood before this frame was planned; anything
+        // planned after it is discarded.
         s.hist = j.hBefore;
         s.next = j.pktIndex;
+        rolledBack = true;
         break;
       }
-      finishFrame(s, j, statuses.data(), results);
+      failed = finishFrame(s, j, statuses.data(), results) != kOK || failed;
       attempted++;
     }
-    if (!s.resident) s.pending = false;
+    if (rolledBack || (newer && failed)) {
+      // The newer round assumed this chain's frames succeeded: discard it and
+      // continue after this chain.
+      if (!rolledBack) s.next = R.jobs[(size_t)chain.back()].pktIndex + 1;
+      s.epoch++;
+      s.hasProv = false;
+    } else if (newer) {
+      s.hist = newest;
+    }
+    if (s.lastRound == R.id) s.hasProv = false;  // no later round holds provisional state
   }
+  R.clear();
   return attempted;
+}
+
+int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* results,
+                     const std::vector<int>* maxFrames) {
+  if (!pipelined_) {
+    Round& R = rounds_[0];
+    R.parity = 0;
+    if (planRound(ids, maxFrames, R) || launchRecon(R)) {
+      for (Job& j : R.jobs)
+        if (j.status == kOK) j.status = kErrDevice;
+      R.nDesc = 0;
+      collectRound(R, results);
+      return -1;
+    }
+    return collectRound(R, results);
+  }
+  // Pipelined: plan this round and start its entropy stage, collect the
+  // round in flight, then launch this round's reconstruction.
+  const int p = inflight_ < 0 ? 0 : 1 - inflight_;
+  Round& R = rounds_[p];
+  R.parity = p;
+  const int planSt = planRound(ids, maxFrames, R);
+  int n = 0;
+  if (inflight_ >= 0) n = collectRound(rounds_[inflight_], results);
+  inflight_ = -1;
+  if (planSt || launchRecon(R)) {
+    for (Job& j : R.jobs)
+      if (j.status == kOK) j.status = kErrDevice;
+    R.nDesc = 0;
+    collectRound(R, results);
+    return -1;
+  }
+  inflight_ = p;
+  return n;
+}
+
+int Engine::drain(std::vector<RoundResult>* results) {
+  if (inflight_ < 0) return 0;
+  const int n = collectRound(rounds_[inflight_], results);
+  inflight_ = -1;
+  return n;
 }
 
 int Engine::downloadFrame(const EngineFrameView& v, uint8_t* packed, size_t cap) {
@@ -847,6 +1050,16 @@ int ebivgpu_batch_timing(ebivgpu_batch* b, int enable, double* kernel_ms, double
 }
 
 int ebivgpu_batch_set_lookahead(ebivgpu_batch* b, int frames) { return b ? b->e.setLookahead(frames) : kErrArg; }
+
+int ebivgpu_batch_set_pipeline(ebivgpu_batch* b, int on) { return b ? b->e.setPipelined(on != 0) : kErrArg; }
+
+int ebivgpu_batch_drain(ebivgpu_batch* b, int* frames) {
+  if (!b) return kErrArg;
+  b->last.clear();
+  const int n = b->e.drain(&b->last);
+  if (frames) *frames = n < 0 ? 0 : n;
+  return n < 0 ? kErrDevice : kOK;
+}
 
 int64_t ebivgpu_batch_launches(ebivgpu_batch* b) { return b ? b->e.launches() : 0; }
 uint64_t ebivgpu_batch_device_bytes(ebivgpu_batch* b) { return b ? (uint64_t)b->e.deviceBytes() : 0; }

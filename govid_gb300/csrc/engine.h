@@ -76,6 +76,14 @@ class Engine {
   // to ids) caps each stream's frames this round below the lookahead.
   int roundFor(const std::vector<int>& ids, std::vector<RoundResult>* results,
                const std::vector<int>* maxFrames = nullptr);
+  // Pipelined rounds (set before adding streams; resident streams only):
+  // each round() plans a round and starts its entropy stage on a second CUDA
+  // stream, collects the round in flight (whose results it returns) and then
+  // launches the new round's reconstruction, so one round's entropy overlaps
+  // the previous round's reconstruction.  drain() collects the last round.
+  int setPipelined(bool on);
+  bool pipelined() const { return pipelined_; }
+  int drain(std::vector<RoundResult>* results);
 
   int downloadFrame(const EngineFrameView& v, uint8_t* packed, size_t cap);
   int downloadStrided(const EngineFrameView& v, uint8_t* y, int ys, uint8_t* cb, uint8_t* cr, int cs);
@@ -83,7 +91,8 @@ class Engine {
   int64_t launches() const { return launches_; }
   size_t deviceBytes() const { return deviceBytes_; }
   // Per-stream HBM footprint (pool + scratch) for a geometry.
-  static size_t footprint(int w, int h, int ring, int lookahead);
+  static size_t footprint(int w, int h, int ring, int lookahead, bool pipelined = false);
+  static int poolSize(int ring, int lookahead, bool pipelined);
 
   // Kernel-time accounting: CUDA events recorded around each round's
   // kernels on the engine's stream.
@@ -96,22 +105,37 @@ class Engine {
  private:
   struct Stream;
   struct Job;
+  struct StepInfo;
+  struct Round;
   int configure(Stream& s, int w, int h);
   int planFrame(Stream& s, Job& j, std::vector<char>& busy);
-  void finishFrame(Stream& s, Job& j, const int32_t* statuses, std::vector<RoundResult>* results);
-  int ensureStage(size_t bytes);
+  int finishFrame(Stream& s, Job& j, const int32_t* statuses, std::vector<RoundResult>* results);
+  int ensureStage(int parity, size_t bytes);
+  int ensureStatus(int parity, int n);
+  int planRound(const std::vector<int>& ids, const std::vector<int>* maxFrames, Round& r);
+  int launchRecon(Round& r);
+  int collectRound(Round& r, std::vector<RoundResult>* results);
+  cudaStream_t entropyStream() const { return pipelined_ ? streamE_ : stream_; }
 
-  cudaStream_t stream_ = nullptr;
-  bool ownStream_ = false;
+  cudaStream_t stream_ = nullptr;   // reconstruction, copies, status read-back
+  cudaStream_t streamE_ = nullptr;  // entropy stage of pipelined rounds
+  bool ownStream_ = false, ownStreamE_ = false;
+  bool pipelined_ = false;
   std::vector<std::unique_ptr<Stream>> streams_;
-  uint8_t* dStage_ = nullptr;
-  uint8_t* hStage_ = nullptr;
-  size_t stageCap_ = 0;
+  std::unique_ptr<Round[]> rounds_;  // by parity
+  int inflight_ = -1;  // parity of the round whose reconstruction is in flight
+  int64_t roundSeq_ = 0;
+  uint8_t* dStage_[2] = {nullptr, nullptr};
+  uint8_t* hStage_[2] = {nullptr, nullptr};
+  size_t stageCap_[2] = {0, 0};
+  int32_t* hStatus_[2] = {nullptr, nullptr};
+  int statusCap_[2] = {0, 0};
+  int32_t* dOne_ = nullptr;  // constant 1: the gate of discarded frames
   int64_t launches_ = 0;
   int lookahead_ = 1;
   size_t deviceBytes_ = 0;
   bool timing_ = false;
-  cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev_[2][4] = {};
   double kernelMs_ = 0, entropyMs_ = 0, reconMs_ = 0;
 };
 

@@ -206,13 +206,18 @@ class Batch:
     """Many independent EBIV streams decoded together: each round decodes the
     next packet of every active stream with one set of kernel launches."""
 
-    def __init__(self, lookahead: int = 1):
+    def __init__(self, lookahead: int = 1, pipeline: bool = False):
+        """pipeline: each round() returns the previous round's results while
+        the new round's entropy stage overlaps its reconstruction; drain()
+        returns the last round's (resident streams only)."""
         L = _native.lib()
         h = C.c_void_p()
         _check(L.ebivgpu_batch_create(C.byref(h)), "batch")
         self._h, self._L = h, L
         if lookahead != 1:
             _check(L.ebivgpu_batch_set_lookahead(h, int(lookahead)), "lookahead")
+        if pipeline:
+            _check(L.ebivgpu_batch_set_pipeline(h, 1), "pipeline")
 
     def add_stream(self, packets: list[bytes], ring: int = 3) -> int:
         n = len(packets)
@@ -249,6 +254,15 @@ class Batch:
         else:
             arr = (C.c_int * len(ids))(*ids)
             _check(self._L.ebivgpu_batch_round_for(self._h, arr, len(ids), C.byref(n)))
+        return self._results()
+
+    def drain(self) -> list[BatchResult]:
+        """Collects the round in flight (pipelined batches)."""
+        n = C.c_int()
+        _check(self._L.ebivgpu_batch_drain(self._h, C.byref(n)))
+        return self._results()
+
+    def _results(self) -> list[BatchResult]:
         out = []
         for i in range(self._L.ebivgpu_batch_result_count(self._h)):
             s, st, k = C.c_int(), C.c_int(), C.c_int()

@@ -116,6 +116,13 @@ int ebivgpu_batch_timing(ebivgpu_batch* b, int enable, double* kernel_ms, double
  * tiles in one launch and reconstructs the frames in order.  Set it before
  * adding streams. */
 int ebivgpu_batch_set_lookahead(ebivgpu_batch* b, int frames);
+/* Pipelined rounds (set before adding streams; resident streams only): each
+ * ebivgpu_batch_round starts the new round's entropy stage, collects the
+ * round in flight and returns ITS results, so one round's entropy overlaps the
+ * previous round's reconstruction; ebivgpu_batch_drain collects the last one.
+ * Results and frame order per stream are those of the synchronous rounds. */
+int ebivgpu_batch_set_pipeline(ebivgpu_batch* b, int on);
+int ebivgpu_batch_drain(ebivgpu_batch* b, int* frames);
 int64_t ebivgpu_batch_launches(ebivgpu_batch* b);
 uint64_t ebivgpu_batch_device_bytes(ebivgpu_batch* b);
 /* HBM bytes one stream of this geometry holds (frame pool + scratch). */

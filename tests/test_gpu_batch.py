@@ -11,6 +11,18 @@ from helpers import encode_gen, first_diff, flash_gen, noisy_gen
 pytestmark = pytest.mark.gpu
 
 
+def run_rounds(b):
+    """All results of a batch, synchronous or pipelined: a pipelined round
+    returns the previous round's results, so stop after two empty rounds and
+    collect the last one."""
+    empty = 0
+    while empty < 2:
+        res = b.round()
+        empty = empty + 1 if not res else 0
+        yield from res
+    yield from b.drain()
+
+
 def _streams():
     out = []
     specs = [((160, 96), (1, 1), 18, 8, 1), ((320, 192), (2, 2), 22, 5, 2), ((96, 64), (4, 3), 28, 3, 3),
@@ -26,10 +38,10 @@ def _streams():
     return out
 
 
-@pytest.mark.parametrize("lookahead", [1, 4])
-def test_batch_matches_oracle(gpu_required, lookahead):
+@pytest.mark.parametrize("lookahead,pipeline", [(1, False), (4, False), (1, True), (4, True)])
+def test_batch_matches_oracle(gpu_required, lookahead, pipeline):
     streams = _streams()
-    b = ebiv.Batch(lookahead=lookahead)
+    b = ebiv.Batch(lookahead=lookahead, pipeline=pipeline)
     want, ids, dims = {}, [], {}
     for cont, w, h in streams:
         pkts = [p.data for p in ebiv.Reader(cont).packets()]
@@ -38,18 +50,14 @@ def test_batch_matches_oracle(gpu_required, lookahead):
         dims[sid] = (w, h)
         want[sid] = ebiv_oracle.decode_all(pkts)
     seen = 0
-    while True:
-        res = b.round()
-        if not res:
-            break
-        for r in res:
-            ws, wp = want[r.stream][r.frame_index]
-            assert r.status == ws, f"stream {r.stream} frame {r.frame_index}: status {r.status} vs {ws}"
-            if ws == 0:
-                w, h = dims[r.stream]
-                got = b.download(r, w, h)
-                assert got == wp, f"stream {r.stream} frame {r.frame_index}: {first_diff(got, wp, w, h)}"
-            seen += 1
+    for r in run_rounds(b):
+        ws, wp = want[r.stream][r.frame_index]
+        assert r.status == ws, f"stream {r.stream} frame {r.frame_index}: status {r.status} vs {ws}"
+        if ws == 0:
+            w, h = dims[r.stream]
+            got = b.download(r, w, h)
+            assert got == wp, f"stream {r.stream} frame {r.frame_index}: {first_diff(got, wp, w, h)}"
+        seen += 1
     assert seen == sum(len(v) for v in want.values())
 
 
@@ -120,8 +128,8 @@ def _zero_tile(pkt: bytes, tile: int) -> bytes:
     return bytes(b)
 
 
-@pytest.mark.parametrize("lookahead", [1, 4])
-def test_batch_error_mid_chain_matches_oracle(gpu_required, lookahead):
+@pytest.mark.parametrize("lookahead,pipeline", [(1, False), (4, False), (1, True), (4, True)])
+def test_batch_error_mid_chain_matches_oracle(gpu_required, lookahead, pipeline):
     # A frame that fails on the GPU leaves its references untouched
     # (ebiv/codec.go:174-191); later frames of the same round are re-planned.
     spec = ebiv.SceneSpec(width=160, height=96, seed=21, sprites=3)
@@ -131,15 +139,12 @@ def test_batch_error_mid_chain_matches_oracle(gpu_required, lookahead):
     pkts[8] = _zero_tile(pkts[8], 0)
     want = ebiv_oracle.decode_all(pkts)
     assert want[3][0] == ebiv.ErrCorrupt.status and want[8][0] == ebiv.ErrCorrupt.status
-    b = ebiv.Batch(lookahead=lookahead)
+    b = ebiv.Batch(lookahead=lookahead, pipeline=pipeline)
     b.add_stream(pkts)
     got = {}
-    while True:
-        res = b.round()
-        if not res:
-            break
-        for r in res:
-            got[r.frame_index] = (r.status, b.download(r, 160, 96) if r.status == 0 else None)
+    for r in run_rounds(b):
+        assert r.frame_index not in got, f"frame {r.frame_index} delivered twice"
+        got[r.frame_index] = (r.status, b.download(r, 160, 96) if r.status == 0 else None)
     assert sorted(got) == list(range(len(pkts)))
     for i, (ws, wp) in enumerate(want):
         assert got[i][0] == ws, f"frame {i}: status {got[i][0]} vs oracle {ws}"
@@ -176,3 +181,43 @@ def test_fuzzed_packets_match_oracle(gpu_required):
                 g = (e.status, None)
             assert g[0] == want[i][0], f"case {case} frame {i}: status {g[0]} vs oracle {want[i][0]}"
             assert g[1] == want[i][1], f"case {case} frame {i}: planes differ from the oracle"
+
+
+@pytest.mark.parametrize("lookahead", [1, 3])
+def test_fuzzed_streams_pipelined_batch_match_oracle(gpu_required, lookahead):
+    # Corrupted packets in several streams decoded together by a pipelined
+    # batch: every status and plane equals the oracle decoding each stream
+    # alone, through the rollbacks that failures force on rounds planned
+    # ahead of them.
+    import random
+
+    rng = random.Random(77 + lookahead)
+    streams = []
+    for k in range(4):
+        spec = ebiv.SceneSpec(width=96 + 32 * k, height=64, seed=300 + k, sprites=2)
+        cont = ebiv.encode_scene(spec, 14, qp=22, gop=5 + k, tiles=(2, 1), fast=True)
+        pkts = []
+        for p in (q.data for q in ebiv.Reader(cont).packets()):
+            b = bytearray(p)
+            if rng.random() < 0.3:
+                for _ in range(rng.randint(1, 3)):
+                    i = rng.randrange(len(b))
+                    b[i] ^= 1 << rng.randrange(8)
+            pkts.append(bytes(b))
+        streams.append((pkts, 96 + 32 * k, 64))
+    b = ebiv.Batch(lookahead=lookahead, pipeline=True)
+    want, dims = {}, {}
+    for pkts, w, h in streams:
+        sid = b.add_stream(pkts)
+        want[sid] = ebiv_oracle.decode_all(pkts)
+        dims[sid] = (w, h)
+    got = {}
+    for r in run_rounds(b):
+        key = (r.stream, r.frame_index)
+        assert key not in got, f"{key} delivered twice"
+        got[key] = (r.status, b.download(r, *dims[r.stream]) if r.status == 0 else None)
+    for sid, frames in want.items():
+        for i, (ws, wp) in enumerate(frames):
+            assert (sid, i) in got, f"stream {sid} frame {i} never delivered"
+            assert got[(sid, i)][0] == ws, f"stream {sid} frame {i}: status {got[(sid, i)][0]} vs {ws}"
+            assert got[(sid, i)][1] == wp, f"stream {sid} frame {i} differs from the oracle"
