@@ -732,7 +732,7 @@ struct ReconView {
   int strideY, strideC, padW, padH, padCW, padCH, mbCols;
   int32_t qdc, qac;
   const MBRec* mbrec;
-  const uint32_t* coef;
+  uint32_t* coef;
   __device__ __forceinline__ void load(const FrameDesc& f) {
     for (int k = 0; k < 3; k++) {
       rec[k] = f.rec[k];
@@ -877,7 +877,7 @@ constexpr int kIntraWarps = 8;
 // above-right), column 0 the column to its left; chroma likewise (9 x 9).
 constexpr int kAreaW = 48;
 struct IntraScratch {
-  int32_t ref[4 * 16 + 1];
+  int32_t ref[2][4 * 16 + 1];  // one reference array per half-warp block
   int32_t res[384];  // levels, then residuals (mbResidual)
   int32_t tmp[384];
   uint8_t areaY[17 * kAreaW];
@@ -909,17 +909,25 @@ __device__ __forceinline__ int32_t refValue(int i, int n, bool avAbove, bool avL
 
 // Predicts and reconstructs one n x n block (predictIntra,
 // ebiv/predict.go:131-219) at area coordinates (ax, ay) of working area a,
-// writing each sample to the area and to plane p at (px, py).
-__device__ void intraBlock(IntraScratch& S, uint8_t* a, int as, int ax, int ay, uint8_t* p, int stride, int px,
-                           int py, int n, int mode, bool avAbove, bool avLeft, bool avAR, const int32_t* res,
-                           int resStride, int lane) {
+// writing each sample to the area and to plane p at (px, py).  Lanes l of nl
+// (a half warp or the whole warp) share the block; every lane of the warp
+// calls it, with active false where its half has no block this step, so
+// both __syncwarp barriers see the full warp.
+__device__ void intraBlock(int32_t* ref, uint8_t* a, int as, int ax, int ay, uint8_t* p, int stride, int px, int py,
+                           int n, int mode, bool avAbove, bool avLeft, bool avAR, const int32_t* res, int resStride,
+                           int l, int nl, bool active) {
   const int corner = 2 * n;
-  for (int i = lane; i <= 4 * n; i += 32) S.ref[i] = refValue(i, n, avAbove, avLeft, avAR, a, as, ax, ay);
+  if (active)
+    for (int i = l; i <= 4 * n; i += nl) ref[i] = refValue(i, n, avAbove, avLeft, avAR, a, as, ax, ay);
   __syncwarp();
+  if (!active) {
+    __syncwarp();
+    return;
+  }
   int32_t dc = 0;
   if (mode == modeDC) {
     int32_t sum = 0;
-    for (int i = 0; i < n; i++) sum += S.ref[corner + 1 + i] + S.ref[corner - 1 - i];
+    for (int i = 0; i < n; i++) sum += ref[corner + 1 + i] + ref[corner - 1 - i];
     dc = (sum + n) / (2 * n);
   }
   int angle = 0, inv = 0;
@@ -934,13 +942,13 @@ __device__ void intraBlock(IntraScratch& S, uint8_t* a, int as, int ax, int ay, 
     default: break;
   }
   const int nn = n * n;
-  for (int o = lane; o < nn; o += 32) {
+  for (int o = l; o < nn; o += nl) {
     const int r = o / n, c = o - r * n;
     int32_t v;
     switch (mode) {
-      case modeV: v = S.ref[corner + 1 + c]; break;
-      case modeH: v = S.ref[corner - 1 - r]; break;
-      case modeTM: v = clampByteD(S.ref[corner + 1 + c] + S.ref[corner - 1 - r] - S.ref[corner]); break;
+      case modeV: v = ref[corner + 1 + c]; break;
+      case modeH: v = ref[corner - 1 - r]; break;
+      case modeTM: v = clampByteD(ref[corner + 1 + c] + ref[corner - 1 - r] - ref[corner]); break;
       case modeDC: v = dc; break;
       default: {
         const int aa = vertical ? r : c, b = vertical ? c : r;
@@ -949,16 +957,16 @@ __device__ void intraBlock(IntraScratch& S, uint8_t* a, int as, int ax, int ay, 
         auto ext = [&](int k) -> int32_t {
           if (k >= 0) {
             if (k > 2 * n) return 0;
-            return vertical ? S.ref[corner + k] : S.ref[corner - k];
+            return vertical ? ref[corner + k] : ref[corner - k];
           }
           const int t = (k * inv + 128) >> 8;
-          return vertical ? S.ref[corner - t] : S.ref[corner + t];
+          return vertical ? ref[corner - t] : ref[corner + t];
         };
         v = ((32 - fact) * ext(b + idx + 1) + fact * ext(b + idx + 2) + 16) >> 5;
       }
     }
     v = res ? clampByteD(wadd(v, res[r * resStride + c])) : clampByteD(v);
-    a[(ay + r) * as + ax + c] = (uint8_t)v;  // the block's reference array is already in S.ref
+    a[(ay + r) * as + ax + c] = (uint8_t)v;  // the block's reference array is already in ref
     p[(size_t)(py + r) * stride + px + c] = (uint8_t)v;
   }
   __syncwarp();
@@ -977,8 +985,13 @@ __device__ void intraMB(const ReconView& f, IntraScratch& S, int mbx, int mby, i
   const int mbLeft = mbx * 16, mbTop = mby * 16, mbRight = mbLeft + 16;
   uint8_t* const Y = f.rec[0];
   const int ys = f.strideY, cs = f.strideC;
+  // The residual was computed before the level loop (kIntraRecon) and
+  // stored over the macroblock's coefficient region.
   const uint32_t resMask = nzm & wm;
-  if (resMask) mbResidual(f.coef + (size_t)idx * kCoefPerMB, tx, resMask, f.qdc, f.qac, S.res, S.tmp, lane);
+  if (resMask) {
+    const uint32_t* rg = f.coef + (size_t)idx * kCoefPerMB;
+    for (int q = lane; q < 384; q += 32) S.res[q] = (int32_t)rg[q];
+  }
   // Working areas: the row above and the column to the left, where they
   // lie inside the tile (nothing outside it is ever predicted from).
   const bool up = mbTop > tileTop, left = mbLeft > tileLeft;
@@ -996,16 +1009,39 @@ __device__ void intraMB(const ReconView& f, IntraScratch& S, int mbx, int mby, i
     }
     __syncwarp();
   }
-  for (int k = 0; k < nb; k++) {
-    if (!((wm >> k) & 1)) break;
+  // Luma blocks.  A block reads its left, above-left, above and above-right
+  // neighbours only, so the 4x4 blocks with equal bx + 2*by are independent:
+  // ten diagonal steps of up to two blocks, one per half warp.  Blocks
+  // beyond the first unwritten one (a prefix in raster order) are skipped.
+  auto block = [&](int k, int l, int nl, bool active, int half) {
     const int bx = (k % per) * n, by = (k / per) * n;
     const int x0 = mbLeft + bx, y0 = mbTop + by;
     const bool avAbove = y0 > tileTop, avLeft = x0 > tileLeft;
     bool avAR = false;
     if (!(y0 <= tileTop || x0 + 2 * n > tileRight)) avAR = (y0 == mbTop) ? true : (x0 + 2 * n <= mbRight);
     const bool hasRes = (nzm >> k) & 1;
-    intraBlock(S, S.areaY, kAreaW, 1 + bx, 1 + by, Y, ys, x0, y0, n, r.lmode(k), avAbove, avLeft, avAR,
-               hasRes ? S.res + by * 16 + bx : nullptr, 16, lane);
+    intraBlock(S.ref[half], S.areaY, kAreaW, 1 + bx, 1 + by, Y, ys, x0, y0, n, active ? r.lmode(k) : 0, avAbove,
+               avLeft, avAR, hasRes ? S.res + by * 16 + bx : nullptr, 16, l, nl, active);
+  };
+  if (tx == 0) {
+    const int half = lane >> 4;
+    for (int t = 0; t < 10; t++) {
+      int k = -1, seen = 0;
+      for (int yy = 0; yy < 4; yy++) {
+        const int xx = t - 2 * yy;
+        if (xx >= 0 && xx < 4) {
+          if (seen == half) k = yy * 4 + xx;
+          seen++;
+        }
+      }
+      const bool active = k >= 0 && ((wm >> k) & 1);
+      block(active ? k : 0, lane & 15, 16, active, half);
+    }
+  } else {
+    for (int k = 0; k < nb; k++) {
+      if (!((wm >> k) & 1)) break;
+      block(k, lane, 32, true, 0);
+    }
   }
   const int cx0 = mbx * 8, cy0 = mby * 8;
   const int cmode = r.cmode();
@@ -1013,8 +1049,8 @@ __device__ void intraMB(const ReconView& f, IntraScratch& S, int mbx, int mby, i
     const uint32_t bit = 1u << (16 + pl);
     if (!(wm & bit)) break;
     const bool hasRes = (nzm & bit) != 0;
-    intraBlock(S, S.areaC[pl], 16, 1, 1, f.rec[1 + pl], cs, cx0, cy0, 8, cmode, up, left, false,
-               hasRes ? S.res + 256 + pl * 64 : nullptr, 8, lane);
+    intraBlock(S.ref[0], S.areaC[pl], 16, 1, 1, f.rec[1 + pl], cs, cx0, cy0, 8, cmode, up, left, false,
+               hasRes ? S.res + 256 + pl * 64 : nullptr, 8, lane, 32, true);
   }
 }
 
@@ -1047,6 +1083,21 @@ __global__ void __launch_bounds__(32 * kIntraWarps, 1) kIntraRecon(const FrameDe
   uint32_t* sorted = f.intraSorted + tr.mbBase;
   ReconView view;
   view.load(f);
+  // Residuals of every listed macroblock, all warps in parallel (they do not
+  // depend on neighbouring pixels); each replaces its macroblock's
+  // coefficient region, which nothing reads afterwards.
+  for (int i = warp; i < n; i += kIntraWarps) {
+    const int idx = (int)(list[i] & kIndexMask);
+    RecRegs rr;
+    rr.load(view.mbrec + idx);
+    const uint32_t resMask = rr.nzmask() & rr.wmask();
+    if (rr.mode() != kRecIntra || !resMask) continue;
+    uint32_t* cg = view.coef + (size_t)idx * kCoefPerMB;
+    mbResidual(cg, rr.tx(), resMask, view.qdc, view.qac, sS[warp].res, sS[warp].tmp, lane);
+    for (int q = lane; q < 384; q += 32) cg[q] = (uint32_t)sS[warp].res[q];
+    __syncwarp();
+  }
+  __syncthreads();
   auto runMB = [&](uint32_t e) {
     const int idx = (int)(e & kIndexMask);
     intraMB(view, sS[warp], idx % view.mbCols, idx / view.mbCols, tr.mbX0, tr.mbX1, tr.mbY0, lane);
