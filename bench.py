@@ -373,7 +373,9 @@ def all_rounds(b, lat=None):
 
 
 def run_batched(args):
-    """64 mixed streams in rounds vs the same streams one stream per launch."""
+    """64 mixed streams in rounds vs the same streams one stream per launch,
+    at each lookahead of --mix-lookahead (the first is the headline: the
+    latency-bounded configuration; the last the throughput one)."""
     import torch
 
     from govid_gb300 import ebiv
@@ -383,39 +385,49 @@ def run_batched(args):
     log(f"[bench] mix content ready in {time.time() - t0:.1f}s")
     eq1080 = sum(algorithmic_bytes([p.data for p in ebiv.Reader(c).packets()], w, h)
                  for w, h, c in streams)
-    b = ebiv.Batch(lookahead=args.mix_lookahead, pipeline=not args.no_pipeline)
-    single_b = ebiv.Batch(lookahead=1)
-    ids, single_ids = [], []
-    totals = 0
-    px = 0
-    for w, h, c in streams:
-        pk = [p.data for p in ebiv.Reader(c).packets()]
-        ids.append(b.add_stream(pk, ring=3))
-        single_ids.append(single_b.add_stream(pk, ring=3))
-        totals += len(pk)
-        px += len(pk) * w * h
-    # warm-up round set
-    for sid in ids:
-        b.seek(sid, 0)
-    b.round()
-    b.drain()
-    for sid in ids:
-        b.seek(sid, 0)
-    flush_l2()
-    lat = []
-    torch.cuda.synchronize()
-    b.timing(1)
-    ts = time.perf_counter()
-    frames = 0
-    for r in all_rounds(b, lat):
-        frames += 1
-        if r.status != 0:
-            raise RuntimeError(f"batched decode failed: {r}")
-    torch.cuda.synchronize()
-    te = time.perf_counter()
-    kernel_ms, _, _ = b.timing(-1)
-    batched_fps = frames / (te - ts)
+    pkts = [[p.data for p in ebiv.Reader(c).packets()] for _, _, c in streams]
+    totals = sum(len(pk) for pk in pkts)
+    px = sum(len(pk) * w * h for pk, (w, h, _) in zip(pkts, streams))
+    peak = 6800.0
+    try:
+        peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+    except Exception:
+        pass
+
+    def one(lookahead):
+        b = ebiv.Batch(lookahead=lookahead, pipeline=not args.no_pipeline)
+        ids = [b.add_stream(pk, ring=3) for pk in pkts]
+        for sid in ids:  # warm-up round
+            b.seek(sid, 0)
+        b.round()
+        b.drain()
+        for sid in ids:
+            b.seek(sid, 0)
+        flush_l2()
+        lat = []
+        torch.cuda.synchronize()
+        b.timing(1)
+        ts = time.perf_counter()
+        frames = 0
+        for r in all_rounds(b, lat):
+            frames += 1
+            if r.status != 0:
+                raise RuntimeError(f"batched decode failed: {r}")
+        torch.cuda.synchronize()
+        te = time.perf_counter()
+        kernel_ms, _, _ = b.timing(-1)
+        fps = frames / (te - ts)
+        hbm = eq1080 / (kernel_ms / 1000) / 1e9 if kernel_ms > 0 else 0.0
+        return {"lookahead_frames": lookahead, "frames": frames, "frames_per_s": round(fps, 2),
+                "frames_1080p_equiv_per_s": round(fps * (px / totals) / (W * H), 2),
+                "round_latency_ms": {"p50": round(1000 * statistics.median(lat), 3),
+                                     "p99": round(1000 * sorted(lat)[int(0.99 * (len(lat) - 1))], 3)},
+                "hbm_gbs_over_kernel_time": round(hbm, 2), "hbm_frac": round(hbm / peak, 4)}
+
+    runs = [one(int(k)) for k in str(args.mix_lookahead).split(",")]
     # one stream per launch: each stream decoded alone, one frame per round
+    single_b = ebiv.Batch(lookahead=1)
+    single_ids = [single_b.add_stream(pk, ring=3) for pk in pkts]
     flush_l2()
     torch.cuda.synchronize()
     s0 = time.perf_counter()
@@ -429,24 +441,15 @@ def run_batched(args):
     torch.cuda.synchronize()
     s1 = time.perf_counter()
     per_stream_fps = single / (s1 - s0)
-    peak = 6800.0
-    try:
-        peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
-    except Exception:
-        pass
-    hbm = eq1080 / (kernel_ms / 1000) / 1e9 if kernel_ms > 0 else 0.0
-    return {
-        "streams": len(streams), "distinct_bitstreams": len({id(c) for _, _, c in streams}),
-        "lookahead_frames": args.mix_lookahead, "pipelined_rounds": not args.no_pipeline,
-        "frames_per_stream": args.mix_frames, "frames": frames,
-        "frames_per_s": round(batched_fps, 2),
-        "frames_1080p_equiv_per_s": round(batched_fps * (px / totals) / (W * H), 2),
-        "one_stream_per_launch_frames_per_s": round(per_stream_fps, 2),
-        "speedup_vs_one_stream_per_launch": round(batched_fps / per_stream_fps, 3),
-        "round_latency_ms": {"p50": round(1000 * statistics.median(lat), 3),
-                             "p99": round(1000 * sorted(lat)[int(0.99 * (len(lat) - 1))], 3)},
-        "hbm_gbs_over_kernel_time": round(hbm, 2), "hbm_frac": round(hbm / peak, 4),
-    }
+    for r in runs:
+        r["speedup_vs_one_stream_per_launch"] = round(r["frames_per_s"] / per_stream_fps, 3)
+    out = {"streams": len(streams), "distinct_bitstreams": len({id(c) for _, _, c in streams}),
+           "pipelined_rounds": not args.no_pipeline, "frames_per_stream": args.mix_frames,
+           "one_stream_per_launch_frames_per_s": round(per_stream_fps, 2)}
+    out.update(runs[0])
+    if len(runs) > 1:
+        out["throughput_config"] = runs[-1]
+    return out
 
 
 def run_serve(args):
@@ -549,7 +552,7 @@ def main():
     ap.add_argument("--mix-frames", type=int, default=120)
     ap.add_argument("--mix-distinct", type=int, default=1)
     ap.add_argument("--lookahead", type=int, default=32)
-    ap.add_argument("--mix-lookahead", type=int, default=4)
+    ap.add_argument("--mix-lookahead", default="1,4", help="comma list: headline (latency-bounded) first")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-pipeline", action="store_true", help="synchronous rounds (no entropy/recon overlap)")
     ap.add_argument("--no-serve", action="store_true")
