@@ -283,24 +283,59 @@ def run_gpu(args):
     bytes_per_step = alg
     achieved = bytes_per_step * args.steps / kernel_s / 1e9 if kernel_s > 0 else 0.0
 
-    # ---- e2e: through the C-ABI codec, host packets in / host frames out ----
-    codec = ebiv.Codec(3)
-    for p in pkts[: min(n, 70)]:
-        codec.decode(p)
-    e2e_frames = 0
+    # ---- e2e: the Batch API end to end.  Every step uploads the clip's
+    # packets from pinned host memory (reload) and reads every decoded frame
+    # back into pinned host memory (queued copies, waited for at the end).
+    fb = frame_bytes(W, H)
     h2d = sum(len(p) for p in pkts)
-    d2h = n * frame_bytes(W, H)
+    d2h = n * fb
+    pin_pk = torch.empty(h2d, dtype=torch.uint8, pin_memory=True)
+    addrs, lens, o = [], [], 0
+    for p in pkts:
+        pin_pk[o:o + len(p)] = torch.frombuffer(bytearray(p), dtype=torch.uint8)
+        addrs.append(pin_pk.data_ptr() + o)
+        lens.append(len(p))
+        o += len(p)
+    ring_frames = 64
+    pin_out = torch.empty(ring_frames * fb, dtype=torch.uint8, pin_memory=True)
+    eb = ebiv.Batch(lookahead=args.lookahead, pipeline=not args.no_pipeline)
+    esid = eb.add_stream(pkts, ring=3)
+
+    def e2e_pass():
+        eb.reload(esid, addrs, lens)
+        k = 0
+        for r in all_rounds(eb):
+            if r.status != 0:
+                raise RuntimeError(f"decode failed at frame {r.frame_index}: {r.status}")
+            eb.download_async(r, pin_out.data_ptr() + (k % ring_frames) * fb, fb)
+            k += 1
+        eb.sync()
+        return k
+
+    for _ in range(args.warmup):
+        e2e_pass()
+    e2e_frames = 0
+    flush_l2()
     barrier(dist)
     torch.cuda.synchronize()
     e0 = time.perf_counter()
-    for _ in range(args.steps):
-        for p in pkts:
-            codec.decode(p)
-            e2e_frames += 1
+    for s in range(args.steps):
+        if s:
+            flush_l2()
+        e2e_frames += e2e_pass()
     torch.cuda.synchronize()
     e1 = time.perf_counter()
     e2e_elapsed = max_over_ranks(dist, e1 - e0)
     e2e = e2e_frames * world / e2e_elapsed
+    # The govid Codec contract (one packet in, one host frame out per call).
+    codec = ebiv.Codec(3)
+    for p in pkts[:20]:
+        codec.decode(p)
+    torch.cuda.synchronize()
+    c0 = time.perf_counter()
+    for p in pkts:
+        codec.decode(p)
+    codec_fps = n / (time.perf_counter() - c0)
 
     peaks = {}
     try:
@@ -327,7 +362,9 @@ def run_gpu(args):
                    "frames_per_step": n, "packet_bytes_per_step": h2d, "l2": "flushed between steps",
                    "lookahead_frames": args.lookahead, "pipelined_rounds": not args.no_pipeline,
                    "parallelism": f"replicas x{world}"},
-        "e2e": {"value": round(e2e, 2), "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": round(e2e, 2), "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "api": "Batch: packets reloaded from pinned host memory, every frame copied to pinned host memory"},
+        "codec_api_frames_per_s": round(codec_fps, 2),
         "latency_ms": {"p50": round(1000 * statistics.median(lat), 3) if lat else None,
                        "p99": round(1000 * sorted(lat)[int(0.99 * (len(lat) - 1))], 3) if lat else None},
         "kernel_ms_per_step": {"total": round(kernel_ms / args.steps, 3), "entropy": round(entropy_ms / args.steps, 3),

@@ -66,6 +66,7 @@ struct Engine::Stream {
   // Resident packets: host copies (for planning) and one device block.
   std::vector<std::vector<uint8_t>> hostPkts;
   uint8_t* dPkts = nullptr;
+  size_t dPktsCap = 0;
   std::vector<size_t> dOff;
   int64_t next = 0;
   // Streaming: the submitted packet awaiting its round.
@@ -215,14 +216,69 @@ int Engine::addResidentStream(const uint8_t* const* pkts, const size_t* lens, in
     total += al(lens[i], 16);
   }
   if (cudaMalloc(&s->dPkts, total ? total : 16) != cudaSuccess) return kErrDevice;
+  s->dPktsCap = total ? total : 16;
   for (int i = 0; i < n; i++)
     if (lens[i] && cudaMemcpy(s->dPkts + s->dOff[(size_t)i], pkts[i], lens[i], cudaMemcpyHostToDevice) != cudaSuccess)
       return kErrDevice;
-  s->bytes += total;
-  deviceBytes_ += total;
+  s->bytes += s->dPktsCap;
+  deviceBytes_ += s->dPktsCap;
   s->id = (int)streams_.size();
   *id = s->id;
   streams_.push_back(std::move(s));
+  return kOK;
+}
+
+// Replaces a resident stream's packets (a new clip on the same stream: it
+// starts with a key frame of the stream's size) and rewinds it, keeping its
+// frame pool.  The copies run on the entropy stream, ahead of the next
+// round's entropy stage, the only reader of packet bytes.
+int Engine::reloadStream(int id, const uint8_t* const* pkts, const size_t* lens, int n) {
+  if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id] || n < 0) return kErrArg;
+  if (inflight_ >= 0) return kErrArg;  // drain() first
+  Stream& s = *streams_[(size_t)id];
+  if (!s.resident) return kErrArg;
+  size_t total = 0;
+  s.hostPkts.resize((size_t)n);
+  s.dOff.resize((size_t)n);
+  for (int i = 0; i < n; i++) {
+    s.hostPkts[(size_t)i].assign(pkts[i], pkts[i] + lens[i]);
+    s.dOff[(size_t)i] = total;
+    total += al(lens[i], 16);
+  }
+  cudaStream_t se = entropyStream();
+  if (total > s.dPktsCap) {
+    if (cudaStreamSynchronize(se) != cudaSuccess) return kErrDevice;
+    cudaFree(s.dPkts);
+    s.bytes -= s.dPktsCap;
+    deviceBytes_ -= s.dPktsCap;
+    s.dPkts = nullptr;
+    s.dPktsCap = 0;
+    if (cudaMalloc(&s.dPkts, total) != cudaSuccess) return kErrDevice;
+    s.dPktsCap = total;
+    s.bytes += total;
+    deviceBytes_ += total;
+  }
+  for (int i = 0; i < n; i++)
+    if (lens[i] &&
+        cudaMemcpyAsync(s.dPkts + s.dOff[(size_t)i], pkts[i], lens[i], cudaMemcpyHostToDevice, se) != cudaSuccess)
+      return kErrDevice;
+  s.next = 0;
+  s.hasProv = false;
+  s.epoch++;
+  return kOK;
+}
+
+int Engine::downloadFrameAsync(const EngineFrameView& v, uint8_t* packed, size_t cap) {
+  const int cw = (v.width + 1) / 2, ch = (v.height + 1) / 2;
+  const size_t need = (size_t)v.width * v.height + 2 * (size_t)cw * ch;
+  if (!v.y || cap < need) return kErrArg;
+  uint8_t* y = packed;
+  uint8_t* cb = packed + (size_t)v.width * v.height;
+  uint8_t* cr = cb + (size_t)cw * ch;
+  if (cudaMemcpy2DAsync(y, v.width, v.y, v.yStride, v.width, v.height, cudaMemcpyDeviceToHost, stream_) ||
+      cudaMemcpy2DAsync(cb, cw, v.cb, v.cStride, cw, ch, cudaMemcpyDeviceToHost, stream_) ||
+      cudaMemcpy2DAsync(cr, cw, v.cr, v.cStride, cw, ch, cudaMemcpyDeviceToHost, stream_))
+    return kErrDevice;
   return kOK;
 }
 
@@ -1035,6 +1091,24 @@ int ebivgpu_batch_result_download(ebivgpu_batch* b, int i, uint8_t* packed, size
   const RoundResult& r = b->last[(size_t)i];
   if (r.status != kOK) return r.status;
   return b->e.downloadFrame(r.view, packed, cap);
+}
+
+int ebivgpu_batch_result_download_async(ebivgpu_batch* b, int i, uint8_t* packed, size_t cap) {
+  if (!b || i < 0 || i >= (int)b->last.size()) return kErrArg;
+  const RoundResult& r = b->last[(size_t)i];
+  if (r.status != kOK) return r.status;
+  return b->e.downloadFrameAsync(r.view, packed, cap);
+}
+
+int ebivgpu_batch_sync(ebivgpu_batch* b) {
+  if (!b) return kErrArg;
+  return cudaStreamSynchronize(b->e.stream()) == cudaSuccess ? kOK : kErrDevice;
+}
+
+int ebivgpu_batch_reload_stream(ebivgpu_batch* b, int stream_id, const uint8_t* const* pkts, const size_t* lens,
+                                int n) {
+  if (!b || (!pkts && n) || (!lens && n)) return kErrArg;
+  return b->e.reloadStream(stream_id, pkts, lens, n);
 }
 
 int ebivgpu_batch_timing(ebivgpu_batch* b, int enable, double* kernel_ms, double* entropy_ms, double* recon_ms) {

@@ -86,6 +86,11 @@ class Engine {
   int drain(std::vector<RoundResult>* results);
 
   int downloadFrame(const EngineFrameView& v, uint8_t* packed, size_t cap);
+  // Queues the copy on the engine's stream; complete after the stream syncs.
+  int downloadFrameAsync(const EngineFrameView& v, uint8_t* packed, size_t cap);
+  // New packets for a resident stream (its frame pool is kept); no round may
+  // be in flight.
+  int reloadStream(int id, const uint8_t* const* pkts, const size_t* lens, int n);
   int downloadStrided(const EngineFrameView& v, uint8_t* y, int ys, uint8_t* cb, uint8_t* cr, int cs);
   int copyReference(int id, int which, uint8_t* dst, size_t cap);
   int64_t launches() const { return launches_; }

@@ -277,6 +277,22 @@ class Batch:
         _check(self._L.ebivgpu_batch_result_download(self._h, r.index, buf, n))
         return bytes(buf)
 
+    def download_async(self, r: BatchResult, address: int, cap: int) -> None:
+        """Queues the packed planes of r into host memory at address (pinned
+        memory makes the copy asynchronous); complete after sync()."""
+        _check(self._L.ebivgpu_batch_result_download_async(self._h, r.index, C.c_void_p(address), cap))
+
+    def sync(self) -> None:
+        _check(self._L.ebivgpu_batch_sync(self._h))
+
+    def reload(self, sid: int, addresses: list[int], lengths: list[int]) -> None:
+        """New packets (host addresses, e.g. in pinned memory) for a resident
+        stream; rewinds it and keeps its frame pool (no round in flight)."""
+        n = len(addresses)
+        a = (C.c_void_p * n)(*addresses)
+        ln = (C.c_size_t * n)(*lengths)
+        _check(self._L.ebivgpu_batch_reload_stream(self._h, sid, a, ln, n), "reload")
+
     def planes(self, r: BatchResult) -> "_native.PlaneView":
         v = _native.PlaneView()
         _check(self._L.ebivgpu_batch_result_planes(self._h, r.index, C.byref(v)))

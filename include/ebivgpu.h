@@ -122,6 +122,17 @@ int ebivgpu_batch_set_lookahead(ebivgpu_batch* b, int frames);
  * previous round's reconstruction; ebivgpu_batch_drain collects the last one.
  * Results and frame order per stream are those of the synchronous rounds. */
 int ebivgpu_batch_set_pipeline(ebivgpu_batch* b, int on);
+/* Replaces a resident stream's packets with a new clip of the same size
+ * (starting with a key frame) and rewinds it; its frame pool is kept.  No
+ * round may be in flight (drain first); the copies from pkts (pinned memory
+ * makes them asynchronous) complete before the next round's decode. */
+int ebivgpu_batch_reload_stream(ebivgpu_batch* b, int stream_id, const uint8_t* const* pkts, const size_t* lens,
+                                int n);
+/* Queues a result's packed-plane copy to host memory without waiting;
+ * ebivgpu_batch_sync waits for every queued copy.  A result's frame stays
+ * valid until `ring` newer frames of its stream are returned. */
+int ebivgpu_batch_result_download_async(ebivgpu_batch* b, int index, uint8_t* packed, size_t cap);
+int ebivgpu_batch_sync(ebivgpu_batch* b);
 int ebivgpu_batch_drain(ebivgpu_batch* b, int* frames);
 int64_t ebivgpu_batch_launches(ebivgpu_batch* b);
 uint64_t ebivgpu_batch_device_bytes(ebivgpu_batch* b);
