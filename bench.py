@@ -127,7 +127,7 @@ def frame_bytes(w, h):
 
 
 def algorithmic_bytes(packets, w, h):
-    """SURVEY-defined bytes per decoded frame: packet + visible output written
+    """Algorithmic bytes per decoded frame: packet + visible output written
     once + one reference read per predicted sample for inter frames."""
     from govid_gb300 import ebiv
 

@@ -1375,7 +1375,7 @@ MotionVector TileEncoder::searchMVRect(const Frame* ref, int mbx, int mby, int p
 
 // Exhaustive full-pel search over +-range pixels around zero and the
 // predictor, then the same half/quarter-pel refinement as the diamond.  It is
-// the reference search the learned proposer is trained against and judged by.
+// the reference search the learned proposer is trained and evaluated against.
 MotionVector TileEncoder::searchExhaustive(const Frame* ref, int mbx, int mby, int px, int py, int pw, int ph,
                                            MotionVector pred) {
   MotionVector best;

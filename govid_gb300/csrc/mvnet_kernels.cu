@@ -13,7 +13,7 @@
 // activations are stored in BF16, every product is accumulated in FP32,
 // gradients and the Adam state are FP32.  Labels come from an exhaustive
 // full-pel SAD search on the GPU (kExhaustive), the search the proposer is
-// trained against and judged by.
+// trained and evaluated against.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
