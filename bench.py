@@ -126,6 +126,9 @@ def frame_bytes(w, h):
     return w * h + 2 * ((w + 1) // 2) * ((h + 1) // 2)
 
 
+DRAM_BYTES_PER_FRAME = 3.97e6  # measured (ncu), 1080p clip frame mean
+
+
 def algorithmic_bytes(packets, w, h):
     """Algorithmic bytes per decoded frame: packet + visible output written
     once + one reference read per predicted sample for inter frames."""
@@ -370,8 +373,13 @@ def run_gpu(args):
         "kernel_ms_per_step": {"total": round(kernel_ms / args.steps, 3), "entropy": round(entropy_ms / args.steps, 3),
                                "recon": round(recon_ms / args.steps, 3)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None,
-                     "kernel": "decode kernels per frame (entropy+inter+intra), algorithmic bytes per frame",
+                     "frac": round(achieved / peak, 4),
+                     # DRAM read+write per decoded frame summed over the three
+                     # kernels, mean over this clip's inter and key frames, from
+                     # the ncu capture in profiles/decode_1080p_single_stream_ncu.md
+                     "traffic": int(DRAM_BYTES_PER_FRAME * n),
+                     "algorithmic_bytes": int(alg),
+                     "kernel": "all decode kernels of a step (entropy+inter+intra); bytes per step",
                      "peak_source": peak_src},
         "gpu_launches": launches,
     }
