@@ -508,7 +508,8 @@ def run_serve(args):
     base = mix_streams(args.mix_frames, args.mix_distinct)
     rng = random.Random(args.serve_seed)
     srv = ebiv.Server(duration_s=args.serve_seconds, frames_per_stream=600, seek_prob=0.05, seed=args.serve_seed,
-                      hbm_budget_bytes=120 << 30, max_frames_per_round=args.serve_max_frames, ring=3)
+                      hbm_budget_bytes=120 << 30, max_frames_per_round=args.serve_max_frames, ring=3,
+                      key_lane=True, start_spread_s=1.0)
     counts = {}
     for i in range(args.serve_streams):
         w, h, c = base[i % len(base)]
@@ -524,6 +525,7 @@ def run_serve(args):
         "loops": st["loops"], "rounds": st["rounds"], "frames_per_s": round(st["frames_per_s"], 2),
         "latency_ms": {"p50": round(st["latency_p50_ms"], 3), "p99": round(st["latency_p99_ms"], 3),
                        "max": round(st["latency_max_ms"], 3)},
+        "key_lane": True, "start_spread_s": 1.0, "key_frames": st["key_frames"],
         "note": "clips are the 120-frame mix bitstreams: non-looping streams end at their clip end",
     }
 

@@ -36,7 +36,8 @@ class PlaneView(C.Structure):
 class ServeOptions(C.Structure):
     _fields_ = [("duration_s", C.c_double), ("frames_per_stream", C.c_int64), ("seek_prob", C.c_double),
                 ("seed", C.c_uint64), ("hbm_budget_bytes", C.c_uint64), ("max_frames_per_round", C.c_int32),
-                ("ring", C.c_int32), ("record", C.c_int32)]
+                ("ring", C.c_int32), ("record", C.c_int32), ("key_lane", C.c_int32),
+                ("start_spread_s", C.c_double)]
 
 
 class ServeStats(C.Structure):

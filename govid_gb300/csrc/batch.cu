@@ -82,7 +82,8 @@ struct Engine::Stream {
   int pRef = -1, pGolden = -1;
   int64_t lastRound = 0;
   int64_t epoch = 0;
-  std::vector<int> roundBufs[2];
+  std::vector<int> roundBufs[3];  // by round parity (2: side lane)
+  bool inSide = false;            // a side round holds this stream
 
   uint8_t* plane(int b, int k) const {
     return pool[(size_t)b] + (k == 0 ? 0 : yBytes + (size_t)(k - 1) * cBytes);
@@ -145,14 +146,16 @@ struct Engine::Round {
   }
 };
 
-Engine::Engine() : rounds_(new Round[2]) {}
+Engine::Engine() : rounds_(new Round[3]) {}
 
 Engine::~Engine() {
   if (streamE_) cudaStreamSynchronize(streamE_);
   if (stream_) cudaStreamSynchronize(stream_);
   for (auto& s : streams_)
     if (s) s->release();
-  for (int p = 0; p < 2; p++) {
+  if (streamES_) cudaStreamSynchronize(streamES_);
+  if (streamRS_) cudaStreamSynchronize(streamRS_);
+  for (int p = 0; p < kParities; p++) {
     if (dStage_[p]) cudaFree(dStage_[p]);
     if (hStage_[p]) cudaFreeHost(hStage_[p]);
     if (hStatus_[p]) cudaFreeHost(hStatus_[p]);
@@ -160,6 +163,9 @@ Engine::~Engine() {
       if (e) cudaEventDestroy(e);
   }
   if (dOne_) cudaFree(dOne_);
+  if (sideDone_) cudaEventDestroy(sideDone_);
+  if (streamES_) cudaStreamDestroy(streamES_);
+  if (streamRS_) cudaStreamDestroy(streamRS_);
   if (ownStreamE_ && streamE_) cudaStreamDestroy(streamE_);
   if (ownStream_ && stream_) cudaStreamDestroy(stream_);
 }
@@ -192,14 +198,16 @@ int Engine::setLookahead(int k) {
 // Frame buffers per stream: the ring's outputs plus a round's, the two
 // references, and the buffers a round claims; a pipelined engine holds two
 // rounds' worth of claims.
-int Engine::poolSize(int ring, int k, bool pipelined) { return pipelined ? ring + 3 * k + 4 : ring + 2 * k + 3; }
+int Engine::poolSize(int ring, int k, bool pipelined, bool side) {
+  return (pipelined ? ring + 3 * k + 4 : ring + 2 * k + 3) + (side ? k + 1 : 0);
+}
 
-size_t Engine::footprint(int w, int h, int ring, int lookahead, bool pipelined) {
+size_t Engine::footprint(int w, int h, int ring, int lookahead, bool pipelined, bool side) {
   const Geometry g = Geometry::of(w, h);
   const size_t yb = (size_t)stride64(g.padW()) * g.padH(), cb = (size_t)stride64(g.padCW()) * g.padCH();
   const size_t mbs = (size_t)g.mbCols * g.mbRows;
-  return (size_t)poolSize(ring, lookahead, pipelined) * (yb + 2 * cb) +
-         (size_t)(pipelined ? 2 : 1) * (lookahead + 1) * Slot::bytes(mbs);
+  return (size_t)poolSize(ring, lookahead, pipelined, side) * (yb + 2 * cb) +
+         (size_t)((pipelined ? 2 : 1) + (side ? 1 : 0)) * (lookahead + 1) * Slot::bytes(mbs);
 }
 
 int Engine::addResidentStream(const uint8_t* const* pkts, const size_t* lens, int n, int ring, int* id) {
@@ -324,6 +332,8 @@ int Engine::setActive(int id, bool active) {
 int Engine::removeStream(int id) {
   if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) return kErrArg;
   if (streamE_) cudaStreamSynchronize(streamE_);
+  if (streamES_) cudaStreamSynchronize(streamES_);
+  if (streamRS_) cudaStreamSynchronize(streamRS_);
   cudaStreamSynchronize(stream_);
   deviceBytes_ -= streams_[(size_t)id]->bytes;
   streams_[(size_t)id]->release();
@@ -342,11 +352,12 @@ int Engine::configure(Stream& s, int w, int h) {
   s.cBytes = (size_t)s.strideC * s.geo.padCH();
   s.bufBytes = s.yBytes + 2 * s.cBytes;
   const int k = s.resident ? lookahead_ : 1;
-  const int P = poolSize(s.ring, k, pipelined_);
+  const int P = poolSize(s.ring, k, pipelined_, side_);
+  cudaStream_t zs = planStream_ ? planStream_ : stream_;
   for (int i = 0; i < P; i++) {
     uint8_t* p = nullptr;
     if (cudaMalloc(&p, s.bufBytes) != cudaSuccess) return kErrDevice;
-    if (cudaMemsetAsync(p, 0, s.bufBytes, stream_) != cudaSuccess) return kErrDevice;
+    if (cudaMemsetAsync(p, 0, s.bufBytes, zs) != cudaSuccess) return kErrDevice;
     s.pool.push_back(p);
   }
   // The reference allocates zeroed work/ref/golden buffers at configure.
@@ -357,12 +368,12 @@ int Engine::configure(Stream& s, int w, int h) {
   // Job slots index lookahead_ + 1 per parity; streaming streams use slot 0
   // and the override slot.
   const int perParity = lookahead_ + 1;
-  s.slots.resize((size_t)(pipelined_ ? 2 : 1) * perParity);
+  s.slots.resize((size_t)slotSets() * perParity);
   for (size_t i = 0; i < s.slots.size(); i++) {
     const int within = (int)(i % (size_t)perParity);
     if ((within < k || within == perParity - 1) && !s.slots[i].alloc(s.mbs)) return kErrDevice;
   }
-  const size_t b = (size_t)P * s.bufBytes + (size_t)(pipelined_ ? 2 : 1) * (k + 1) * Slot::bytes(s.mbs);
+  const size_t b = (size_t)P * s.bufBytes + (size_t)slotSets() * (k + 1) * Slot::bytes(s.mbs);
   s.bytes += b;
   deviceBytes_ += b;
   s.ready = true;
@@ -463,7 +474,7 @@ int Engine::planFrame(Stream& s, Job& j, std::vector<char>& busy) {
       if (j.ovBuf < 0) return j.status = kErrDevice;
       busy[(size_t)j.ovBuf] = 1;
       if (cudaMemcpyAsync(s.pool[(size_t)j.ovBuf], s.pool[(size_t)j.golden], s.bufBytes, cudaMemcpyDeviceToDevice,
-                          stream_) != cudaSuccess)
+                          planStream_) != cudaSuccess)
         return j.status = kErrDevice;
     }
   }
@@ -553,11 +564,16 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
   std::vector<Job>& jobs = R.jobs;
   jobs.reserve(ids.size() * (size_t)lookahead_);
   size_t streamedBytes = 0;
-  cudaStream_t se = entropyStream();
+  cudaStream_t se = entropyStream(P);
+  cudaStream_t sr = reconStream(P);
+  planStream_ = sr;
   for (size_t ii = 0; ii < ids.size(); ii++) {
     const int id = ids[ii];
     if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) continue;
     Stream& s = *streams_[(size_t)id];
+    // A stream in the side lane stays out of main rounds; the side lane takes
+    // only streams with no round in flight.
+    if (P == kSide ? (s.inSide || s.hasProv) : s.inSide) continue;
     std::vector<int> chain;
     std::vector<char> busy;
     // Start from the provisional references after the stream's in-flight
@@ -567,11 +583,13 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
     if (provRef >= 0) busy[(size_t)provRef] = 1;
     if (provGolden >= 0) busy[(size_t)provGolden] = 1;
     for (int b : s.outputs) busy[(size_t)b] = 1;
-    for (int b : s.roundBufs[P ^ 1]) busy[(size_t)b] = 1;
+    for (int q = 0; q < kParities; q++)
+      if (q != P)
+        for (int b : s.roundBufs[q]) busy[(size_t)b] = 1;
     s.roundBufs[P].clear();
     int k = s.resident ? lookahead_ : 1;
     if (maxFrames && ii < maxFrames->size()) k = std::max(0, std::min(k, (*maxFrames)[ii]));
-    const int slotBase = P * (lookahead_ + 1);
+    const int slotBase = slotSet(P) * (lookahead_ + 1);
     int lastGpu = -1;  // job index of the chain's last GPU frame
     for (int step = 0; step < k; step++) {
       Job j;
@@ -624,6 +642,7 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
       s.pGolden = provGolden;
       s.hasProv = true;
       s.lastRound = R.id;
+      if (P == kSide) s.inSide = true;
     }
   }
   // Raw frames: scatter the packed planes into their pool buffer (engine
@@ -634,11 +653,10 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
     const Geometry& g = s.geo;
     const uint8_t* body = j.hPkt + j.fh.bodyOffset;
     const size_t ys = (size_t)g.W * g.H, cs = (size_t)g.CW * g.CH;
-    if (cudaMemcpy2DAsync(s.plane(j.work, 0), s.strideY, body, g.W, g.W, g.H, cudaMemcpyHostToDevice, stream_) ||
-        cudaMemcpy2DAsync(s.plane(j.work, 1), s.strideC, body + ys, g.CW, g.CW, g.CH, cudaMemcpyHostToDevice,
-                          stream_) ||
+    if (cudaMemcpy2DAsync(s.plane(j.work, 0), s.strideY, body, g.W, g.W, g.H, cudaMemcpyHostToDevice, sr) ||
+        cudaMemcpy2DAsync(s.plane(j.work, 1), s.strideC, body + ys, g.CW, g.CW, g.CH, cudaMemcpyHostToDevice, sr) ||
         cudaMemcpy2DAsync(s.plane(j.work, 2), s.strideC, body + ys + cs, g.CW, g.CW, g.CH, cudaMemcpyHostToDevice,
-                          stream_))
+                          sr))
       j.status = kErrDevice;
   }
   // ---- descriptors grouped by step: [main step 0][ov step 0][main step 1]... --
@@ -757,7 +775,7 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
     if (j.mainDesc < 0) continue;
     Stream& s = *streams_[(size_t)j.stream];
     const int gate = j.gateDesc >= 0 ? jobs[(size_t)j.gateDesc].mainDesc : -1;
-    const int ovSlot = P * (lookahead_ + 1) + lookahead_;
+    const int ovSlot = slotSet(P) * (lookahead_ + 1) + lookahead_;
     fill(j, j.main, j.mainDesc, j.work, j.ref, j.golden, j.fh.coding == kCodingInter, gate, s.slots[(size_t)j.slot]);
     if (!s.resident) std::memcpy(h + oPkt + j.stageOff, j.hPkt, j.n);
     if (j.ovDesc >= 0) fill(j, j.ov, j.ovDesc, j.ovBuf, j.work, j.work, true, j.mainDesc, s.slots[(size_t)ovSlot]);
@@ -786,12 +804,14 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
   launches_++;
   cudaEventRecord(ev_[P][1], se);  // entropy done: the reconstruction waits on it
   R.launched = true;
+  planStream_ = nullptr;
   return kOK;
 }
 
 int Engine::launchRecon(Round& R) {
   if (!R.launched) return kOK;
   const int P = R.parity;
+  cudaStream_t sr = reconStream(P);
   uint8_t* h = hStage_[P];
   uint8_t* d = dStage_[P];
   // Frames of streams rolled back since planning: point their gate at a word
@@ -804,31 +824,31 @@ int Engine::launchRecon(Round& R) {
       FrameDesc* hd = reinterpret_cast<FrameDesc*>(h + R.oDesc) + di;
       hd->gate = dOne_;
       FrameDesc* ddi = reinterpret_cast<FrameDesc*>(d + R.oDesc) + di;
-      if (cudaMemcpyAsync(&ddi->gate, &hd->gate, sizeof(hd->gate), cudaMemcpyHostToDevice, stream_) != cudaSuccess)
+      if (cudaMemcpyAsync(&ddi->gate, &hd->gate, sizeof(hd->gate), cudaMemcpyHostToDevice, sr) != cudaSuccess)
         return -1;
     }
   }
-  if (cudaStreamWaitEvent(stream_, ev_[P][1], 0) != cudaSuccess) return -1;
+  if (cudaStreamWaitEvent(sr, ev_[P][1], 0) != cudaSuccess) return -1;
   const FrameDesc* dd = reinterpret_cast<const FrameDesc*>(d + R.oDesc);
   const int2* dj = reinterpret_cast<const int2*>(d + R.oJobs);
-  if (timing_) cudaEventRecord(ev_[P][2], stream_);
+  if (timing_) cudaEventRecord(ev_[P][2], sr);
   for (const StepInfo& si : R.steps) {
     if (si.maxInterMBs > 0) {
-      launchInter(dd + si.mainFirst, si.mainCount, si.maxInterMBs, stream_);
+      launchInter(dd + si.mainFirst, si.mainCount, si.maxInterMBs, sr);
       launches_++;
     }
     if (si.jobCount > 0) {
-      launchIntra(dd, dj + si.jobFirst, si.jobCount, stream_);
+      launchIntra(dd, dj + si.jobFirst, si.jobCount, sr);
       launches_++;
     }
     if (si.ovCount > 0) {
-      launchInter(dd + si.ovFirst, si.ovCount, si.maxOvMBs, stream_);
-      launchIntra(dd, dj + si.ovJobFirst, si.ovJobCount, stream_);
+      launchInter(dd + si.ovFirst, si.ovCount, si.maxOvMBs, sr);
+      launchIntra(dd, dj + si.ovJobFirst, si.ovJobCount, sr);
       launches_ += 2;
     }
   }
-  if (timing_) cudaEventRecord(ev_[P][3], stream_);
-  if (cudaMemcpyAsync(hStatus_[P], d + R.oStat, sizeof(int32_t) * R.nDesc, cudaMemcpyDeviceToHost, stream_) !=
+  if (timing_) cudaEventRecord(ev_[P][3], sr);
+  if (cudaMemcpyAsync(hStatus_[P], d + R.oStat, sizeof(int32_t) * R.nDesc, cudaMemcpyDeviceToHost, sr) !=
       cudaSuccess)
     return -1;
   return kOK;
@@ -838,7 +858,7 @@ int Engine::collectRound(Round& R, std::vector<RoundResult>* results) {
   const int P = R.parity;
   const bool gpu = R.nDesc > 0;
   std::vector<int32_t> statuses((size_t)std::max(R.nDesc, 1), 0);
-  if (cudaStreamSynchronize(stream_) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+  if (cudaStreamSynchronize(reconStream(P)) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
     for (Job& j : R.jobs)
       if (j.status == kOK) j.status = kErrDevice;
   } else if (gpu) {
@@ -859,6 +879,7 @@ int Engine::collectRound(Round& R, std::vector<RoundResult>* results) {
     if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) continue;  // removed meanwhile
     Stream& s = *streams_[(size_t)id];
     s.roundBufs[P].clear();
+    if (P == kSide) s.inSide = false;
     if (R.jobs[(size_t)chain[0]].epoch != s.epoch) continue;  // planned before a rollback: discarded
     // A newer round of this stream was planned on top of this chain's
     // outcome; commit this chain as if it were the newest.
@@ -929,6 +950,39 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
     return -1;
   }
   inflight_ = p;
+  return n;
+}
+
+int Engine::enableSideLane() {
+  for (auto& s : streams_)
+    if (s) return kErrArg;  // pool and slot counts depend on it
+  if (!streamES_ && cudaStreamCreateWithFlags(&streamES_, cudaStreamNonBlocking) != cudaSuccess) return kErrDevice;
+  if (!streamRS_ && cudaStreamCreateWithFlags(&streamRS_, cudaStreamNonBlocking) != cudaSuccess) return kErrDevice;
+  if (!sideDone_ && cudaEventCreateWithFlags(&sideDone_, cudaEventDisableTiming) != cudaSuccess) return kErrDevice;
+  side_ = true;
+  return kOK;
+}
+
+int Engine::launchSide(const std::vector<int>& ids, const std::vector<int>* maxFrames) {
+  if (!side_ || sideInflight_) return kErrArg;
+  Round& R = rounds_[kSide];
+  R.parity = kSide;
+  if (planRound(ids, maxFrames, R) || launchRecon(R)) {
+    for (Job& j : R.jobs)
+      if (j.status == kOK) j.status = kErrDevice;
+    R.nDesc = 0;
+  }
+  if (cudaEventRecord(sideDone_, streamRS_) != cudaSuccess) return kErrDevice;
+  sideInflight_ = true;
+  return kOK;
+}
+
+bool Engine::sideReady() { return sideInflight_ && cudaEventQuery(sideDone_) != cudaErrorNotReady; }
+
+int Engine::collectSide(std::vector<RoundResult>* results) {
+  if (!sideInflight_) return 0;
+  const int n = collectRound(rounds_[kSide], results);
+  sideInflight_ = false;
   return n;
 }
 

@@ -84,6 +84,16 @@ class Engine {
   int setPipelined(bool on);
   bool pipelined() const { return pipelined_; }
   int drain(std::vector<RoundResult>* results);
+  // Side lane (set before adding streams): a round for a few streams (the
+  // serving loop sends key frames there) that runs on its own pair of CUDA
+  // streams next to the main rounds and is collected when it is done.  A
+  // stream in the side lane is left out of main rounds until collected; the
+  // caller sends a stream to it only between its main rounds.
+  int enableSideLane();
+  int launchSide(const std::vector<int>& ids, const std::vector<int>* maxFrames);
+  bool sideBusy() const { return sideInflight_; }
+  bool sideReady();  // the side round's work is complete
+  int collectSide(std::vector<RoundResult>* results);
 
   int downloadFrame(const EngineFrameView& v, uint8_t* packed, size_t cap);
   // Queues the copy on the engine's stream; complete after the stream syncs.
@@ -96,8 +106,8 @@ class Engine {
   int64_t launches() const { return launches_; }
   size_t deviceBytes() const { return deviceBytes_; }
   // Per-stream HBM footprint (pool + scratch) for a geometry.
-  static size_t footprint(int w, int h, int ring, int lookahead, bool pipelined = false);
-  static int poolSize(int ring, int lookahead, bool pipelined);
+  static size_t footprint(int w, int h, int ring, int lookahead, bool pipelined = false, bool side = false);
+  static int poolSize(int ring, int lookahead, bool pipelined, bool side = false);
 
   // Kernel-time accounting: CUDA events recorded around each round's
   // kernels on the engine's stream.
@@ -120,27 +130,38 @@ class Engine {
   int planRound(const std::vector<int>& ids, const std::vector<int>* maxFrames, Round& r);
   int launchRecon(Round& r);
   int collectRound(Round& r, std::vector<RoundResult>* results);
-  cudaStream_t entropyStream() const { return pipelined_ ? streamE_ : stream_; }
+  // Streams of a round by parity: 0/1 main (pipelined rounds alternate), 2 side.
+  cudaStream_t entropyStream(int parity = 0) const {
+    return parity == kSide ? streamES_ : (pipelined_ ? streamE_ : stream_);
+  }
+  cudaStream_t reconStream(int parity = 0) const { return parity == kSide ? streamRS_ : stream_; }
+  int slotSet(int parity) const { return parity == kSide ? (pipelined_ ? 2 : 1) : parity; }
+  int slotSets() const { return (pipelined_ ? 2 : 1) + (side_ ? 1 : 0); }
+  static constexpr int kSide = 2;
+  static constexpr int kParities = 3;
 
   cudaStream_t stream_ = nullptr;   // reconstruction, copies, status read-back
   cudaStream_t streamE_ = nullptr;  // entropy stage of pipelined rounds
+  cudaStream_t streamES_ = nullptr, streamRS_ = nullptr;  // side lane: entropy, reconstruction
+  cudaStream_t planStream_ = nullptr;  // reconstruction stream of the round being planned
+  cudaEvent_t sideDone_ = nullptr;
   bool ownStream_ = false, ownStreamE_ = false;
-  bool pipelined_ = false;
+  bool pipelined_ = false, side_ = false, sideInflight_ = false;
   std::vector<std::unique_ptr<Stream>> streams_;
   std::unique_ptr<Round[]> rounds_;  // by parity
   int inflight_ = -1;  // parity of the round whose reconstruction is in flight
   int64_t roundSeq_ = 0;
-  uint8_t* dStage_[2] = {nullptr, nullptr};
-  uint8_t* hStage_[2] = {nullptr, nullptr};
-  size_t stageCap_[2] = {0, 0};
-  int32_t* hStatus_[2] = {nullptr, nullptr};
-  int statusCap_[2] = {0, 0};
+  uint8_t* dStage_[3] = {nullptr, nullptr, nullptr};
+  uint8_t* hStage_[3] = {nullptr, nullptr, nullptr};
+  size_t stageCap_[3] = {0, 0, 0};
+  int32_t* hStatus_[3] = {nullptr, nullptr, nullptr};
+  int statusCap_[3] = {0, 0, 0};
   int32_t* dOne_ = nullptr;  // constant 1: the gate of discarded frames
   int64_t launches_ = 0;
   int lookahead_ = 1;
   size_t deviceBytes_ = 0;
   bool timing_ = false;
-  cudaEvent_t ev_[2][4] = {};
+  cudaEvent_t ev_[3][4] = {};
   double kernelMs_ = 0, entropyMs_ = 0, reconMs_ = 0;
 };
 

@@ -54,6 +54,8 @@ struct ServeOptionsC {
   int maxFramesPerRound = 4;
   int ring = 3;
   int record = 0;
+  int keyLane = 1;  // key frames decode on the engine's side lane
+  double startSpread = 0;  // streams admitted at start begin at a uniform offset in [0, startSpread) s
 };
 
 struct ServeStatsC {
@@ -72,6 +74,7 @@ class Server {
     if (st) return st;
     st = eng_.init();
     if (st) return st;
+    if (opt_.keyLane && (st = eng_.enableSideLane())) return st;
     eng_.enableTiming(true);
     return kOK;
   }
@@ -92,7 +95,8 @@ class Server {
     }
     sp.fps = fps;
     sp.loop = loop;
-    sp.footprint = Engine::footprint(sp.w, sp.h, opt_.ring, std::max(1, opt_.maxFramesPerRound)) +
+    sp.footprint = Engine::footprint(sp.w, sp.h, opt_.ring, std::max(1, opt_.maxFramesPerRound), false,
+                                     opt_.keyLane != 0) +
                    [&] {
                      size_t b = 0;
                      for (auto& p : sp.pkts) b += (p.size() + 15) / 16 * 16;
@@ -106,6 +110,7 @@ class Server {
     std::deque<int> waiting;
     for (size_t i = 0; i < specs_.size(); i++) waiting.push_back((int)i);
     std::vector<int> admitted;  // spec indices
+    std::vector<int> specOf;    // engine stream id -> spec index
     uint64_t used = 0;
     ServeStatsC st;
     const double t0 = nowSec();
@@ -121,7 +126,11 @@ class Server {
           lens.push_back(p.size());
         }
         if (eng_.addResidentStream(ptrs.data(), lens.data(), (int)ptrs.size(), opt_.ring, &sp.engineId)) break;
+        if ((int)specOf.size() <= sp.engineId) specOf.resize((size_t)sp.engineId + 1, -1);
+        specOf[(size_t)sp.engineId] = si;
         sp.nextArrival = nowSec() - t0;
+        if (opt_.startSpread > 0 && st.rounds == 0)
+          sp.nextArrival += std::uniform_real_distribution<double>(0, opt_.startSpread)(rng_);
         sp.pos = 0;
         used += sp.footprint;
         admitted.push_back(si);
@@ -132,96 +141,10 @@ class Server {
     };
     admit();
     std::vector<double> lat;
-    for (;;) {
-      const double now = nowSec() - t0;
-      // Arrivals up to now.
-      for (int si : admitted) {
-        Spec& sp = specs_[(size_t)si];
-        while (sp.nextArrival <= now && sp.nextArrival <= opt_.duration && sp.issued < opt_.framesPerStream &&
-               !sp.done) {
-          Request r;
-          r.arrival = sp.nextArrival;
-          if (std::uniform_real_distribution<double>(0, 1)(rng_) < opt_.seekProb && !sp.keys.empty()) {
-            r.seekTo = sp.keys[std::uniform_int_distribution<size_t>(0, sp.keys.size() - 1)(rng_)];
-          }
-          sp.queue.push_back(r);
-          sp.issued++;
-          st.requests++;
-          sp.nextArrival += std::exponential_distribution<double>(sp.fps)(rng_);
-        }
-      }
-      // Build the round: each stream's run of plain requests at its head.
-      std::vector<int> ids, counts, owners;
-      for (int si : admitted) {
-        Spec& sp = specs_[(size_t)si];
-        if (sp.queue.empty()) continue;
-        Request& head = sp.queue.front();
-        if (head.seekTo >= 0) {
-          eng_.seekStream(sp.engineId, head.seekTo);
-          sp.pos = head.seekTo;
-          head.seekTo = -1;
-          st.seeks++;
-        }
-        if (sp.pos >= (int64_t)sp.pkts.size()) {
-          if (sp.loop) {
-            eng_.seekStream(sp.engineId, 0);
-            sp.pos = 0;
-            st.loops++;
-          } else {
-            // The clip ended: the remaining requests cannot be served.
-            sp.queue.clear();
-            continue;
-          }
-        }
-        int n = 0;
-        for (const Request& r : sp.queue) {
-          if (n > 0 && r.seekTo >= 0) break;
-          if (++n >= opt_.maxFramesPerRound) break;
-        }
-        n = std::min<int64_t>(n, (int64_t)sp.pkts.size() - sp.pos);
-        ids.push_back(sp.engineId);
-        counts.push_back(n);
-        owners.push_back(si);
-      }
-      if (ids.empty()) {
-        // Finished streams release their memory; admit waiting ones.
-        bool changed = false;
-        for (size_t k = 0; k < admitted.size();) {
-          Spec& sp = specs_[(size_t)admitted[k]];
-          const bool ended = sp.queue.empty() && (sp.issued >= opt_.framesPerStream || sp.nextArrival > opt_.duration ||
-                                                  (!sp.loop && sp.pos >= (int64_t)sp.pkts.size()));
-          if (ended) {
-            eng_.removeStream(sp.engineId);
-            used -= sp.footprint;
-            sp.done = true;
-            admitted.erase(admitted.begin() + (long)k);
-            changed = true;
-          } else {
-            k++;
-          }
-        }
-        if (changed) admit();
-        if (admitted.empty() && waiting.empty()) break;
-        if (now > opt_.duration && admitted.empty()) break;
-        double nextT = 1e30;
-        for (int si : admitted) nextT = std::min(nextT, specs_[(size_t)si].nextArrival);
-        if (nextT > opt_.duration + 1 && waiting.empty()) {
-          bool pending = false;
-          for (int si : admitted) pending |= !specs_[(size_t)si].queue.empty();
-          if (!pending) break;
-        }
-        const double wait = nextT - (nowSec() - t0);
-        if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.005)));
-        continue;
-      }
-      results_.clear();
-      eng_.roundFor(ids, &results_, &counts);
-      const double done = nowSec() - t0;
-      st.rounds++;
-      for (const RoundResult& r : results_) {
-        int si = -1;
-        for (size_t k = 0; k < ids.size(); k++)
-          if (ids[k] == r.stream) si = owners[k];
+    // Each result answers the head request of its stream.
+    auto deliver = [&](const std::vector<RoundResult>& rs, double done) {
+      for (const RoundResult& r : rs) {
+        const int si = r.stream >= 0 && r.stream < (int)specOf.size() ? specOf[(size_t)r.stream] : -1;
         if (si < 0) continue;
         Spec& sp = specs_[(size_t)si];
         if (sp.queue.empty()) continue;
@@ -242,6 +165,135 @@ class Server {
           hashes_.push_back({si, r.frameIndex, fnv1a(buf.data(), buf.size())});
         }
       }
+    };
+    // Applies the head request's seek and the clip end (loop, or drop the
+    // requests of a finished clip); false when there is nothing to decode.
+    auto prepareHead = [&](Spec& sp) -> bool {
+      if (sp.queue.empty()) return false;
+      Request& head = sp.queue.front();
+      if (head.seekTo >= 0) {
+        eng_.seekStream(sp.engineId, head.seekTo);
+        sp.pos = head.seekTo;
+        head.seekTo = -1;
+        st.seeks++;
+      }
+      if (sp.pos >= (int64_t)sp.pkts.size()) {
+        if (!sp.loop) {
+          sp.queue.clear();  // the clip ended: the remaining requests cannot be served
+          return false;
+        }
+        eng_.seekStream(sp.engineId, 0);
+        sp.pos = 0;
+        st.loops++;
+      }
+      return true;
+    };
+    auto isKey = [](const Spec& sp, int64_t i) { return std::binary_search(sp.keys.begin(), sp.keys.end(), i); };
+    std::vector<RoundResult> res;
+    std::vector<int> sideSpecs;
+    for (;;) {
+      const double now = nowSec() - t0;
+      // Arrivals up to now.
+      for (int si : admitted) {
+        Spec& sp = specs_[(size_t)si];
+        while (sp.nextArrival <= now && sp.nextArrival <= opt_.duration && sp.issued < opt_.framesPerStream &&
+               !sp.done) {
+          Request r;
+          r.arrival = sp.nextArrival;
+          if (std::uniform_real_distribution<double>(0, 1)(rng_) < opt_.seekProb && !sp.keys.empty()) {
+            r.seekTo = sp.keys[std::uniform_int_distribution<size_t>(0, sp.keys.size() - 1)(rng_)];
+          }
+          sp.queue.push_back(r);
+          sp.issued++;
+          st.requests++;
+          sp.nextArrival += std::exponential_distribution<double>(sp.fps)(rng_);
+        }
+      }
+      // Key lane: collect a finished side round, then send every stream whose
+      // next frame is a key frame (start, seek, loop, GOP boundary) to it, so
+      // no main round waits for a key frame's long entropy chains.
+      if (opt_.keyLane && eng_.sideBusy() && eng_.sideReady()) {
+        res.clear();
+        eng_.collectSide(&res);
+        deliver(res, nowSec() - t0);
+        for (int si : sideSpecs) specs_[(size_t)si].inSide = false;
+        sideSpecs.clear();
+        st.rounds++;
+      }
+      if (opt_.keyLane && !eng_.sideBusy()) {
+        std::vector<int> kids, kcap;
+        for (int si : admitted) {
+          Spec& sp = specs_[(size_t)si];
+          if (sp.inSide || !prepareHead(sp) || !isKey(sp, sp.pos)) continue;
+          kids.push_back(sp.engineId);
+          kcap.push_back(1);
+          sideSpecs.push_back(si);
+          sp.inSide = true;
+        }
+        if (!kids.empty() && eng_.launchSide(kids, &kcap)) return kErrDevice;
+      }
+      // Main round: each stream's run of plain requests at its queue head,
+      // ending before a seek and (with the key lane) before a key frame.
+      std::vector<int> ids, counts;
+      for (int si : admitted) {
+        Spec& sp = specs_[(size_t)si];
+        if (sp.inSide || !prepareHead(sp)) continue;
+        if (opt_.keyLane && isKey(sp, sp.pos)) continue;  // waits for the key lane
+        int n = 0;
+        for (const Request& r : sp.queue) {
+          if (n > 0 && r.seekTo >= 0) break;
+          if (++n >= opt_.maxFramesPerRound) break;
+        }
+        n = (int)std::min<int64_t>(n, (int64_t)sp.pkts.size() - sp.pos);
+        if (opt_.keyLane) {
+          const auto nk = std::upper_bound(sp.keys.begin(), sp.keys.end(), sp.pos);
+          if (nk != sp.keys.end()) n = (int)std::min<int64_t>(n, *nk - sp.pos);
+        }
+        ids.push_back(sp.engineId);
+        counts.push_back(n);
+      }
+      if (ids.empty()) {
+        // Finished streams release their memory; admit waiting ones.
+        bool changed = false;
+        for (size_t k = 0; k < admitted.size();) {
+          Spec& sp = specs_[(size_t)admitted[k]];
+          const bool ended = !sp.inSide && sp.queue.empty() &&
+                             (sp.issued >= opt_.framesPerStream || sp.nextArrival > opt_.duration ||
+                              (!sp.loop && sp.pos >= (int64_t)sp.pkts.size()));
+          if (ended) {
+            eng_.removeStream(sp.engineId);
+            used -= sp.footprint;
+            sp.done = true;
+            admitted.erase(admitted.begin() + (long)k);
+            changed = true;
+          } else {
+            k++;
+          }
+        }
+        if (changed) admit();
+        if (admitted.empty() && waiting.empty()) break;
+        if (now > opt_.duration && admitted.empty()) break;
+        double nextT = 1e30;
+        for (int si : admitted) nextT = std::min(nextT, specs_[(size_t)si].nextArrival);
+        if (nextT > opt_.duration + 1 && waiting.empty() && !eng_.sideBusy()) {
+          bool pending = false;
+          for (int si : admitted) pending |= !specs_[(size_t)si].queue.empty();
+          if (!pending) break;
+        }
+        double wait = nextT - (nowSec() - t0);
+        if (eng_.sideBusy()) wait = std::min(wait, 0.0002);  // poll the key lane
+        if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.005)));
+        continue;
+      }
+      res.clear();
+      eng_.roundFor(ids, &res, &counts);
+      st.rounds++;
+      deliver(res, nowSec() - t0);
+    }
+    if (eng_.sideBusy()) {
+      res.clear();
+      eng_.collectSide(&res);
+      deliver(res, nowSec() - t0);
     }
     st.elapsed = nowSec() - t0;
     st.waitingAtEnd = (int64_t)waiting.size();
@@ -288,6 +340,7 @@ class Server {
     int64_t issued = 0;
     int64_t pos = 0;
     bool done = false;
+    bool inSide = false;  // its key frame is on the side lane
     std::deque<Request> queue;
   };
   ServeOptionsC opt_;
@@ -323,6 +376,8 @@ int ebivgpu_server_create(const ebivgpu_serve_options* o, ebivgpu_server** out) 
   c.maxFramesPerRound = o->max_frames_per_round > 0 ? o->max_frames_per_round : 1;
   c.ring = o->ring >= 2 ? o->ring : 3;
   c.record = o->record;
+  c.keyLane = o->key_lane;
+  c.startSpread = o->start_spread_s > 0 ? o->start_spread_s : 0;
   ebivgpu_server* h = new (std::nothrow) ebivgpu_server();
   if (!h) return kErrDevice;
   h->s.reset(new Server(c));

@@ -156,6 +156,8 @@ typedef struct {
   int32_t max_frames_per_round;/* per stream, when it fell behind */
   int32_t ring;
   int32_t record;              /* hash every delivered frame (testing) */
+  int32_t key_lane;            /* key frames decode on a side lane beside the main rounds (1 = on) */
+  double start_spread_s;       /* streams admitted at start begin uniformly within this many seconds */
 } ebivgpu_serve_options;
 typedef struct {
   int64_t requests, frames, errors, seeks, loops, rounds;
