@@ -12,7 +12,7 @@
 
 namespace ebiv {
 
-void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, cudaStream_t s);
+void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* next, cudaStream_t s);
 void launchInter(const FrameDesc* frames, int nframes, int maxMBs, cudaStream_t s);
 void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, cudaStream_t s);
 
@@ -706,7 +706,8 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
   const size_t oTiles = al(oTab + sizeof(DeviceTables) * nDesc, 64);
   R.oJobs = al(oTiles + sizeof(TileRange) * (size_t)nTiles, 64);
   R.oEJobs = al(R.oJobs + sizeof(int2) * (size_t)nTiles, 64);
-  const size_t oPkt = al(R.oEJobs + sizeof(int4) * (size_t)nEJobs, 256);
+  const size_t oQueue = al(R.oEJobs + sizeof(int4) * (size_t)nEJobs, 64);  // entropy job counter
+  const size_t oPkt = al(oQueue + 64, 256);
   const size_t total = oPkt + streamedBytes;
   if (ensureStage(P, total) || ensureStatus(P, nDesc)) return -1;
   uint8_t* h = hStage_[P];
@@ -796,11 +797,12 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
                                               const std::pair<uint32_t, int4>& b) { return a.first > b.first; });
     int4* he = reinterpret_cast<int4*>(h + R.oEJobs);
     for (size_t k = 0; k < ej.size(); k++) he[k] = ej[k].second;
+    *reinterpret_cast<int32_t*>(h + oQueue) = 0;
   }
   if (cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, se) != cudaSuccess) return -1;
   const FrameDesc* dd = reinterpret_cast<const FrameDesc*>(d + R.oDesc);
   if (timing_) cudaEventRecord(ev_[P][0], se);
-  launchEntropy(dd, reinterpret_cast<const int4*>(d + R.oEJobs), nEJobs, se);
+  launchEntropy(dd, reinterpret_cast<const int4*>(d + R.oEJobs), nEJobs, reinterpret_cast<int32_t*>(d + oQueue), se);
   launches_++;
   cudaEventRecord(ev_[P][1], se);  // entropy done: the reconstruction waits on it
   R.launched = true;

@@ -22,6 +22,7 @@
 // spins on memory written by another CTA.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 
 #include "gpu_types.h"
@@ -436,18 +437,9 @@ __device__ __forceinline__ uint32_t writeMask(const BlockPlan& p, int done) {
 
 constexpr int kEntropyWarps = kEntropyTilesPerJob;
 
-// One CTA per entropy job: up to kEntropyWarps tiles of one frame, one warp
-// per tile, sharing the frame's symbol tables.
-__global__ void __launch_bounds__(32 * kEntropyWarps, 4) kEntropy(const FrameDesc* frames, const int4* jobs, int njobs) {
-  __shared__ EntropyTables sT;
-  __shared__ WarpRows sR[kEntropyWarps];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (blockIdx.x >= njobs) return;
-  const int4 job = jobs[blockIdx.x];
-  const FrameDesc* fp = frames + job.x;
-  buildTables(sT, *fp->tables, threadIdx.x, blockDim.x);
-  if (warp >= job.z) return;  // no barrier follows
-  const int tile = job.y + warp;
+// One tile's chain, by one warp (the frame's tables are in sT).
+__device__ __forceinline__ void entropyTile(const FrameDesc* fp, int tile, const EntropyTables& sT, WarpRows& rows,
+                                            int lane) {
   // Descriptor fields into registers: the kernel's global stores cannot alias them then.
   const int mbCols = fp->mbCols;
   const int inter = fp->inter;
@@ -461,7 +453,6 @@ __global__ void __launch_bounds__(32 * kEntropyWarps, 4) kEntropy(const FrameDes
   const bool wide = (x1 - x0) > kRowMax;
   uint32_t* const gmv = reinterpret_cast<uint32_t*>(fp->mvgrid);
   int16_t* const glv = fp->lvgrid;
-  WarpRows& rows = sR[warp];
 
   Chain d;
   d.buf = fp->pkt + tr.offset;
@@ -583,6 +574,31 @@ __global__ void __launch_bounds__(32 * kEntropyWarps, 4) kEntropy(const FrameDes
     ts.pad = 0;
     tstat[tile] = ts;
     if (d.err) atomicExch(status, kErrCorrupt);
+  }
+}
+
+// Entropy jobs: up to kEntropyWarps tiles of one frame per job, one warp per
+// tile, sharing the frame's symbol tables.  With a queue counter the grid is
+// persistent: each CTA takes jobs (longest first, as listed) until none are
+// left, so a round with more jobs than resident CTAs has no second-wave tail;
+// without one, CTA b runs job b.
+__global__ void __launch_bounds__(32 * kEntropyWarps, 4) kEntropy(const FrameDesc* frames, const int4* jobs, int njobs,
+                                                                   int* next) {
+  __shared__ EntropyTables sT;
+  __shared__ WarpRows sR[kEntropyWarps];
+  __shared__ int sJob;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (;;) {
+    if (threadIdx.x == 0) sJob = next ? atomicAdd(next, 1) : (int)blockIdx.x;
+    __syncthreads();
+    const int jb = sJob;
+    if (jb >= njobs) return;  // the same for the whole CTA
+    const int4 job = jobs[jb];
+    const FrameDesc* fp = frames + job.x;
+    buildTables(sT, *fp->tables, threadIdx.x, blockDim.x);
+    if (warp < job.z) entropyTile(fp, job.y + warp, sT, sR[warp], lane);
+    if (!next) return;
+    __syncthreads();  // every warp is done with sT and sJob before the next job
   }
 }
 
@@ -1164,9 +1180,24 @@ int uploadCodingTables(const int* scan4, const int* scan8, const int* scan16, co
   return kOK;
 }
 
-void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, cudaStream_t s) {
+// next: a zeroed device counter for the persistent grid (sized to the CTAs
+// the device holds at once), or null for one CTA per job.
+void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* next, cudaStream_t s) {
   if (njobs <= 0) return;
-  dev::kEntropy<<<njobs, 32 * dev::kEntropyWarps, 0, s>>>(frames, jobs, njobs);
+  static int resident[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int grid = njobs;
+  if (next && dev >= 0 && dev < 64) {
+    if (!resident[dev]) {
+      int perSM = 0, sms = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, dev::kEntropy, 32 * dev::kEntropyWarps, 0);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      resident[dev] = std::max(1, perSM * sms);
+    }
+    grid = std::min(njobs, resident[dev]);
+  }
+  dev::kEntropy<<<grid, 32 * dev::kEntropyWarps, 0, s>>>(frames, jobs, njobs, next);
 }
 
 void launchInter(const FrameDesc* frames, int nframes, int maxMBs, cudaStream_t s) {
