@@ -846,17 +846,40 @@ __global__ void __launch_bounds__(32 * kInterWarps) kInterRecon(const FrameDesc*
     const int fx = mvx & 3, fy = mvy & 3;
     const int sx = mbx * 16 + c0 + (mvx >> 2), sy = mby * 16 + row + (mvy >> 2);
     int pred[8];
+    if (fx == 0 && fy == 0 && sx >= 0 && sy >= 0 && sy < v.padH && sx + 8 <= v.padW && (sx & ~7) + 16 <= v.strideY) {
+      // Whole-pel vector with the row segment inside the plane: the samples
+      // need no clamping; two aligned 8-byte loads cover them (rows start
+      // 64-byte aligned and the loads stay inside the row's stride).
+      const uint8_t* rowp = refp[0] + (size_t)sy * v.strideY;
+      const int base = sx & ~7, sh = (sx & 7) * 8;
+      uint64_t w = __ldg(reinterpret_cast<const unsigned long long*>(rowp + base));
+      if (sh) w = (w >> sh) | ((uint64_t)__ldg(reinterpret_cast<const unsigned long long*>(rowp + base + 8)) << (64 - sh));
 #pragma unroll
-    for (int k = 0; k < 8; k++) pred[k] = lumaSample(refp[0], v.strideY, v.padW, v.padH, sx + k, sy, fx, fy);
+      for (int k = 0; k < 8; k++) pred[k] = (int)((w >> (8 * k)) & 0xFF);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; k++) pred[k] = lumaSample(refp[0], v.strideY, v.padW, v.padH, sx + k, sy, fx, fy);
+    }
     const int n = 4 << tx, per = 4 >> tx;
     uint8_t* out = v.rec[0] + (size_t)(mby * 16 + row) * v.strideY + mbx * 16 + c0;
+    const int blkA = (row / n) * per + c0 / n, blkB = (row / n) * per + (c0 + 7) / n;
+    if (((wm >> blkA) & 1) && ((wm >> blkB) & 1)) {
+      uint64_t o = 0;  // all eight samples are written: one 8-byte store (out is 8-byte aligned)
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-      const int c = c0 + k;
-      const int blk = (row / n) * per + c / n;
-      if (!((wm >> blk) & 1)) continue;
-      const int v = resMask ? clampByteD(wadd(pred[k], S.res[row * 16 + c])) : pred[k];
-      out[k] = (uint8_t)v;
+      for (int k = 0; k < 8; k++) {
+        const int val = resMask ? clampByteD(wadd(pred[k], S.res[row * 16 + c0 + k])) : pred[k];
+        o |= (uint64_t)(uint32_t)val << (8 * k);
+      }
+      *reinterpret_cast<unsigned long long*>(out) = o;
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const int c = c0 + k;
+        const int blk = (row / n) * per + c / n;
+        if (!((wm >> blk) & 1)) continue;
+        const int val = resMask ? clampByteD(wadd(pred[k], S.res[row * 16 + c])) : pred[k];
+        out[k] = (uint8_t)val;
+      }
     }
   }
   // Chroma: lane -> row lane/4, 2 columns; Cb then Cr.
