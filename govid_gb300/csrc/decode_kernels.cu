@@ -803,7 +803,18 @@ struct InterScratch {
   int32_t tmp[384];
 };
 
+// Reconstruction kernels are launched with programmatic stream
+// serialisation, so a grid may start while the previous kernel of the stream
+// finishes; this wait (a no-op without a prerequisite grid) holds every
+// thread until that kernel's results are complete and visible.
+__device__ __forceinline__ void waitPreviousGrid() {
+#ifdef __CUDA_ARCH__
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+
 __global__ void __launch_bounds__(32 * kInterWarps) kInterRecon(const FrameDesc* frames) {
+  waitPreviousGrid();
   __shared__ InterScratch sS[kInterWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const FrameDesc& f = frames[blockIdx.y];
@@ -1101,6 +1112,7 @@ constexpr int kLevelBuckets = 1024;  // tiles with more intra levels take the sc
 // frames get the classic wavefront (level = x + 2y); inter frames with a few
 // isolated intra macroblocks take one or two levels.
 __global__ void __launch_bounds__(32 * kIntraWarps, 1) kIntraRecon(const FrameDesc* frames, const int2* jobs, int njobs) {
+  waitPreviousGrid();
   __shared__ IntraScratch sS[kIntraWarps];
   __shared__ int sStart[kLevelBuckets + 1];
   __shared__ int sCur[kLevelBuckets];
@@ -1223,15 +1235,31 @@ void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* ne
   dev::kEntropy<<<grid, 32 * dev::kEntropyWarps, 0, s>>>(frames, jobs, njobs, next);
 }
 
+// The reconstruction launches overlap their start with the previous kernel
+// of the stream (programmatic dependent launch; the kernels wait for it).
+template <class... A>
+static void launchDependent(void (*k)(A...), dim3 grid, dim3 block, cudaStream_t s, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 void launchInter(const FrameDesc* frames, int nframes, int maxMBs, cudaStream_t s) {
   if (nframes <= 0 || maxMBs <= 0) return;
   dim3 grid((maxMBs + dev::kInterWarps - 1) / dev::kInterWarps, nframes);
-  dev::kInterRecon<<<grid, 32 * dev::kInterWarps, 0, s>>>(frames);
+  launchDependent(dev::kInterRecon, grid, dim3(32 * dev::kInterWarps), s, frames);
 }
 
 void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, cudaStream_t s) {
   if (njobs <= 0) return;
-  dev::kIntraRecon<<<njobs, 32 * dev::kIntraWarps, 0, s>>>(frames, jobs, njobs);
+  launchDependent(dev::kIntraRecon, dim3(njobs), dim3(32 * dev::kIntraWarps), s, frames, jobs, njobs);
 }
 
 }  // namespace ebiv
