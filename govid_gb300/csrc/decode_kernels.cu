@@ -278,13 +278,15 @@ struct Nbr {
   bool cOK;
 };
 
-// predictMV — ebiv/mv.go:21-52 (neighbours within the tile)
+// predictMV — ebiv/mv.go:21-52 (neighbours within the tile).  The median of
+// three runs on both packed 16-bit components at once: median(a, b, c) =
+// max(min(a, b), min(max(a, b), c)); unavailable neighbours are zero.
 __device__ __forceinline__ uint32_t predictMV(const Nbr& n) {
   if (!n.aOK && !n.bOK && !n.cOK) return 0;
   if (n.aOK && !n.bOK && !n.cOK) return n.mvA;
   if (!n.aOK && n.bOK && !n.cOK) return n.mvB;
-  return packMV(median3((int16_t)mvX(n.mvA), (int16_t)mvX(n.mvB), (int16_t)mvX(n.mvC)),
-                median3((int16_t)mvY(n.mvA), (int16_t)mvY(n.mvB), (int16_t)mvY(n.mvC)));
+  const uint32_t lo = __vmins2(n.mvA, n.mvB), hi = __vmaxs2(n.mvA, n.mvB);
+  return __vmaxs2(lo, __vmins2(hi, n.mvC));
 }
 
 // The coded blocks of one macroblock in bitstream order: nLuma luma blocks
@@ -940,21 +942,24 @@ struct IntraScratch {
 // in the working area a (row stride as).
 __device__ __forceinline__ int32_t refValue(int i, int n, bool avAbove, bool avLeft, bool avAR, const uint8_t* a,
                                             int as, int x0, int y0) {
+  // Each entry is one sample of the area: the left column L(r) = (x0-1, y0+r)
+  // (rows past n-1 repeat row n-1), the top row Tp(j) = (x0+j, y0-1) (past
+  // n-1 without above-right: Tp(n-1)), the corner; a missing side is
+  // replaced by the other side's nearest sample, both missing by kDCPred.
   const int corner = 2 * n;
-  auto L = [&](int r) -> int32_t { return a[(y0 + r) * as + x0 - 1]; };
-  auto Tp = [&](int j) -> int32_t { return a[(y0 - 1) * as + x0 + j]; };
-  if (!avLeft && !avAbove) return kDCPred;
+  int ax, ay;
   if (i < corner) {
-    const int row = 2 * n - 1 - i;
-    return avLeft ? L(row < n ? row : n - 1) : Tp(0);
+    ax = avLeft ? x0 - 1 : x0;
+    ay = avLeft ? y0 + min(corner - 1 - i, n - 1) : y0 - 1;
+  } else if (i == corner) {
+    ax = avLeft ? x0 - 1 : x0;
+    ay = avAbove ? y0 - 1 : y0;
+  } else {
+    const int j = i - corner - 1;
+    ax = avAbove ? x0 + ((j < n || avAR) ? j : n - 1) : x0 - 1;
+    ay = avAbove ? y0 - 1 : y0;
   }
-  if (i == corner) {
-    if (avLeft && avAbove) return a[(y0 - 1) * as + x0 - 1];
-    return avLeft ? L(0) : Tp(0);
-  }
-  const int j = i - corner - 1;
-  if (avAbove) return (j < n || avAR) ? Tp(j) : Tp(n - 1);
-  return L(0);
+  return (avLeft || avAbove) ? (int32_t)a[ay * as + ax] : kDCPred;
 }
 
 // Predicts and reconstructs one n x n block (predictIntra,
