@@ -352,9 +352,8 @@ __device__ __forceinline__ void intraHeader(Chain& d, Rec& r, BlockPlan* p) {
 // Returns 0 when the macroblock is complete without blocks (*wOut holds its
 // write mask), 1 when the blocks of *p follow.  *mvOut is the vector
 // neighbours predict from.
-__device__ __forceinline__ int interHeader(Chain& d, Rec& r, const Nbr& n, BlockPlan* p, bool* intra,
+__device__ __forceinline__ int interHeader(Chain& d, Rec& r, const Nbr& n, int mode, BlockPlan* p, bool* intra,
                                            uint32_t* mvOut, uint32_t* wOut) {
-  const int mode = d.sym(ctxMBMode);
   *mvOut = 0;
   *wOut = 0;
   if (mode == mbSkip) {
@@ -515,6 +514,29 @@ __device__ __forceinline__ void entropyTile(const FrameDesc* fp, int tile, const
           n.mvB = mvUp[mbx];
           if (n.cOK) n.mvC = mvUp[n.arOK ? mbx + 1 : mbx - 1];
         }
+        int mode = 0;
+        if (inter) {
+          mode = d.sym(ctxMBMode);
+          if (mode == mbSkip) {
+            // Skip macroblock (most of an inter frame): predicted vector,
+            // fixed record, rows updated; nothing else to decode.
+            const uint32_t pv = predictMV(n);
+            if (lane < 3) {
+              const uint4 v = lane == 0 ? make_uint4(kRecSkip, 0u, pv, 0u)
+                                        : (lane == 1 ? make_uint4(0u, 0u, 0u, 0u) : make_uint4(0u, 0u, 0u, kWriteAll));
+              reinterpret_cast<uint4*>(recs + idx)[lane] = v;
+            }
+            if (lane == 0) {
+              mvCur[mbx] = pv;
+              lvCur[mbx] = (int16_t)-1;
+            }
+            mvLeft = pv;
+            lvLeft = -1;
+            done++;
+            if (d.err) break;
+            continue;
+          }
+        }
         uint32_t* coef = coefBase + (size_t)idx * kCoefPerMB;
         Rec r;
         r.clear();
@@ -523,7 +545,7 @@ __device__ __forceinline__ void entropyTile(const FrameDesc* fp, int tile, const
         BlockPlan p;
         int blocks;
         if (inter) {
-          blocks = interHeader(d, r, n, &p, &intra, &mv, &w);
+          blocks = interHeader(d, r, n, mode, &p, &intra, &mv, &w);
         } else {
           intraHeader(d, r, &p);
           blocks = d.err ? 0 : 1;
