@@ -1049,7 +1049,11 @@ __device__ void intraBlock(int32_t* ref, uint8_t* a, int as, int ax, int ay, uin
   __syncwarp();
 }
 
-__device__ void intraMB(const ReconView& f, IntraScratch& S, int mbx, int mby, int tx0, int tx1, int ty0, int lane) {
+// One part of an intra macroblock: part 0 its luma, part 1 its chroma.  The
+// two never read each other (chroma predicts from neighbouring chroma only),
+// so different warps take them.
+__device__ void intraMB(const ReconView& f, IntraScratch& S, int mbx, int mby, int tx0, int tx1, int ty0, int lane,
+                        int part) {
   const int idx = mby * f.mbCols + mbx;
   RecRegs r;
   r.load(f.mbrec + idx);
@@ -1065,25 +1069,41 @@ __device__ void intraMB(const ReconView& f, IntraScratch& S, int mbx, int mby, i
   // The residual was computed before the level loop (kIntraRecon) and
   // stored over the macroblock's coefficient region.
   const uint32_t resMask = nzm & wm;
-  if (resMask) {
-    const uint32_t* rg = f.coef + (size_t)idx * kCoefPerMB;
-    for (int q = lane; q < 384; q += 32) S.res[q] = (int32_t)rg[q];
-  }
-  // Working areas: the row above and the column to the left, where they
-  // lie inside the tile (nothing outside it is ever predicted from).
+  const uint32_t* rg = f.coef + (size_t)idx * kCoefPerMB;
   const bool up = mbTop > tileTop, left = mbLeft > tileLeft;
-  {
-    for (int i = lane; i < 33; i += 32) {
-      const int x = mbLeft - 1 + i;
-      if (up && x >= tileLeft && x < tileRight) S.areaY[i] = Y[(size_t)(mbTop - 1) * ys + x];
-    }
-    if (left && lane < 16) S.areaY[(1 + lane) * kAreaW] = Y[(size_t)(mbTop + lane) * ys + mbLeft - 1];
+  if (part == 1) {
+    // Chroma: residuals, working areas (row above and column to the left,
+    // inside the tile) and the two 8x8 blocks.
+    if (resMask >> 16)
+      for (int q = 256 + lane; q < 384; q += 32) S.res[q] = (int32_t)rg[q];
     const int cl = mbx * 8, ct = mby * 8;
     for (int pl = 0; pl < 2; pl++) {
       const uint8_t* C = f.rec[1 + pl];
       if (up && lane < 9 && (lane > 0 || left)) S.areaC[pl][lane] = C[(size_t)(ct - 1) * cs + cl - 1 + lane];
       if (left && lane < 8) S.areaC[pl][(1 + lane) * 16] = C[(size_t)(ct + lane) * cs + cl - 1];
     }
+    __syncwarp();
+    const int cmode = r.cmode();
+    for (int pl = 0; pl < 2; pl++) {
+      const uint32_t bit = 1u << (16 + pl);
+      if (!(wm & bit)) break;
+      const bool hasRes = (nzm & bit) != 0;
+      intraBlock(S.ref[0], S.areaC[pl], 16, 1, 1, f.rec[1 + pl], cs, mbx * 8, mby * 8, 8, cmode, up, left, false,
+                 hasRes ? S.res + 256 + pl * 64 : nullptr, 8, lane, 32, true);
+    }
+    return;
+  }
+  // Luma: residuals and working area (row above from one left of the
+  // macroblock to 31 right of its left edge, column to the left; inside the
+  // tile only: nothing outside it is ever predicted from).
+  if (resMask & 0xFFFFu)
+    for (int q = lane; q < 256; q += 32) S.res[q] = (int32_t)rg[q];
+  {
+    for (int i = lane; i < 33; i += 32) {
+      const int x = mbLeft - 1 + i;
+      if (up && x >= tileLeft && x < tileRight) S.areaY[i] = Y[(size_t)(mbTop - 1) * ys + x];
+    }
+    if (left && lane < 16) S.areaY[(1 + lane) * kAreaW] = Y[(size_t)(mbTop + lane) * ys + mbLeft - 1];
     __syncwarp();
   }
   // Luma blocks.  A block reads its left, above-left, above and above-right
@@ -1119,15 +1139,6 @@ __device__ void intraMB(const ReconView& f, IntraScratch& S, int mbx, int mby, i
       if (!((wm >> k) & 1)) break;
       block(k, lane, 32, true, 0);
     }
-  }
-  const int cx0 = mbx * 8, cy0 = mby * 8;
-  const int cmode = r.cmode();
-  for (int pl = 0; pl < 2; pl++) {
-    const uint32_t bit = 1u << (16 + pl);
-    if (!(wm & bit)) break;
-    const bool hasRes = (nzm & bit) != 0;
-    intraBlock(S.ref[0], S.areaC[pl], 16, 1, 1, f.rec[1 + pl], cs, cx0, cy0, 8, cmode, up, left, false,
-               hasRes ? S.res + 256 + pl * 64 : nullptr, 8, lane, 32, true);
   }
 }
 
@@ -1176,9 +1187,9 @@ __global__ void __launch_bounds__(32 * kIntraWarps, 1) kIntraRecon(const FrameDe
     __syncwarp();
   }
   __syncthreads();
-  auto runMB = [&](uint32_t e) {
+  auto runMB = [&](uint32_t e, int part) {
     const int idx = (int)(e & kIndexMask);
-    intraMB(view, sS[warp], idx % view.mbCols, idx / view.mbCols, tr.mbX0, tr.mbX1, tr.mbY0, lane);
+    intraMB(view, sS[warp], idx % view.mbCols, idx / view.mbCols, tr.mbX0, tr.mbX1, tr.mbY0, lane, part);
   };
   if (L <= kLevelBuckets) {
     for (int l = tid; l <= L; l += blockDim.x) sStart[l] = 0;
@@ -1209,15 +1220,15 @@ __global__ void __launch_bounds__(32 * kIntraWarps, 1) kIntraRecon(const FrameDe
       sorted[atomicAdd(&sCur[e >> kLevelShift], 1)] = e;
     }
     __syncthreads();
-    for (int l = 0; l < L; l++) {
-      for (int k = sStart[l] + warp; k < sStart[l + 1]; k += kIntraWarps) runMB(sorted[k]);
+    for (int l = 0; l < L; l++) {  // jobs: (macroblock, part) pairs of the level
+      for (int k = 2 * sStart[l] + warp; k < 2 * sStart[l + 1]; k += kIntraWarps) runMB(sorted[k >> 1], k & 1);
       __syncthreads();
     }
   } else {
     // Very wide or tall tiles: scan the list once per level.
     for (int l = 0; l < L; l++) {
-      for (int i = warp; i < n; i += kIntraWarps)
-        if ((int)(list[i] >> kLevelShift) == l) runMB(list[i]);
+      for (int i = warp; i < 2 * n; i += kIntraWarps)
+        if ((int)(list[i >> 1] >> kLevelShift) == l) runMB(list[i >> 1], i & 1);
       __syncthreads();
     }
   }
