@@ -13,8 +13,8 @@
 namespace ebiv {
 
 void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* next, cudaStream_t s);
-void launchInter(const FrameDesc* frames, int nframes, int maxMBs, cudaStream_t s);
-void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, cudaStream_t s);
+void launchInter(const FrameDesc* frames, int nframes, int maxMBs, int phase, cudaStream_t s);
+void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, cudaStream_t s);
 
 namespace {
 inline size_t al(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -29,8 +29,11 @@ struct Slot {
   int16_t* lv = nullptr;
   uint32_t* intra = nullptr;  // intra list, then the level-sorted copy
   TileStat* ts = nullptr;
+  // per macroblock: whether its inter prediction waits for the previous
+  // frame's intra stage; then two intra progress bytes (large tiles)
+  uint8_t* dep = nullptr;
   bool alloc(size_t mbs) {
-    return cudaMalloc(&rec, mbs * sizeof(MBRec)) == cudaSuccess &&
+    return cudaMalloc(&dep, 3 * mbs) == cudaSuccess && cudaMalloc(&rec, mbs * sizeof(MBRec)) == cudaSuccess &&
            cudaMalloc(&coef, mbs * kCoefPerMB * sizeof(uint32_t)) == cudaSuccess &&
            cudaMalloc(&mv, mbs * 2 * sizeof(int16_t)) == cudaSuccess &&
            cudaMalloc(&lv, mbs * sizeof(int16_t)) == cudaSuccess &&
@@ -38,6 +41,7 @@ struct Slot {
            cudaMalloc(&ts, mbs * sizeof(TileStat)) == cudaSuccess;
   }
   void release() {
+    cudaFree(dep);
     cudaFree(rec);
     cudaFree(coef);
     cudaFree(mv);
@@ -46,7 +50,7 @@ struct Slot {
     cudaFree(ts);
   }
   static size_t bytes(size_t mbs) {
-    return mbs * (sizeof(MBRec) + kCoefPerMB * 4 + 4 + 2 + 8 + sizeof(TileStat));
+    return mbs * (sizeof(MBRec) + kCoefPerMB * 4 + 4 + 2 + 8 + sizeof(TileStat) + 3);
   }
 };
 
@@ -125,7 +129,8 @@ struct Engine::Job {
 struct Engine::StepInfo {
   int mainFirst = 0, mainCount = 0, ovFirst = 0, ovCount = 0;
   int jobFirst = 0, jobCount = 0, ovJobFirst = 0, ovJobCount = 0;
-  int maxInterMBs = 0, maxOvMBs = 0;
+  int maxMBs = 0, maxOvMBs = 0;  // largest frame of the step (macroblocks)
+  bool hasPrev = false;  // a frame of the step follows a frame of the same round (two inter phases)
 };
 
 struct Engine::Round {
@@ -135,13 +140,16 @@ struct Engine::Round {
   std::vector<std::vector<int>> chains;  // per stream, indices into jobs in decode order
   std::vector<StepInfo> steps;
   int nDesc = 0, nTiles = 0, nEJobs = 0;
+  int maxTileMBs = 0;  // largest tile of the round's frames (macroblocks)
+  int groups = 1, stepsPerGroup = 1;  // entropy launches (groups of consecutive steps)
   size_t oDesc = 0, oStat = 0, oJobs = 0, oEJobs = 0;
   bool launched = false;  // entropy launched; statuses pending
   void clear() {
     jobs.clear();
     chains.clear();
     steps.clear();
-    nDesc = nTiles = nEJobs = 0;
+    nDesc = nTiles = nEJobs = maxTileMBs = 0;
+    groups = stepsPerGroup = 1;
     launched = false;
   }
 };
@@ -164,6 +172,25 @@ Engine::~Engine() {
   }
   if (dOne_) cudaFree(dOne_);
   if (sideDone_) cudaEventDestroy(sideDone_);
+  if (streamB_) {
+    cudaStreamSynchronize(streamB_);
+    cudaStreamDestroy(streamB_);
+  }
+  for (int p = 0; p < 2; p++)
+    for (int k = 0; k < kMaxSteps; k++) {
+      if (stepA_[p][k]) cudaEventDestroy(stepA_[p][k]);
+      if (stepB_[p][k]) cudaEventDestroy(stepB_[p][k]);
+    }
+  for (auto& sg : streamEG_)
+    if (sg) {
+      cudaStreamSynchronize(sg);
+      cudaStreamDestroy(sg);
+    }
+  for (int p = 0; p < 2; p++) {
+    if (evUp_[p]) cudaEventDestroy(evUp_[p]);
+    for (auto& e : evGroup_[p])
+      if (e) cudaEventDestroy(e);
+  }
   if (streamES_) cudaStreamDestroy(streamES_);
   if (streamRS_) cudaStreamDestroy(streamRS_);
   if (ownStreamE_ && streamE_) cudaStreamDestroy(streamE_);
@@ -180,6 +207,17 @@ int Engine::init(cudaStream_t s) {
   for (auto& row : ev_)
     for (auto& e : row)
       if (cudaEventCreate(&e) != cudaSuccess) return kErrDevice;
+  if (cudaStreamCreateWithFlags(&streamB_, cudaStreamNonBlocking) != cudaSuccess) return kErrDevice;
+  for (int p = 0; p < 2; p++) {
+    if (cudaEventCreateWithFlags(&evUp_[p], cudaEventDisableTiming) != cudaSuccess) return kErrDevice;
+    for (auto& e : evGroup_[p])
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return kErrDevice;
+  }
+  for (int p = 0; p < 2; p++)
+    for (int k = 0; k < kMaxSteps; k++)
+      if (cudaEventCreateWithFlags(&stepA_[p][k], cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&stepB_[p][k], cudaEventDisableTiming) != cudaSuccess)
+        return kErrDevice;
   int32_t one = 1;
   if (cudaMalloc(&dOne_, sizeof(int32_t)) != cudaSuccess ||
       cudaMemcpy(dOne_, &one, sizeof(one), cudaMemcpyHostToDevice) != cudaSuccess)
@@ -553,6 +591,8 @@ int Engine::setPipelined(bool on) {
     if (cudaStreamCreateWithFlags(&streamE_, cudaStreamNonBlocking) != cudaSuccess) return kErrDevice;
     ownStreamE_ = true;
   }
+  for (auto& sg : streamEG_)
+    if (on && !sg && cudaStreamCreateWithFlags(&sg, cudaStreamNonBlocking) != cudaSuccess) return kErrDevice;
   pipelined_ = on;
   return kOK;
 }
@@ -675,7 +715,9 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
       si.mainCount++;
       nTiles += (int)j.main.tiles.size();
       si.jobCount += (int)j.main.tiles.size();
-      if (j.fh.coding == kCodingInter) si.maxInterMBs = std::max(si.maxInterMBs, (int)streams_[(size_t)j.stream]->mbs);
+      si.maxMBs = std::max(si.maxMBs, (int)streams_[(size_t)j.stream]->mbs);
+      for (const TileRange& t : j.main.tiles)
+        R.maxTileMBs = std::max(R.maxTileMBs, (int)(t.mbX1 - t.mbX0) * (int)(t.mbY1 - t.mbY0));
     }
     si.ovFirst = nDesc;
     si.ovJobFirst = nTiles;
@@ -686,6 +728,8 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
       nTiles += (int)j.ov.tiles.size();
       si.ovJobCount += (int)j.ov.tiles.size();
       si.maxOvMBs = std::max(si.maxOvMBs, (int)streams_[(size_t)j.stream]->mbs);
+      for (const TileRange& t : j.ov.tiles)
+        R.maxTileMBs = std::max(R.maxTileMBs, (int)(t.mbX1 - t.mbX0) * (int)(t.mbY1 - t.mbY0));
     }
   }
   R.nDesc = nDesc;
@@ -700,14 +744,22 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
   int nEJobs = 0;
   for (int t : tilesOf) nEJobs += (t + kEntropyTilesPerJob - 1) / kEntropyTilesPerJob;
   R.nEJobs = nEJobs;
+  // Pipelined main rounds decode their steps' tiles in up to kEntropyGroups
+  // launches of consecutive steps on separate streams, so a step's
+  // reconstruction waits only for its own group: the long chains of a large
+  // frame late in the round do not hold back the steps before it.
+  const int nsteps = (int)R.steps.size();
+  R.groups = (P != kSide && pipelined_ && streamEG_[0] && nsteps > 1) ? std::min(kEntropyGroups, nsteps) : 1;
+  R.stepsPerGroup = (nsteps + R.groups - 1) / R.groups;
+  R.groups = (nsteps + R.stepsPerGroup - 1) / R.stepsPerGroup;
   R.oDesc = 0;
   R.oStat = al(R.oDesc + sizeof(FrameDesc) * nDesc, 64);
   const size_t oTab = al(R.oStat + sizeof(int32_t) * nDesc, 64);
   const size_t oTiles = al(oTab + sizeof(DeviceTables) * nDesc, 64);
   R.oJobs = al(oTiles + sizeof(TileRange) * (size_t)nTiles, 64);
   R.oEJobs = al(R.oJobs + sizeof(int2) * (size_t)nTiles, 64);
-  const size_t oQueue = al(R.oEJobs + sizeof(int4) * (size_t)nEJobs, 64);  // entropy job counter
-  const size_t oPkt = al(oQueue + 64, 256);
+  const size_t oQueue = al(R.oEJobs + sizeof(int4) * (size_t)nEJobs, 64);  // entropy job counters, 64 B apart
+  const size_t oPkt = al(oQueue + 64 * (size_t)R.groups, 256);
   const size_t total = oPkt + streamedBytes;
   if (ensureStage(P, total) || ensureStatus(P, nDesc)) return -1;
   uint8_t* h = hStage_[P];
@@ -729,7 +781,7 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
   }
   std::vector<const PayloadPlan*> planOf((size_t)nDesc, nullptr);
   auto fill = [&](const Job& j, const PayloadPlan& plan, int di, int rec, int ref, int gold, bool inter, int gateDesc,
-                  const Slot& sl) {
+                  const Slot& sl, const Job* prev) {
     const Stream& s = *streams_[(size_t)j.stream];
     FrameDesc& fd = hd[di];
     std::memset(&fd, 0, sizeof(fd));
@@ -764,6 +816,14 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
     fd.tileStat = sl.ts;
     fd.status = reinterpret_cast<int32_t*>(d + R.oStat) + di;
     fd.gate = gateDesc >= 0 ? reinterpret_cast<const int32_t*>(d + R.oStat) + gateDesc : nullptr;
+    fd.dep = sl.dep;
+    fd.prevRec = nullptr;
+    fd.prevKey = 0;
+    if (prev) {  // the previous frame of the chain, reconstructed one step earlier in this round
+      const Stream& ps = *streams_[(size_t)prev->stream];
+      fd.prevRec = ps.slots[(size_t)prev->slot].rec;
+      fd.prevKey = prev->fh.type == kFrameKey ? 1 : 0;
+    }
     hs[di] = 0;
     ht[di] = plan.tables;
     for (size_t t = 0; t < plan.tiles.size(); t++) {
@@ -777,34 +837,71 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
     Stream& s = *streams_[(size_t)j.stream];
     const int gate = j.gateDesc >= 0 ? jobs[(size_t)j.gateDesc].mainDesc : -1;
     const int ovSlot = slotSet(P) * (lookahead_ + 1) + lookahead_;
-    fill(j, j.main, j.mainDesc, j.work, j.ref, j.golden, j.fh.coding == kCodingInter, gate, s.slots[(size_t)j.slot]);
+    const Job* prev = j.gateDesc >= 0 ? &jobs[(size_t)j.gateDesc] : nullptr;
+    fill(j, j.main, j.mainDesc, j.work, j.ref, j.golden, j.fh.coding == kCodingInter, gate, s.slots[(size_t)j.slot],
+         prev);
+    if (prev && j.fh.coding == kCodingInter) R.steps[(size_t)j.step].hasPrev = true;
     if (!s.resident) std::memcpy(h + oPkt + j.stageOff, j.hPkt, j.n);
-    if (j.ovDesc >= 0) fill(j, j.ov, j.ovDesc, j.ovBuf, j.work, j.work, true, j.mainDesc, s.slots[(size_t)ovSlot]);
+    if (j.ovDesc >= 0)
+      fill(j, j.ov, j.ovDesc, j.ovBuf, j.work, j.work, true, j.mainDesc, s.slots[(size_t)ovSlot], nullptr);
   }
+  int groupFirst[kEntropyGroups + 1] = {0};
   {
-    // Longest tile first, so the slowest chains start in the first wave.
-    std::vector<std::pair<uint32_t, int4>> ej;
+    // By group, then longest tile first, so the slowest chains start in the
+    // first wave.
+    std::vector<int> groupOf((size_t)nDesc, 0);
+    for (int st = 0; st < nsteps; st++) {
+      const StepInfo& si = R.steps[(size_t)st];
+      for (int di = si.mainFirst; di < si.mainFirst + si.mainCount; di++) groupOf[(size_t)di] = st / R.stepsPerGroup;
+      for (int di = si.ovFirst; di < si.ovFirst + si.ovCount; di++) groupOf[(size_t)di] = st / R.stepsPerGroup;
+    }
+    struct EJob {
+      int group;
+      uint32_t longest;
+      int4 job;
+    };
+    std::vector<EJob> ej;
     ej.reserve((size_t)nEJobs);
     for (int di = 0; di < nDesc; di++) {
       for (int t0 = 0; t0 < tilesOf[(size_t)di]; t0 += kEntropyTilesPerJob) {
         const int nt = std::min(kEntropyTilesPerJob, tilesOf[(size_t)di] - t0);
         uint32_t longest = 0;
         for (int t = t0; t < t0 + nt; t++) longest = std::max(longest, planOf[(size_t)di]->tiles[(size_t)t].length);
-        ej.push_back({longest, make_int4(di, t0, nt, 0)});
+        ej.push_back({groupOf[(size_t)di], longest, make_int4(di, t0, nt, 0)});
       }
     }
-    std::stable_sort(ej.begin(), ej.end(), [](const std::pair<uint32_t, int4>& a,
-                                              const std::pair<uint32_t, int4>& b) { return a.first > b.first; });
+    std::stable_sort(ej.begin(), ej.end(), [](const EJob& a, const EJob& b) {
+      return a.group != b.group ? a.group < b.group : a.longest > b.longest;
+    });
     int4* he = reinterpret_cast<int4*>(h + R.oEJobs);
-    for (size_t k = 0; k < ej.size(); k++) he[k] = ej[k].second;
-    *reinterpret_cast<int32_t*>(h + oQueue) = 0;
+    for (size_t k = 0; k < ej.size(); k++) {
+      he[k] = ej[k].job;
+      groupFirst[ej[k].group + 1] = (int)k + 1;
+    }
+    for (int g = 1; g <= R.groups; g++) groupFirst[g] = std::max(groupFirst[g], groupFirst[g - 1]);
+    for (int g = 0; g < R.groups; g++) *reinterpret_cast<int32_t*>(h + oQueue + 64 * (size_t)g) = 0;
   }
   if (cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, se) != cudaSuccess) return -1;
   const FrameDesc* dd = reinterpret_cast<const FrameDesc*>(d + R.oDesc);
+  const int4* de = reinterpret_cast<const int4*>(d + R.oEJobs);
   if (timing_) cudaEventRecord(ev_[P][0], se);
-  launchEntropy(dd, reinterpret_cast<const int4*>(d + R.oEJobs), nEJobs, reinterpret_cast<int32_t*>(d + oQueue), se);
-  launches_++;
-  cudaEventRecord(ev_[P][1], se);  // entropy done: the reconstruction waits on it
+  if (R.groups == 1) {
+    launchEntropy(dd, de, nEJobs, reinterpret_cast<int32_t*>(d + oQueue), se);
+    launches_++;
+  } else {
+    if (cudaEventRecord(evUp_[P], se) != cudaSuccess) return -1;
+    for (int g = 0; g < R.groups; g++) {
+      cudaStream_t sg = g == 0 ? se : streamEG_[g - 1];
+      if (g > 0 && cudaStreamWaitEvent(sg, evUp_[P], 0) != cudaSuccess) return -1;
+      launchEntropy(dd, de + groupFirst[g], groupFirst[g + 1] - groupFirst[g],
+                    reinterpret_cast<int32_t*>(d + oQueue + 64 * (size_t)g), sg);
+      launches_++;
+      if (cudaEventRecord(evGroup_[P][g], sg) != cudaSuccess) return -1;
+    }
+    for (int g = 1; g < R.groups; g++)
+      if (cudaStreamWaitEvent(se, evGroup_[P][g], 0) != cudaSuccess) return -1;
+  }
+  cudaEventRecord(ev_[P][1], se);  // all entropy done
   R.launched = true;
   planStream_ = nullptr;
   return kOK;
@@ -830,22 +927,61 @@ int Engine::launchRecon(Round& R) {
         return -1;
     }
   }
-  if (cudaStreamWaitEvent(sr, ev_[P][1], 0) != cudaSuccess) return -1;
+  // A step's reconstruction waits for its entropy group (the whole entropy
+  // stage when the round has one group).
+  const bool grouped = R.groups > 1;
+  auto entropyDone = [&](int st) { return grouped ? evGroup_[P][st / R.stepsPerGroup] : ev_[P][1]; };
+  if (cudaStreamWaitEvent(sr, entropyDone(0), 0) != cudaSuccess) return -1;
+  int groupA = 0, groupB = -1;
   const FrameDesc* dd = reinterpret_cast<const FrameDesc*>(d + R.oDesc);
   const int2* dj = reinterpret_cast<const int2*>(d + R.oJobs);
   if (timing_) cudaEventRecord(ev_[P][2], sr);
-  for (const StepInfo& si : R.steps) {
-    if (si.maxInterMBs > 0) {
-      launchInter(dd + si.mainFirst, si.mainCount, si.maxInterMBs, sr);
+  // Per step: inter phase 0 (macroblocks independent of the previous step's
+  // intra stage), inter phase 1 (the rest), intra.  On main rounds phase 0 of
+  // step s+1 runs on a second stream beside step s's intra stage: it waits
+  // for step s's inter pixels (event A) and step s+1's phase 1 waits for it
+  // (event B).
+  const int nsteps = (int)R.steps.size();
+  const bool split = P != kSide && streamB_ && nsteps > 1 && nsteps <= kMaxSteps;
+  for (int st = 0; st < nsteps; st++) {
+    const StepInfo& si = R.steps[(size_t)st];
+    if (grouped && st / R.stepsPerGroup != groupA) {
+      groupA = st / R.stepsPerGroup;
+      if (cudaStreamWaitEvent(sr, entropyDone(st), 0) != cudaSuccess) return -1;
+    }
+    if (split && st > 0) {
+      if (cudaStreamWaitEvent(sr, stepB_[P][st], 0) != cudaSuccess) return -1;
+    } else if (si.maxMBs > 0) {
+      launchInter(dd + si.mainFirst, si.mainCount, si.maxMBs, 0, sr);
       launches_++;
     }
+    if (si.maxMBs > 0 && si.hasPrev) {
+      launchInter(dd + si.mainFirst, si.mainCount, si.maxMBs, 1, sr);
+      launches_++;
+    }
+    if (split && st + 1 < nsteps) {
+      const StepInfo& nx = R.steps[(size_t)st + 1];
+      if (cudaEventRecord(stepA_[P][st], sr) != cudaSuccess ||
+          cudaStreamWaitEvent(streamB_, stepA_[P][st], 0) != cudaSuccess)
+        return -1;
+      const int gB = grouped ? (st + 1) / R.stepsPerGroup : 0;
+      if (gB != groupB) {
+        groupB = gB;
+        if (cudaStreamWaitEvent(streamB_, entropyDone(st + 1), 0) != cudaSuccess) return -1;
+      }
+      if (nx.maxMBs > 0) {
+        launchInter(dd + nx.mainFirst, nx.mainCount, nx.maxMBs, 0, streamB_);
+        launches_++;
+      }
+      if (cudaEventRecord(stepB_[P][st + 1], streamB_) != cudaSuccess) return -1;
+    }
     if (si.jobCount > 0) {
-      launchIntra(dd, dj + si.jobFirst, si.jobCount, sr);
+      launchIntra(dd, dj + si.jobFirst, si.jobCount, R.maxTileMBs, sr);
       launches_++;
     }
     if (si.ovCount > 0) {
-      launchInter(dd + si.ovFirst, si.ovCount, si.maxOvMBs, sr);
-      launchIntra(dd, dj + si.ovJobFirst, si.ovJobCount, sr);
+      launchInter(dd + si.ovFirst, si.ovCount, si.maxOvMBs, 0, sr);
+      launchIntra(dd, dj + si.ovJobFirst, si.ovJobCount, R.maxTileMBs, sr);
       launches_ += 2;
     }
   }

@@ -837,7 +837,44 @@ __device__ __forceinline__ void waitPreviousGrid() {
 #endif
 }
 
-__global__ void __launch_bounds__(32 * kInterWarps) kInterRecon(const FrameDesc* frames) {
+// Whether inter macroblock (mbx, mby) of f predicts from pixels of an intra
+// macroblock of the previous frame (f.prevRec) — a conservative test over
+// the bounding box of its vectors' source blocks, widened for the filter
+// taps and chroma rounding.  A previous key frame makes every macroblock
+// dependent; a golden-reference macroblock reads an older, complete frame.
+__device__ __forceinline__ bool interDepends(const FrameDesc& f, const RecRegs& r, int mode, int part, int mbx,
+                                             int mby) {
+  if (!f.prevRec) return false;
+  if (f.prevKey) return true;
+  if (mode == kRecInter && r.ref() == refGolden) return false;
+  const int np = mode == kRecInter ? (part == partWhole ? 1 : (part == part8x8 ? 4 : 2)) : 1;
+  int lo = 1 << 30, hi = -(1 << 30), vlo = 1 << 30, vhi = -(1 << 30);
+  for (int i = 0; i < np; i++) {
+    const uint32_t m = r.mv(i);
+    const int dx = (int16_t)(m & 0xFFFFu) >> 2, dy = (int16_t)(m >> 16) >> 2;
+    lo = min(lo, dx);
+    hi = max(hi, dx);
+    vlo = min(vlo, dy);
+    vhi = max(vhi, dy);
+  }
+  // Samples outside the plane are clamped to its edge: clamp each end of the
+  // box on its own, so a box wholly outside still names the edge macroblocks.
+  const int x0 = min(max(0, mbx * 16 + lo - 4), f.padW - 1), x1 = min(max(0, mbx * 16 + 15 + hi + 4), f.padW - 1);
+  const int y0 = min(max(0, mby * 16 + vlo - 4), f.padH - 1), y1 = min(max(0, mby * 16 + 15 + vhi + 4), f.padH - 1);
+  const int bx0 = x0 >> 4, bx1 = x1 >> 4, by0 = y0 >> 4, by1 = y1 >> 4;
+  if ((bx1 - bx0 + 1) * (by1 - by0 + 1) > 16) return true;  // wide spread: wait
+  for (int by = by0; by <= by1; by++)
+    for (int bx = bx0; bx <= bx1; bx++) {
+      const MBRec* q = f.prevRec + by * f.mbCols + bx;
+      if (q->mode == kRecIntra && q->wmask != 0) return true;
+    }
+  return false;
+}
+
+// phase 0: the macroblocks that do not depend on the previous frame's intra
+// stage (all of them when that stage is complete), and the residuals of the
+// intra macroblocks; phase 1: the other inter macroblocks.
+__global__ void __launch_bounds__(32 * kInterWarps, 6) kInterRecon(const FrameDesc* frames, int phase) {
   waitPreviousGrid();
   __shared__ InterScratch sS[kInterWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -846,7 +883,6 @@ __global__ void __launch_bounds__(32 * kInterWarps) kInterRecon(const FrameDesc*
     if (threadIdx.x == 0) atomicExch(f.status, kSkipped);
     return;
   }
-  if (!f.inter) return;
   const int idx = blockIdx.x * kInterWarps + warp;
   if (idx >= f.mbCols * f.mbRows) return;
   ReconView v;
@@ -854,24 +890,44 @@ __global__ void __launch_bounds__(32 * kInterWarps) kInterRecon(const FrameDesc*
   RecRegs r;
   r.load(v.mbrec + idx);
   const int mode = r.mode();
-  if (mode != kRecSkip && mode != kRecInter) return;
   const uint32_t wm = r.wmask();
   if (!wm) return;
   InterScratch& S = sS[warp];
+  // An intra macroblock's residual needs no pixels: phase 0 computes it and
+  // stores it over the macroblock's coefficient region, where the intra
+  // stage reads it.
+  const bool intra = mode == kRecIntra;
+  if (intra ? phase != 0 : (!f.inter || (mode != kRecSkip && mode != kRecInter))) return;
   const int mbx = idx % v.mbCols, mby = idx / v.mbCols;
   const bool golden = mode == kRecInter && r.ref() == refGolden;
   const uint8_t* const* refp = golden ? v.gold : v.ref;
   const int part = mode == kRecInter ? r.part() : partWhole;
   const int cbp = mode == kRecInter ? r.cbp() : 0;
+  if (intra) {
+  } else if (phase == 0) {
+    if (interDepends(f, r, mode, part, mbx, mby)) {
+      if (lane == 0) f.dep[idx] = 1;
+      return;
+    }
+    if (lane == 0 && f.prevRec) f.dep[idx] = 0;
+  } else if (!f.prevRec || !f.dep[idx]) {
+    return;
+  }
   const uint32_t nzm = r.nzmask();
   const int tx = r.tx();
 
   // Residuals of the coded blocks that are written, all at once.
-  uint32_t resMask = 0;
+  uint32_t resMask = intra ? nzm & wm : 0;
   if (cbp & cbpLuma) resMask |= nzm & wm & 0xFFFFu;
   if (cbp & cbpCb) resMask |= nzm & wm & (1u << 16);
   if (cbp & cbpCr) resMask |= nzm & wm & (1u << 17);
-  if (resMask) mbResidual(v.coef + (size_t)idx * kCoefPerMB, tx, resMask, v.qdc, v.qac, S.res, S.tmp, lane);
+  uint32_t* const cg = v.coef + (size_t)idx * kCoefPerMB;
+  if (resMask) mbResidual(cg, tx, resMask, v.qdc, v.qac, S.res, S.tmp, lane);
+  if (intra) {
+    if (resMask)
+      for (int q = lane; q < 384; q += 32) cg[q] = (uint32_t)S.res[q];
+    return;
+  }
 
   // Luma: lane -> row lane/2, 8 columns.
   {
@@ -942,7 +998,6 @@ __global__ void __launch_bounds__(32 * kInterWarps) kInterRecon(const FrameDesc*
 // ---------------------------------------------------------------------------
 // Stage B2: intra reconstruction wavefront
 // ---------------------------------------------------------------------------
-constexpr int kIntraWarps = 8;
 
 // Per-warp scratch of the intra stage.  The macroblock being reconstructed
 // lives in a working area in shared memory together with the samples its
@@ -952,8 +1007,7 @@ constexpr int kIntraWarps = 8;
 constexpr int kAreaW = 48;
 struct IntraScratch {
   int32_t ref[2][4 * 16 + 1];  // one reference array per half-warp block
-  int32_t res[384];  // levels, then residuals (mbResidual)
-  int32_t tmp[384];
+  int32_t res[384];            // the macroblock's residual (computed by kInterRecon phase 0)
   uint8_t areaY[17 * kAreaW];
   uint8_t areaC[2][9 * 16];
 };
@@ -1049,11 +1103,51 @@ __device__ void intraBlock(int32_t* ref, uint8_t* a, int as, int ax, int ay, uin
   __syncwarp();
 }
 
-// One part of an intra macroblock: part 0 its luma, part 1 its chroma.  The
-// two never read each other (chroma predicts from neighbouring chroma only),
-// so different warps take them.
-__device__ void intraMB(const ReconView& f, IntraScratch& S, int mbx, int mby, int tx0, int tx1, int ty0, int lane,
-                        int part) {
+// Progress of the intra macroblocks of one tile, shared by the warps of its
+// CTA.  luma[m] counts the completed diagonal steps of macroblock m's 4x4
+// luma blocks (kLumaDone when the luma is complete, at once for 8x8 and
+// 16x16 transforms); chroma[m] is 1 when both chroma blocks are.  Every
+// other macroblock of the tile starts complete.  A wait that runs past
+// kIntraSpinLimit polls sets abort, which ends every later wait at once;
+// the frame is then reported failed.
+constexpr int kLumaDone = 10;
+constexpr int kIntraSpinLimit = 1 << 20;
+struct IntraSync {
+  volatile uint8_t* luma;
+  volatile uint8_t* chroma;
+  volatile int* abort;
+  int x0, y0, x1, tw;  // the tile: first column and row, end column, width (macroblocks)
+  __device__ __forceinline__ int at(int mbx, int mby) const { return (mby - y0) * tw + (mbx - x0); }
+  // Waits until progress word p reaches need (all lanes poll the same word).
+  __device__ __forceinline__ void wait(volatile uint8_t* p, int need) const {
+    for (int it = 0; *p < need && !*abort; it++) {
+      if (it >= kIntraSpinLimit) {
+        *abort = 1;
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence_block();
+  }
+  // Publishes progress v once every lane's writes so far are visible to the CTA.
+  __device__ __forceinline__ void publish(volatile uint8_t* p, int v, int lane) const {
+    __threadfence_block();
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence_block();
+      *p = (uint8_t)v;
+    }
+  }
+};
+
+// The luma of an intra macroblock.  With 4x4 transforms the blocks run in
+// ten diagonal steps (bx + 2*by); step t needs the left neighbour's blocks
+// up to step t+3 (its column 3 at rows by), which the macroblock waits for
+// step by step, and the row above complete: the above-left and above
+// macroblocks done and the above-right one past step 6 (its block (0,3),
+// the only one the top-right block reads).  Other transform sizes wait for
+// all four neighbours to be done.
+__device__ void intraLuma(const ReconView& f, IntraScratch& S, const IntraSync& sy, int mbx, int mby, int lane) {
   const int idx = mby * f.mbCols + mbx;
   RecRegs r;
   r.load(f.mbrec + idx);
@@ -1062,54 +1156,26 @@ __device__ void intraMB(const ReconView& f, IntraScratch& S, int mbx, int mby, i
   if (!wm) return;
   const uint32_t nzm = r.nzmask();
   const int tx = r.tx(), n = 4 << tx, per = 4 >> tx, nb = per * per;
-  const int tileLeft = tx0 * 16, tileTop = ty0 * 16, tileRight = tx1 * 16;
+  const int tileLeft = sy.x0 * 16, tileTop = sy.y0 * 16, tileRight = sy.x1 * 16;
   const int mbLeft = mbx * 16, mbTop = mby * 16, mbRight = mbLeft + 16;
   uint8_t* const Y = f.rec[0];
-  const int ys = f.strideY, cs = f.strideC;
-  // The residual was computed before the level loop (kIntraRecon) and
-  // stored over the macroblock's coefficient region.
+  const int ys = f.strideY;
   const uint32_t resMask = nzm & wm;
   const uint32_t* rg = f.coef + (size_t)idx * kCoefPerMB;
-  const bool up = mbTop > tileTop, left = mbLeft > tileLeft;
-  if (part == 1) {
-    // Chroma: residuals, working areas (row above and column to the left,
-    // inside the tile) and the two 8x8 blocks.
-    if (resMask >> 16)
-      for (int q = 256 + lane; q < 384; q += 32) S.res[q] = (int32_t)rg[q];
-    const int cl = mbx * 8, ct = mby * 8;
-    for (int pl = 0; pl < 2; pl++) {
-      const uint8_t* C = f.rec[1 + pl];
-      if (up && lane < 9 && (lane > 0 || left)) S.areaC[pl][lane] = C[(size_t)(ct - 1) * cs + cl - 1 + lane];
-      if (left && lane < 8) S.areaC[pl][(1 + lane) * 16] = C[(size_t)(ct + lane) * cs + cl - 1];
-    }
-    __syncwarp();
-    const int cmode = r.cmode();
-    for (int pl = 0; pl < 2; pl++) {
-      const uint32_t bit = 1u << (16 + pl);
-      if (!(wm & bit)) break;
-      const bool hasRes = (nzm & bit) != 0;
-      intraBlock(S.ref[0], S.areaC[pl], 16, 1, 1, f.rec[1 + pl], cs, mbx * 8, mby * 8, 8, cmode, up, left, false,
-                 hasRes ? S.res + 256 + pl * 64 : nullptr, 8, lane, 32, true);
-    }
-    return;
-  }
-  // Luma: residuals and working area (row above from one left of the
-  // macroblock to 31 right of its left edge, column to the left; inside the
-  // tile only: nothing outside it is ever predicted from).
+  const bool up = mbTop > tileTop, left = mbLeft > tileLeft, ar = up && mbRight < tileRight;
   if (resMask & 0xFFFFu)
     for (int q = lane; q < 256; q += 32) S.res[q] = (int32_t)rg[q];
-  {
+  if (up) {
+    if (left) sy.wait(sy.luma + sy.at(mbx - 1, mby - 1), kLumaDone);
+    sy.wait(sy.luma + sy.at(mbx, mby - 1), kLumaDone);
+    if (ar) sy.wait(sy.luma + sy.at(mbx + 1, mby - 1), tx == 0 ? 7 : kLumaDone);
     for (int i = lane; i < 33; i += 32) {
       const int x = mbLeft - 1 + i;
-      if (up && x >= tileLeft && x < tileRight) S.areaY[i] = Y[(size_t)(mbTop - 1) * ys + x];
+      if (x >= tileLeft && x < tileRight) S.areaY[i] = Y[(size_t)(mbTop - 1) * ys + x];
     }
-    if (left && lane < 16) S.areaY[(1 + lane) * kAreaW] = Y[(size_t)(mbTop + lane) * ys + mbLeft - 1];
-    __syncwarp();
   }
-  // Luma blocks.  A block reads its left, above-left, above and above-right
-  // neighbours only, so the 4x4 blocks with equal bx + 2*by are independent:
-  // ten diagonal steps of up to two blocks, one per half warp.  Blocks
-  // beyond the first unwritten one (a prefix in raster order) are skipped.
+  volatile uint8_t* const own = sy.luma + sy.at(mbx, mby);
+  volatile uint8_t* const leftP = left ? sy.luma + sy.at(mbx - 1, mby) : nullptr;
   auto block = [&](int k, int l, int nl, bool active, int half) {
     const int bx = (k % per) * n, by = (k / per) * n;
     const int x0 = mbLeft + bx, y0 = mbTop + by;
@@ -1121,8 +1187,15 @@ __device__ void intraMB(const ReconView& f, IntraScratch& S, int mbx, int mby, i
                avLeft, avAR, hasRes ? S.res + by * 16 + bx : nullptr, 16, l, nl, active);
   };
   if (tx == 0) {
+    // Blocks beyond the first unwritten one (a prefix in raster order) are
+    // skipped; each step is published all the same.
     const int half = lane >> 4;
     for (int t = 0; t < 10; t++) {
+      if (left && !(t & 1) && t <= 6) {  // left column rows 2t..2t+3, for block (0, t/2)
+        sy.wait(leftP, t + 4);
+        if (lane < 4) S.areaY[(1 + 2 * t + lane) * kAreaW] = Y[(size_t)(mbTop + 2 * t + lane) * ys + mbLeft - 1];
+      }
+      __syncwarp();
       int k = -1, seen = 0;
       for (int yy = 0; yy < 4; yy++) {
         const int xx = t - 2 * yy;
@@ -1133,8 +1206,14 @@ __device__ void intraMB(const ReconView& f, IntraScratch& S, int mbx, int mby, i
       }
       const bool active = k >= 0 && ((wm >> k) & 1);
       block(active ? k : 0, lane & 15, 16, active, half);
+      sy.publish(own, t + 1, lane);
     }
   } else {
+    if (left) {
+      sy.wait(leftP, kLumaDone);
+      if (lane < 16) S.areaY[(1 + lane) * kAreaW] = Y[(size_t)(mbTop + lane) * ys + mbLeft - 1];
+    }
+    __syncwarp();
     for (int k = 0; k < nb; k++) {
       if (!((wm >> k) & 1)) break;
       block(k, lane, 32, true, 0);
@@ -1142,18 +1221,62 @@ __device__ void intraMB(const ReconView& f, IntraScratch& S, int mbx, int mby, i
   }
 }
 
-constexpr int kLevelBuckets = 1024;  // tiles with more intra levels take the scan path
+// The chroma of an intra macroblock: waits for the left, above-left and
+// above macroblocks' chroma (chroma prediction reads no above-right samples).
+__device__ void intraChroma(const ReconView& f, IntraScratch& S, const IntraSync& sy, int mbx, int mby, int lane) {
+  const int idx = mby * f.mbCols + mbx;
+  RecRegs r;
+  r.load(f.mbrec + idx);
+  if (r.mode() != kRecIntra) return;
+  const uint32_t wm = r.wmask();
+  if (!(wm >> 16)) return;
+  const uint32_t nzm = r.nzmask();
+  const bool up = mby > sy.y0, left = mbx > sy.x0;
+  const int cs = f.strideC;
+  const uint32_t* rg = f.coef + (size_t)idx * kCoefPerMB;
+  if ((nzm & wm) >> 16)
+    for (int q = 256 + lane; q < 384; q += 32) S.res[q] = (int32_t)rg[q];
+  if (up) {
+    if (left) sy.wait(sy.chroma + sy.at(mbx - 1, mby - 1), 1);
+    sy.wait(sy.chroma + sy.at(mbx, mby - 1), 1);
+  }
+  if (left) sy.wait(sy.chroma + sy.at(mbx - 1, mby), 1);
+  const int cl = mbx * 8, ct = mby * 8;
+  for (int pl = 0; pl < 2; pl++) {
+    const uint8_t* C = f.rec[1 + pl];
+    if (up && lane < 9 && (lane > 0 || left)) S.areaC[pl][lane] = C[(size_t)(ct - 1) * cs + cl - 1 + lane];
+    if (left && lane < 8) S.areaC[pl][(1 + lane) * 16] = C[(size_t)(ct + lane) * cs + cl - 1];
+  }
+  __syncwarp();
+  const int cmode = r.cmode();
+  for (int pl = 0; pl < 2; pl++) {
+    const uint32_t bit = 1u << (16 + pl);
+    if (!(wm & bit)) break;
+    const bool hasRes = (nzm & bit) != 0;
+    intraBlock(S.ref[0], S.areaC[pl], 16, 1, 1, f.rec[1 + pl], cs, mbx * 8, mby * 8, 8, cmode, up, left, false,
+               hasRes ? S.res + 256 + pl * 64 : nullptr, 8, lane, 32, true);
+  }
+}
 
-// One CTA per tile.  The tile's intra macroblocks (listed by the entropy
-// stage with their dependency levels) are counting-sorted by level, then each
-// level is reconstructed in parallel with a CTA barrier between levels.  Key
-// frames get the classic wavefront (level = x + 2y); inter frames with a few
-// isolated intra macroblocks take one or two levels.
-__global__ void __launch_bounds__(32 * kIntraWarps, 1) kIntraRecon(const FrameDesc* frames, const int2* jobs, int njobs) {
+// Tiles of up to this many macroblocks keep their progress in shared memory;
+// larger ones use the slot's progress bytes in global memory.
+constexpr int kIntraFlagMBs = 32768;
+
+// One CTA of W warps per tile, a dataflow schedule: the warps take the
+// tile's intra macroblocks' luma and chroma as jobs in raster order and each
+// job waits for exactly the neighbouring samples it predicts from
+// (IntraSync).  Raster order lists every job after the jobs it waits for, so
+// the earliest unfinished job can always proceed.  The residuals were
+// computed by kInterRecon phase 0.  Dynamic shared memory: W IntraScratch,
+// then 2 * min(flagMBs, kIntraFlagMBs) progress bytes.  Few tiles take 16
+// warps per CTA; many tiles fewer, so that several CTAs share an SM.
+template <int W>
+__global__ void __launch_bounds__(32 * W, 16 / W)
+    kIntraRecon(const FrameDesc* frames, const int2* jobs, int njobs, int flagMBs) {
   waitPreviousGrid();
-  __shared__ IntraScratch sS[kIntraWarps];
-  __shared__ int sStart[kLevelBuckets + 1];
-  __shared__ int sCur[kLevelBuckets];
+  extern __shared__ __align__(16) uint8_t sDyn[];
+  __shared__ int sNext, sAbort;
+  IntraScratch* sS = reinterpret_cast<IntraScratch*>(sDyn);
   const int j = blockIdx.x;
   if (j >= njobs) return;
   const FrameDesc& f = frames[jobs[j].x];
@@ -1162,76 +1285,67 @@ __global__ void __launch_bounds__(32 * kIntraWarps, 1) kIntraRecon(const FrameDe
     return;
   }
   const int tile = jobs[j].y;
-  const TileStat ts = f.tileStat[tile];
-  const int n = ts.intraCount;
+  const int n = f.tileStat[tile].intraCount;
   if (n == 0) return;
   const TileRange tr = f.tiles[tile];
-  const int L = ts.maxLevel + 1;
+  const int tw = tr.mbX1 - tr.mbX0, tmbs = tw * (tr.mbY1 - tr.mbY0);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, tid = threadIdx.x;
+  uint8_t* flags;
+  if (tmbs <= flagMBs) {
+    flags = sDyn + sizeof(IntraScratch) * W;
+  } else if (f.dep) {
+    flags = f.dep + (size_t)f.mbCols * f.mbRows + 2 * (size_t)tr.mbBase;
+  } else {
+    if (tid == 0) atomicExch(f.status, kErrDevice);
+    return;
+  }
+  IntraSync sy;
+  sy.luma = flags;
+  sy.chroma = flags + tmbs;
+  sy.abort = &sAbort;
+  sy.x0 = tr.mbX0;
+  sy.y0 = tr.mbY0;
+  sy.x1 = tr.mbX1;
+  sy.tw = tw;
   const uint32_t* list = f.intraList + tr.mbBase;
-  uint32_t* sorted = f.intraSorted + tr.mbBase;
+  for (int i = tid; i < tmbs; i += blockDim.x) {
+    sy.luma[i] = kLumaDone;
+    sy.chroma[i] = 1;
+  }
+  if (tid == 0) {
+    sNext = 0;
+    sAbort = 0;
+  }
+  __syncthreads();
+  const int mbCols = f.mbCols;
+  for (int i = tid; i < n; i += blockDim.x) {
+    const int idx = (int)(list[i] & kIndexMask);
+    const int m = sy.at(idx % mbCols, idx / mbCols);
+    sy.luma[m] = 0;
+    sy.chroma[m] = 0;
+  }
+  __syncthreads();
   ReconView view;
   view.load(f);
-  // Residuals of every listed macroblock, all warps in parallel (they do not
-  // depend on neighbouring pixels); each replaces its macroblock's
-  // coefficient region, which nothing reads afterwards.
-  for (int i = warp; i < n; i += kIntraWarps) {
-    const int idx = (int)(list[i] & kIndexMask);
-    RecRegs rr;
-    rr.load(view.mbrec + idx);
-    const uint32_t resMask = rr.nzmask() & rr.wmask();
-    if (rr.mode() != kRecIntra || !resMask) continue;
-    uint32_t* cg = view.coef + (size_t)idx * kCoefPerMB;
-    mbResidual(cg, rr.tx(), resMask, view.qdc, view.qac, sS[warp].res, sS[warp].tmp, lane);
-    for (int q = lane; q < 384; q += 32) cg[q] = (uint32_t)sS[warp].res[q];
+  IntraScratch& S = sS[warp];
+  for (;;) {
+    int k = 0;
+    if (lane == 0) k = atomicAdd(&sNext, 1);
+    k = __shfl_sync(kFull, k, 0);
+    if (k >= 2 * n) break;
+    const int idx = (int)(list[k >> 1] & kIndexMask);
+    const int mbx = idx % mbCols, mby = idx / mbCols;
+    if (k & 1) {
+      intraChroma(view, S, sy, mbx, mby, lane);
+      sy.publish(sy.chroma + sy.at(mbx, mby), 1, lane);
+    } else {
+      intraLuma(view, S, sy, mbx, mby, lane);
+      sy.publish(sy.luma + sy.at(mbx, mby), kLumaDone, lane);
+    }
     __syncwarp();
   }
   __syncthreads();
-  auto runMB = [&](uint32_t e, int part) {
-    const int idx = (int)(e & kIndexMask);
-    intraMB(view, sS[warp], idx % view.mbCols, idx / view.mbCols, tr.mbX0, tr.mbX1, tr.mbY0, lane, part);
-  };
-  if (L <= kLevelBuckets) {
-    for (int l = tid; l <= L; l += blockDim.x) sStart[l] = 0;
-    __syncthreads();
-    for (int i = tid; i < n; i += blockDim.x) atomicAdd(&sStart[(list[i] >> kLevelShift) + 1], 1);
-    __syncthreads();
-    if (warp == 0) {  // inclusive scan of counts -> exclusive level starts
-      const int per = (L + 1 + 31) / 32;
-      const int b = lane * per, e = min(b + per, L + 1);
-      int run = 0;
-      for (int l = b; l < e; l++) run += sStart[l];
-      int incl = run;
-      for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(kFull, incl, o);
-        if (lane >= o) incl += v;
-      }
-      int acc = incl - run;
-      for (int l = b; l < e; l++) {
-        acc += sStart[l];
-        sStart[l] = acc;
-      }
-    }
-    __syncthreads();
-    for (int l = tid; l < L; l += blockDim.x) sCur[l] = sStart[l];
-    __syncthreads();
-    for (int i = tid; i < n; i += blockDim.x) {
-      const uint32_t e = list[i];
-      sorted[atomicAdd(&sCur[e >> kLevelShift], 1)] = e;
-    }
-    __syncthreads();
-    for (int l = 0; l < L; l++) {  // jobs: (macroblock, part) pairs of the level
-      for (int k = 2 * sStart[l] + warp; k < 2 * sStart[l + 1]; k += kIntraWarps) runMB(sorted[k >> 1], k & 1);
-      __syncthreads();
-    }
-  } else {
-    // Very wide or tall tiles: scan the list once per level.
-    for (int l = 0; l < L; l++) {
-      for (int i = warp; i < 2 * n; i += kIntraWarps)
-        if ((int)(list[i >> 1] >> kLevelShift) == l) runMB(list[i >> 1], i & 1);
-      __syncthreads();
-    }
-  }
+  if (tid == 0 && sAbort) atomicExch(f.status, kErrDevice);
 }
 
 }  // namespace dev
@@ -1276,10 +1390,11 @@ void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* ne
 // The reconstruction launches overlap their start with the previous kernel
 // of the stream (programmatic dependent launch; the kernels wait for it).
 template <class... A>
-static void launchDependent(void (*k)(A...), dim3 grid, dim3 block, cudaStream_t s, A... args) {
+static void launchDependent(void (*k)(A...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -1289,15 +1404,55 @@ static void launchDependent(void (*k)(A...), dim3 grid, dim3 block, cudaStream_t
   cudaLaunchKernelEx(&cfg, k, args...);
 }
 
-void launchInter(const FrameDesc* frames, int nframes, int maxMBs, cudaStream_t s) {
+void launchInter(const FrameDesc* frames, int nframes, int maxMBs, int phase, cudaStream_t s) {
   if (nframes <= 0 || maxMBs <= 0) return;
   dim3 grid((maxMBs + dev::kInterWarps - 1) / dev::kInterWarps, nframes);
-  launchDependent(dev::kInterRecon, grid, dim3(32 * dev::kInterWarps), s, frames);
+  launchDependent(dev::kInterRecon, grid, dim3(32 * dev::kInterWarps), 0, s, frames, phase);
 }
 
-void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, cudaStream_t s) {
+template <int W>
+static void allowIntraSmem() {
+  cudaFuncSetAttribute(dev::kIntraRecon<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(dev::IntraScratch) * W + 2 * (size_t)dev::kIntraFlagMBs));
+}
+
+template <int W>
+static void launchIntraW(const FrameDesc* frames, const int2* jobs, int njobs, int flagMBs, cudaStream_t s) {
+  constexpr size_t kScratch = sizeof(dev::IntraScratch) * W;
+  const size_t smem = kScratch + (((size_t)2 * flagMBs + 15) & ~(size_t)15);
+  launchDependent(dev::kIntraRecon<W>, dim3(njobs), dim3(32 * W), smem, s, frames, jobs, njobs, flagMBs);
+}
+
+// maxTileMBs: the largest tile of the launch's frames, in macroblocks.  The
+// warps per CTA follow the tile count: 16 up to one CTA per SM, 8 up to two,
+// else 4.
+void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, cudaStream_t s) {
   if (njobs <= 0) return;
-  launchDependent(dev::kIntraRecon, dim3(njobs), dim3(32 * dev::kIntraWarps), s, frames, jobs, njobs);
+  static int sms[64] = {0};
+  int d = 0;
+  cudaGetDevice(&d);
+  bool first = false;
+  int nsm = 152;
+  if (d >= 0 && d < 64) {
+    if (!sms[d]) {
+      cudaDeviceGetAttribute(&sms[d], cudaDevAttrMultiProcessorCount, d);
+      sms[d] = std::max(1, sms[d]);
+      first = true;
+    }
+    nsm = sms[d];
+  }
+  if (first) {  // the shared-memory limits of all three, once per device
+    allowIntraSmem<16>();
+    allowIntraSmem<8>();
+    allowIntraSmem<4>();
+  }
+  const int flagMBs = std::max(1, std::min(maxTileMBs, dev::kIntraFlagMBs));
+  if (njobs <= nsm)
+    launchIntraW<16>(frames, jobs, njobs, flagMBs, s);
+  else if (njobs <= 2 * nsm)
+    launchIntraW<8>(frames, jobs, njobs, flagMBs, s);
+  else
+    launchIntraW<4>(frames, jobs, njobs, flagMBs, s);
 }
 
 }  // namespace ebiv

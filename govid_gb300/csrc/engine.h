@@ -145,6 +145,17 @@ class Engine {
   cudaStream_t streamES_ = nullptr, streamRS_ = nullptr;  // side lane: entropy, reconstruction
   cudaStream_t planStream_ = nullptr;  // reconstruction stream of the round being planned
   cudaEvent_t sideDone_ = nullptr;
+  // Entropy groups of pipelined main rounds: streams for groups 1.., the
+  // staging-upload event and one completion event per group.
+  static constexpr int kEntropyGroups = 4;
+  cudaStream_t streamEG_[kEntropyGroups - 1] = {};
+  cudaEvent_t evUp_[2] = {};
+  cudaEvent_t evGroup_[2][kEntropyGroups] = {};
+  // Second reconstruction stream of main rounds and its per-step events.
+  static constexpr int kMaxSteps = 65;
+  cudaStream_t streamB_ = nullptr;
+  cudaEvent_t stepA_[2][kMaxSteps] = {};
+  cudaEvent_t stepB_[2][kMaxSteps] = {};
   bool ownStream_ = false, ownStreamE_ = false;
   bool pipelined_ = false, side_ = false, sideInflight_ = false;
   std::vector<std::unique_ptr<Stream>> streams_;

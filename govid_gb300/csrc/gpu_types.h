@@ -92,6 +92,15 @@ struct FrameDesc {
   // stream decoded in the same round).  When it is nonzero the reconstruction
   // kernels skip this frame and mark it kSkipped; the host re-plans it.
   const int32_t* gate;
+  // Records of that previous frame while its intra stage may still be
+  // running (null when it is complete), and whether it was a key frame
+  // (then every macroblock of this frame waits for it).  Inter
+  // reconstruction runs in two phases: macroblocks whose prediction reads
+  // no intra macroblock of the previous frame, then the rest (marked in dep).
+  const MBRec* prevRec;
+  int32_t prevKey;
+  int32_t pad2;
+  uint8_t* dep;
 };
 
 }  // namespace ebiv
