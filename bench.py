@@ -248,7 +248,7 @@ def run_gpu(args):
     alg = algorithmic_bytes(pkts, W, H)
 
     # ---- value: packets resident in HBM, device frame pool output ----
-    b = ebiv.Batch(lookahead=args.lookahead, pipeline=not args.no_pipeline)
+    b = ebiv.Batch(lookahead=args.lookahead, pipeline=0 if args.no_pipeline else args.pipeline_depth)
     sid = b.add_stream(pkts, ring=3)
 
     def one_pass(lat=None):
@@ -301,7 +301,7 @@ def run_gpu(args):
         o += len(p)
     ring_frames = 64
     pin_out = torch.empty(ring_frames * fb, dtype=torch.uint8, pin_memory=True)
-    eb = ebiv.Batch(lookahead=args.lookahead, pipeline=not args.no_pipeline)
+    eb = ebiv.Batch(lookahead=args.lookahead, pipeline=0 if args.no_pipeline else args.pipeline_depth)
     esid = eb.add_stream(pkts, ring=3)
 
     def e2e_pass():
@@ -363,7 +363,8 @@ def run_gpu(args):
         "data": "synthetic (seeded sprite scene encoded by this repo's EBIV encoder)",
         "config": {"workload": f"EBIV decode, 1 stream {W}x{H} {n} frames q22 gop60 tiles 4x3 (fast encode)",
                    "frames_per_step": n, "packet_bytes_per_step": h2d, "l2": "flushed between steps",
-                   "lookahead_frames": args.lookahead, "pipelined_rounds": not args.no_pipeline,
+                   "lookahead_frames": args.lookahead,
+                   "pipeline_depth": 0 if args.no_pipeline else args.pipeline_depth,
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e, 2), "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "api": "Batch: packets reloaded from pinned host memory, every frame copied to pinned host memory"},
@@ -404,10 +405,11 @@ def run_gpu(args):
 
 def all_rounds(b, lat=None):
     """Every result of a batch until its streams are exhausted.  A pipelined
-    round returns the previous round's results, so stop after two empty
-    rounds and collect the one in flight.  lat gets each call's wall time."""
+    round returns the results of the round planned b.depth calls before, so
+    stop after depth + 1 empty rounds and collect the rounds in flight.  lat
+    gets each call's wall time."""
     empty = 0
-    while empty < 2:
+    while empty < b.depth + 1:
         t = time.perf_counter()
         res = b.round()
         if lat is not None and res:
@@ -602,6 +604,8 @@ def main():
     ap.add_argument("--mix-lookahead", default="1,4", help="comma list: headline (latency-bounded) first")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-pipeline", action="store_true", help="synchronous rounds (no entropy/recon overlap)")
+    ap.add_argument("--pipeline-depth", type=int, default=2,
+                    help="rounds planned ahead of the one reconstructing (single-stream legs)")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-mv", action="store_true")
     ap.add_argument("--mv-frames", type=int, default=16)

@@ -86,7 +86,7 @@ struct Engine::Stream {
   int pRef = -1, pGolden = -1;
   int64_t lastRound = 0;
   int64_t epoch = 0;
-  std::vector<int> roundBufs[3];  // by round parity (2: side lane)
+  std::vector<int> roundBufs[Engine::kParities];  // by round parity (the last: side lane)
   bool inSide = false;            // a side round holds this stream
 
   uint8_t* plane(int b, int k) const {
@@ -144,6 +144,7 @@ struct Engine::Round {
   int groups = 1, stepsPerGroup = 1;  // entropy launches (groups of consecutive steps)
   size_t oDesc = 0, oStat = 0, oJobs = 0, oEJobs = 0;
   bool launched = false;  // entropy launched; statuses pending
+  bool reconLaunched = false;
   void clear() {
     jobs.clear();
     chains.clear();
@@ -154,7 +155,7 @@ struct Engine::Round {
   }
 };
 
-Engine::Engine() : rounds_(new Round[3]) {}
+Engine::Engine() : rounds_(new Round[kParities]) {}
 
 Engine::~Engine() {
   if (streamE_) cudaStreamSynchronize(streamE_);
@@ -176,7 +177,7 @@ Engine::~Engine() {
     cudaStreamSynchronize(streamB_);
     cudaStreamDestroy(streamB_);
   }
-  for (int p = 0; p < 2; p++)
+  for (int p = 0; p < kMainParities; p++)
     for (int k = 0; k < kMaxSteps; k++) {
       if (stepA_[p][k]) cudaEventDestroy(stepA_[p][k]);
       if (stepB_[p][k]) cudaEventDestroy(stepB_[p][k]);
@@ -186,7 +187,7 @@ Engine::~Engine() {
       cudaStreamSynchronize(sg);
       cudaStreamDestroy(sg);
     }
-  for (int p = 0; p < 2; p++) {
+  for (int p = 0; p < kMainParities; p++) {
     if (evUp_[p]) cudaEventDestroy(evUp_[p]);
     for (auto& e : evGroup_[p])
       if (e) cudaEventDestroy(e);
@@ -208,12 +209,12 @@ int Engine::init(cudaStream_t s) {
     for (auto& e : row)
       if (cudaEventCreate(&e) != cudaSuccess) return kErrDevice;
   if (cudaStreamCreateWithFlags(&streamB_, cudaStreamNonBlocking) != cudaSuccess) return kErrDevice;
-  for (int p = 0; p < 2; p++) {
+  for (int p = 0; p < kMainParities; p++) {
     if (cudaEventCreateWithFlags(&evUp_[p], cudaEventDisableTiming) != cudaSuccess) return kErrDevice;
     for (auto& e : evGroup_[p])
       if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return kErrDevice;
   }
-  for (int p = 0; p < 2; p++)
+  for (int p = 0; p < kMainParities; p++)
     for (int k = 0; k < kMaxSteps; k++)
       if (cudaEventCreateWithFlags(&stepA_[p][k], cudaEventDisableTiming) != cudaSuccess ||
           cudaEventCreateWithFlags(&stepB_[p][k], cudaEventDisableTiming) != cudaSuccess)
@@ -234,18 +235,18 @@ int Engine::setLookahead(int k) {
 }
 
 // Frame buffers per stream: the ring's outputs plus a round's, the two
-// references, and the buffers a round claims; a pipelined engine holds two
-// rounds' worth of claims.
-int Engine::poolSize(int ring, int k, bool pipelined, bool side) {
-  return (pipelined ? ring + 3 * k + 4 : ring + 2 * k + 3) + (side ? k + 1 : 0);
+// references, and the buffers a round claims; a pipelined engine of depth D
+// holds D more rounds' worth of claims.
+int Engine::poolSize(int ring, int k, int depth, bool side) {
+  return ring + (2 + depth) * k + 3 + depth + (side ? k + 1 : 0);
 }
 
-size_t Engine::footprint(int w, int h, int ring, int lookahead, bool pipelined, bool side) {
+size_t Engine::footprint(int w, int h, int ring, int lookahead, int depth, bool side) {
   const Geometry g = Geometry::of(w, h);
   const size_t yb = (size_t)stride64(g.padW()) * g.padH(), cb = (size_t)stride64(g.padCW()) * g.padCH();
   const size_t mbs = (size_t)g.mbCols * g.mbRows;
-  return (size_t)poolSize(ring, lookahead, pipelined, side) * (yb + 2 * cb) +
-         (size_t)((pipelined ? 2 : 1) + (side ? 1 : 0)) * (lookahead + 1) * Slot::bytes(mbs);
+  return (size_t)poolSize(ring, lookahead, depth, side) * (yb + 2 * cb) +
+         (size_t)(depth + 1 + (side ? 1 : 0)) * (lookahead + 1) * Slot::bytes(mbs);
 }
 
 int Engine::addResidentStream(const uint8_t* const* pkts, const size_t* lens, int n, int ring, int* id) {
@@ -280,7 +281,7 @@ int Engine::addResidentStream(const uint8_t* const* pkts, const size_t* lens, in
 // round's entropy stage, the only reader of packet bytes.
 int Engine::reloadStream(int id, const uint8_t* const* pkts, const size_t* lens, int n) {
   if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id] || n < 0) return kErrArg;
-  if (inflight_ >= 0) return kErrArg;  // drain() first
+  if (!pipe_.empty()) return kErrArg;  // drain() first
   Stream& s = *streams_[(size_t)id];
   if (!s.resident) return kErrArg;
   size_t total = 0;
@@ -329,7 +330,7 @@ int Engine::downloadFrameAsync(const EngineFrameView& v, uint8_t* packed, size_t
 }
 
 int Engine::addStreamingStream(int ring, int* id) {
-  if (pipelined_) return kErrArg;  // pipelined rounds keep packets resident
+  if (pipeDepth_) return kErrArg;  // pipelined rounds keep packets resident
   std::unique_ptr<Stream> s(new (std::nothrow) Stream());
   if (!s) return kErrArg;
   s->ring = ring >= 2 ? ring : 3;
@@ -390,7 +391,7 @@ int Engine::configure(Stream& s, int w, int h) {
   s.cBytes = (size_t)s.strideC * s.geo.padCH();
   s.bufBytes = s.yBytes + 2 * s.cBytes;
   const int k = s.resident ? lookahead_ : 1;
-  const int P = poolSize(s.ring, k, pipelined_, side_);
+  const int P = poolSize(s.ring, k, pipeDepth_, side_);
   cudaStream_t zs = planStream_ ? planStream_ : stream_;
   for (int i = 0; i < P; i++) {
     uint8_t* p = nullptr;
@@ -584,16 +585,18 @@ int Engine::round(std::vector<RoundResult>* results) {
 // stream whose round-N chain failed has its round-N+1 frames skipped and
 // re-planned).
 // ---------------------------------------------------------------------------
-int Engine::setPipelined(bool on) {
+int Engine::setPipelined(int depth) {
+  if (depth < 0 || depth > kMaxDepth) return kErrArg;
   for (auto& s : streams_)
     if (s) return kErrArg;  // pool and slot counts depend on it
+  const bool on = depth > 0;
   if (on && !streamE_) {
     if (cudaStreamCreateWithFlags(&streamE_, cudaStreamNonBlocking) != cudaSuccess) return kErrDevice;
     ownStreamE_ = true;
   }
   for (auto& sg : streamEG_)
     if (on && !sg && cudaStreamCreateWithFlags(&sg, cudaStreamNonBlocking) != cudaSuccess) return kErrDevice;
-  pipelined_ = on;
+  pipeDepth_ = depth;
   return kOK;
 }
 
@@ -749,7 +752,7 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
   // reconstruction waits only for its own group: the long chains of a large
   // frame late in the round do not hold back the steps before it.
   const int nsteps = (int)R.steps.size();
-  R.groups = (P != kSide && pipelined_ && streamEG_[0] && nsteps > 1) ? std::min(kEntropyGroups, nsteps) : 1;
+  R.groups = (P != kSide && pipeDepth_ && streamEG_[0] && nsteps > 1) ? std::min(kEntropyGroups, nsteps) : 1;
   R.stepsPerGroup = (nsteps + R.groups - 1) / R.groups;
   R.groups = (nsteps + R.stepsPerGroup - 1) / R.stepsPerGroup;
   R.oDesc = 0;
@@ -1059,7 +1062,7 @@ int Engine::collectRound(Round& R, std::vector<RoundResult>* results) {
 
 int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* results,
                      const std::vector<int>* maxFrames) {
-  if (!pipelined_) {
+  if (!pipeDepth_) {
     Round& R = rounds_[0];
     R.parity = 0;
     if (planRound(ids, maxFrames, R) || launchRecon(R)) {
@@ -1071,23 +1074,45 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
     }
     return collectRound(R, results);
   }
-  // Pipelined: plan this round and start its entropy stage, collect the
-  // round in flight, then launch this round's reconstruction.
-  const int p = inflight_ < 0 ? 0 : 1 - inflight_;
+  // Pipelined: plan this round and start its entropy stage; when more than
+  // depth rounds are in flight, collect the oldest (whose results this call
+  // returns); then launch the reconstruction of the oldest round not yet
+  // reconstructing (its predecessor has been collected).
+  int p = 0;
+  for (bool used = true; used; p++) {
+    used = false;
+    for (int q : pipe_) used = used || q == p;
+    if (!used) break;
+  }
   Round& R = rounds_[p];
   R.parity = p;
-  const int planSt = planRound(ids, maxFrames, R);
+  R.reconLaunched = false;
+  int failed = planRound(ids, maxFrames, R) ? p : -1;
+  pipe_.push_back(p);
   int n = 0;
-  if (inflight_ >= 0) n = collectRound(rounds_[inflight_], results);
-  inflight_ = -1;
-  if (planSt || launchRecon(R)) {
-    for (Job& j : R.jobs)
-      if (j.status == kOK) j.status = kErrDevice;
-    R.nDesc = 0;
-    collectRound(R, results);
+  if ((int)pipe_.size() > pipeDepth_ && rounds_[pipe_.front()].reconLaunched) {
+    n = collectRound(rounds_[pipe_.front()], results);
+    pipe_.erase(pipe_.begin());
+  }
+  Round& F = rounds_[pipe_.front()];
+  if (!F.reconLaunched) {
+    if (failed != F.parity && launchRecon(F)) failed = F.parity;
+    F.reconLaunched = true;
+  }
+  if (failed >= 0) {  // a device call failed: finish every round in flight
+    for (int q : pipe_) {
+      Round& X = rounds_[q];
+      if (q == failed) {
+        for (Job& j : X.jobs)
+          if (j.status == kOK) j.status = kErrDevice;
+        X.nDesc = 0;
+      }
+      if (!X.reconLaunched && q != failed) launchRecon(X);
+      n += collectRound(X, results);
+    }
+    pipe_.clear();
     return -1;
   }
-  inflight_ = p;
   return n;
 }
 
@@ -1125,9 +1150,18 @@ int Engine::collectSide(std::vector<RoundResult>* results) {
 }
 
 int Engine::drain(std::vector<RoundResult>* results) {
-  if (inflight_ < 0) return 0;
-  const int n = collectRound(rounds_[inflight_], results);
-  inflight_ = -1;
+  int n = 0;
+  while (!pipe_.empty()) {
+    Round& R = rounds_[pipe_.front()];
+    if (!R.reconLaunched && launchRecon(R)) {
+      for (Job& j : R.jobs)
+        if (j.status == kOK) j.status = kErrDevice;
+      R.nDesc = 0;
+    }
+    R.reconLaunched = true;
+    n += collectRound(R, results);
+    pipe_.erase(pipe_.begin());
+  }
   return n;
 }
 
@@ -1317,7 +1351,7 @@ int ebivgpu_batch_timing(ebivgpu_batch* b, int enable, double* kernel_ms, double
 
 int ebivgpu_batch_set_lookahead(ebivgpu_batch* b, int frames) { return b ? b->e.setLookahead(frames) : kErrArg; }
 
-int ebivgpu_batch_set_pipeline(ebivgpu_batch* b, int on) { return b ? b->e.setPipelined(on != 0) : kErrArg; }
+int ebivgpu_batch_set_pipeline(ebivgpu_batch* b, int depth) { return b ? b->e.setPipelined(depth) : kErrArg; }
 
 int ebivgpu_batch_drain(ebivgpu_batch* b, int* frames) {
   if (!b) return kErrArg;

@@ -81,8 +81,13 @@ class Engine {
   // stream, collects the round in flight (whose results it returns) and then
   // launches the new round's reconstruction, so one round's entropy overlaps
   // the previous round's reconstruction.  drain() collects the last round.
-  int setPipelined(bool on);
-  bool pipelined() const { return pipelined_; }
+  // depth 2 keeps two rounds ahead of the one reconstructing: a round's
+  // entropy stage starts two round() calls before its reconstruction, and a
+  // round's results come back two calls after it was planned.  depth 0 is
+  // the synchronous engine.
+  int setPipelined(int depth);
+  bool pipelined() const { return pipeDepth_ > 0; }
+  int pipeDepth() const { return pipeDepth_; }
   int drain(std::vector<RoundResult>* results);
   // Side lane (set before adding streams): a round for a few streams (the
   // serving loop sends key frames there) that runs on its own pair of CUDA
@@ -106,8 +111,8 @@ class Engine {
   int64_t launches() const { return launches_; }
   size_t deviceBytes() const { return deviceBytes_; }
   // Per-stream HBM footprint (pool + scratch) for a geometry.
-  static size_t footprint(int w, int h, int ring, int lookahead, bool pipelined = false, bool side = false);
-  static int poolSize(int ring, int lookahead, bool pipelined, bool side = false);
+  static size_t footprint(int w, int h, int ring, int lookahead, int depth = 0, bool side = false);
+  static int poolSize(int ring, int lookahead, int depth, bool side = false);
 
   // Kernel-time accounting: CUDA events recorded around each round's
   // kernels on the engine's stream.
@@ -132,13 +137,16 @@ class Engine {
   int collectRound(Round& r, std::vector<RoundResult>* results);
   // Streams of a round by parity: 0/1 main (pipelined rounds alternate), 2 side.
   cudaStream_t entropyStream(int parity = 0) const {
-    return parity == kSide ? streamES_ : (pipelined_ ? streamE_ : stream_);
+    return parity == kSide ? streamES_ : (pipeDepth_ ? streamE_ : stream_);
   }
   cudaStream_t reconStream(int parity = 0) const { return parity == kSide ? streamRS_ : stream_; }
-  int slotSet(int parity) const { return parity == kSide ? (pipelined_ ? 2 : 1) : parity; }
-  int slotSets() const { return (pipelined_ ? 2 : 1) + (side_ ? 1 : 0); }
-  static constexpr int kSide = 2;
-  static constexpr int kParities = 3;
+  int mainSets() const { return pipeDepth_ + 1; }
+  int slotSet(int parity) const { return parity == kSide ? mainSets() : parity; }
+  int slotSets() const { return mainSets() + (side_ ? 1 : 0); }
+  static constexpr int kMaxDepth = 2;
+  static constexpr int kMainParities = kMaxDepth + 1;  // main rounds in flight at most
+  static constexpr int kSide = kMainParities;
+  static constexpr int kParities = kMainParities + 1;
 
   cudaStream_t stream_ = nullptr;   // reconstruction, copies, status read-back
   cudaStream_t streamE_ = nullptr;  // entropy stage of pipelined rounds
@@ -149,30 +157,31 @@ class Engine {
   // staging-upload event and one completion event per group.
   static constexpr int kEntropyGroups = 4;
   cudaStream_t streamEG_[kEntropyGroups - 1] = {};
-  cudaEvent_t evUp_[2] = {};
-  cudaEvent_t evGroup_[2][kEntropyGroups] = {};
+  cudaEvent_t evUp_[kMainParities] = {};
+  cudaEvent_t evGroup_[kMainParities][kEntropyGroups] = {};
   // Second reconstruction stream of main rounds and its per-step events.
   static constexpr int kMaxSteps = 65;
   cudaStream_t streamB_ = nullptr;
-  cudaEvent_t stepA_[2][kMaxSteps] = {};
-  cudaEvent_t stepB_[2][kMaxSteps] = {};
+  cudaEvent_t stepA_[kMainParities][kMaxSteps] = {};
+  cudaEvent_t stepB_[kMainParities][kMaxSteps] = {};
   bool ownStream_ = false, ownStreamE_ = false;
-  bool pipelined_ = false, side_ = false, sideInflight_ = false;
+  int pipeDepth_ = 0;
+  bool side_ = false, sideInflight_ = false;
   std::vector<std::unique_ptr<Stream>> streams_;
   std::unique_ptr<Round[]> rounds_;  // by parity
-  int inflight_ = -1;  // parity of the round whose reconstruction is in flight
+  std::vector<int> pipe_;  // parities of the main rounds in flight, oldest first
   int64_t roundSeq_ = 0;
-  uint8_t* dStage_[3] = {nullptr, nullptr, nullptr};
-  uint8_t* hStage_[3] = {nullptr, nullptr, nullptr};
-  size_t stageCap_[3] = {0, 0, 0};
-  int32_t* hStatus_[3] = {nullptr, nullptr, nullptr};
-  int statusCap_[3] = {0, 0, 0};
+  uint8_t* dStage_[kParities] = {};
+  uint8_t* hStage_[kParities] = {};
+  size_t stageCap_[kParities] = {};
+  int32_t* hStatus_[kParities] = {};
+  int statusCap_[kParities] = {};
   int32_t* dOne_ = nullptr;  // constant 1: the gate of discarded frames
   int64_t launches_ = 0;
   int lookahead_ = 1;
   size_t deviceBytes_ = 0;
   bool timing_ = false;
-  cudaEvent_t ev_[3][4] = {};
+  cudaEvent_t ev_[kParities][4] = {};
   double kernelMs_ = 0, entropyMs_ = 0, reconMs_ = 0;
 };
 

@@ -206,18 +206,21 @@ class Batch:
     """Many independent EBIV streams decoded together: each round decodes the
     next packet of every active stream with one set of kernel launches."""
 
-    def __init__(self, lookahead: int = 1, pipeline: bool = False):
-        """pipeline: each round() returns the previous round's results while
-        the new round's entropy stage overlaps its reconstruction; drain()
-        returns the last round's (resident streams only)."""
+    def __init__(self, lookahead: int = 1, pipeline: bool | int = False):
+        """pipeline (True or a depth of 1 or 2): each round() plans a round
+        and starts its entropy stage while earlier rounds reconstruct, and
+        returns the results of the round planned `depth` calls before; drain()
+        returns those of the rounds still in flight (resident streams only).
+        Depth 2 starts a round's entropy stage one round earlier."""
         L = _native.lib()
         h = C.c_void_p()
         _check(L.ebivgpu_batch_create(C.byref(h)), "batch")
         self._h, self._L = h, L
+        self.depth = int(pipeline)  # rounds between planning a round and getting its results
         if lookahead != 1:
             _check(L.ebivgpu_batch_set_lookahead(h, int(lookahead)), "lookahead")
         if pipeline:
-            _check(L.ebivgpu_batch_set_pipeline(h, 1), "pipeline")
+            _check(L.ebivgpu_batch_set_pipeline(h, self.depth), "pipeline")
 
     def add_stream(self, packets: list[bytes], ring: int = 3) -> int:
         n = len(packets)

@@ -13,10 +13,10 @@ pytestmark = pytest.mark.gpu
 
 def run_rounds(b):
     """All results of a batch, synchronous or pipelined: a pipelined round
-    returns the previous round's results, so stop after two empty rounds and
-    collect the last one."""
+    returns the results of the round planned b.depth calls before, so stop
+    after depth + 1 empty rounds and collect the rounds still in flight."""
     empty = 0
-    while empty < 2:
+    while empty < b.depth + 1:
         res = b.round()
         empty = empty + 1 if not res else 0
         yield from res
@@ -38,7 +38,7 @@ def _streams():
     return out
 
 
-@pytest.mark.parametrize("lookahead,pipeline", [(1, False), (4, False), (1, True), (4, True)])
+@pytest.mark.parametrize("lookahead,pipeline", [(1, False), (4, False), (1, True), (4, True), (1, 2), (4, 2)])
 def test_batch_matches_oracle(gpu_required, lookahead, pipeline):
     streams = _streams()
     b = ebiv.Batch(lookahead=lookahead, pipeline=pipeline)
@@ -128,7 +128,7 @@ def _zero_tile(pkt: bytes, tile: int) -> bytes:
     return bytes(b)
 
 
-@pytest.mark.parametrize("lookahead,pipeline", [(1, False), (4, False), (1, True), (4, True)])
+@pytest.mark.parametrize("lookahead,pipeline", [(1, False), (4, False), (1, True), (4, True), (4, 2)])
 def test_batch_error_mid_chain_matches_oracle(gpu_required, lookahead, pipeline):
     # A frame that fails on the GPU leaves its references untouched
     # (ebiv/codec.go:174-191); later frames of the same round are re-planned.
@@ -183,8 +183,8 @@ def test_fuzzed_packets_match_oracle(gpu_required):
             assert g[1] == want[i][1], f"case {case} frame {i}: planes differ from the oracle"
 
 
-@pytest.mark.parametrize("lookahead", [1, 3])
-def test_fuzzed_streams_pipelined_batch_match_oracle(gpu_required, lookahead):
+@pytest.mark.parametrize("lookahead,depth", [(1, 1), (3, 1), (3, 2)])
+def test_fuzzed_streams_pipelined_batch_match_oracle(gpu_required, lookahead, depth):
     # Corrupted packets in several streams decoded together by a pipelined
     # batch: every status and plane equals the oracle decoding each stream
     # alone, through the rollbacks that failures force on rounds planned
@@ -205,7 +205,7 @@ def test_fuzzed_streams_pipelined_batch_match_oracle(gpu_required, lookahead):
                     b[i] ^= 1 << rng.randrange(8)
             pkts.append(bytes(b))
         streams.append((pkts, 96 + 32 * k, 64))
-    b = ebiv.Batch(lookahead=lookahead, pipeline=True)
+    b = ebiv.Batch(lookahead=lookahead, pipeline=depth)
     want, dims = {}, {}
     for pkts, w, h in streams:
         sid = b.add_stream(pkts)
