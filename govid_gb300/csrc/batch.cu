@@ -14,7 +14,7 @@ namespace ebiv {
 
 void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* next, cudaStream_t s);
 void launchInter(const FrameDesc* frames, int nframes, int maxMBs, int phase, cudaStream_t s);
-void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, cudaStream_t s);
+void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, int maxTileKeys, cudaStream_t s);
 
 namespace {
 inline size_t al(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -140,16 +140,22 @@ struct Engine::Round {
   std::vector<std::vector<int>> chains;  // per stream, indices into jobs in decode order
   std::vector<StepInfo> steps;
   int nDesc = 0, nTiles = 0, nEJobs = 0;
-  int maxTileMBs = 0;  // largest tile of the round's frames (macroblocks)
+  int maxTileMBs = 0;   // largest tile of the round's frames (macroblocks)
+  int maxTileKeys = 0;  // largest intra wavefront key range of those tiles
   int groups = 1, stepsPerGroup = 1;  // entropy launches (groups of consecutive steps)
   size_t oDesc = 0, oStat = 0, oJobs = 0, oEJobs = 0;
   bool launched = false;  // entropy launched; statuses pending
   bool reconLaunched = false;
+  void noteTile(const TileRange& t) {
+    const int w = t.mbX1 - t.mbX0, h = t.mbY1 - t.mbY0;
+    maxTileMBs = std::max(maxTileMBs, w * h);
+    maxTileKeys = std::max(maxTileKeys, 4 * (w - 1) + 11 * (h - 1) + 1);
+  }
   void clear() {
     jobs.clear();
     chains.clear();
     steps.clear();
-    nDesc = nTiles = nEJobs = maxTileMBs = 0;
+    nDesc = nTiles = nEJobs = maxTileMBs = maxTileKeys = 0;
     groups = stepsPerGroup = 1;
     launched = false;
   }
@@ -211,8 +217,8 @@ int Engine::init(cudaStream_t s) {
   if (cudaStreamCreateWithFlags(&streamB_, cudaStreamNonBlocking) != cudaSuccess) return kErrDevice;
   for (int p = 0; p < kMainParities; p++) {
     if (cudaEventCreateWithFlags(&evUp_[p], cudaEventDisableTiming) != cudaSuccess) return kErrDevice;
-    for (auto& e : evGroup_[p])
-      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return kErrDevice;
+    for (auto& e : evGroup_[p])  // timed: the entropy time of a grouped round ends at its last group
+      if (cudaEventCreate(&e) != cudaSuccess) return kErrDevice;
   }
   for (int p = 0; p < kMainParities; p++)
     for (int k = 0; k < kMaxSteps; k++)
@@ -719,8 +725,7 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
       nTiles += (int)j.main.tiles.size();
       si.jobCount += (int)j.main.tiles.size();
       si.maxMBs = std::max(si.maxMBs, (int)streams_[(size_t)j.stream]->mbs);
-      for (const TileRange& t : j.main.tiles)
-        R.maxTileMBs = std::max(R.maxTileMBs, (int)(t.mbX1 - t.mbX0) * (int)(t.mbY1 - t.mbY0));
+      for (const TileRange& t : j.main.tiles) R.noteTile(t);
     }
     si.ovFirst = nDesc;
     si.ovJobFirst = nTiles;
@@ -731,8 +736,7 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
       nTiles += (int)j.ov.tiles.size();
       si.ovJobCount += (int)j.ov.tiles.size();
       si.maxOvMBs = std::max(si.maxOvMBs, (int)streams_[(size_t)j.stream]->mbs);
-      for (const TileRange& t : j.ov.tiles)
-        R.maxTileMBs = std::max(R.maxTileMBs, (int)(t.mbX1 - t.mbX0) * (int)(t.mbY1 - t.mbY0));
+      for (const TileRange& t : j.ov.tiles) R.noteTile(t);
     }
   }
   R.nDesc = nDesc;
@@ -891,20 +895,21 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
   if (R.groups == 1) {
     launchEntropy(dd, de, nEJobs, reinterpret_cast<int32_t*>(d + oQueue), se);
     launches_++;
+    cudaEventRecord(ev_[P][1], se);  // entropy done
   } else {
+    // The entropy stream carries only the staging copy; the groups run on
+    // pool streams after it.
     if (cudaEventRecord(evUp_[P], se) != cudaSuccess) return -1;
     for (int g = 0; g < R.groups; g++) {
-      cudaStream_t sg = g == 0 ? se : streamEG_[g - 1];
-      if (g > 0 && cudaStreamWaitEvent(sg, evUp_[P], 0) != cudaSuccess) return -1;
+      cudaStream_t sg = streamEG_[nextEG_];
+      nextEG_ = (nextEG_ + 1) % kEntropyStreams;
+      if (cudaStreamWaitEvent(sg, evUp_[P], 0) != cudaSuccess) return -1;
       launchEntropy(dd, de + groupFirst[g], groupFirst[g + 1] - groupFirst[g],
                     reinterpret_cast<int32_t*>(d + oQueue + 64 * (size_t)g), sg);
       launches_++;
       if (cudaEventRecord(evGroup_[P][g], sg) != cudaSuccess) return -1;
     }
-    for (int g = 1; g < R.groups; g++)
-      if (cudaStreamWaitEvent(se, evGroup_[P][g], 0) != cudaSuccess) return -1;
   }
-  cudaEventRecord(ev_[P][1], se);  // all entropy done
   R.launched = true;
   planStream_ = nullptr;
   return kOK;
@@ -979,12 +984,12 @@ int Engine::launchRecon(Round& R) {
       if (cudaEventRecord(stepB_[P][st + 1], streamB_) != cudaSuccess) return -1;
     }
     if (si.jobCount > 0) {
-      launchIntra(dd, dj + si.jobFirst, si.jobCount, R.maxTileMBs, sr);
+      launchIntra(dd, dj + si.jobFirst, si.jobCount, R.maxTileMBs, R.maxTileKeys, sr);
       launches_++;
     }
     if (si.ovCount > 0) {
       launchInter(dd + si.ovFirst, si.ovCount, si.maxOvMBs, 0, sr);
-      launchIntra(dd, dj + si.ovJobFirst, si.ovJobCount, R.maxTileMBs, sr);
+      launchIntra(dd, dj + si.ovJobFirst, si.ovJobCount, R.maxTileMBs, R.maxTileKeys, sr);
       launches_ += 2;
     }
   }
@@ -1007,7 +1012,15 @@ int Engine::collectRound(Round& R, std::vector<RoundResult>* results) {
   }
   if (timing_ && gpu) {
     float a = 0, b = 0;
-    cudaEventElapsedTime(&a, ev_[P][0], ev_[P][1]);
+    if (R.groups > 1) {  // entropy time: until the last group is done
+      for (int g = 0; g < R.groups; g++) {
+        float t = 0;
+        cudaEventElapsedTime(&t, ev_[P][0], evGroup_[P][g]);
+        a = std::max(a, t);
+      }
+    } else {
+      cudaEventElapsedTime(&a, ev_[P][0], ev_[P][1]);
+    }
     cudaEventElapsedTime(&b, ev_[P][2], ev_[P][3]);
     entropyMs_ += a;
     reconMs_ += b;

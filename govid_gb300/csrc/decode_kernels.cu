@@ -1261,21 +1261,32 @@ __device__ void intraChroma(const ReconView& f, IntraScratch& S, const IntraSync
 // Tiles of up to this many macroblocks keep their progress in shared memory;
 // larger ones use the slot's progress bytes in global memory.
 constexpr int kIntraFlagMBs = 32768;
+// Shared memory for ordering a tile's jobs (key counts, then the ordered list).
+constexpr int kIntraSortBytes = 64 * 1024;
+
+// Wavefront key of an intra macroblock at (x, y) of its tile: a 4x4-luma
+// macroblock can start 4 diagonal steps after its left neighbour, 7 after
+// the above-right one and 11 after the one above (10 steps, then the row
+// above is complete), so 4x + 11y orders every job after the jobs it waits
+// for and interleaves the rows the way the dependencies allow.
+__device__ __forceinline__ int intraKey(int x, int y) { return 4 * x + 11 * y; }
 
 // One CTA of W warps per tile, a dataflow schedule: the warps take the
-// tile's intra macroblocks' luma and chroma as jobs in raster order and each
-// job waits for exactly the neighbouring samples it predicts from
-// (IntraSync).  Raster order lists every job after the jobs it waits for, so
+// tile's intra macroblocks' luma and chroma as jobs in wavefront order
+// (intraKey; raster order when the tile's ordering does not fit sortInts)
+// and each job waits for exactly the neighbouring samples it predicts from
+// (IntraSync).  Either order lists every job after the jobs it waits for, so
 // the earliest unfinished job can always proceed.  The residuals were
 // computed by kInterRecon phase 0.  Dynamic shared memory: W IntraScratch,
-// then 2 * min(flagMBs, kIntraFlagMBs) progress bytes.  Few tiles take 16
-// warps per CTA; many tiles fewer, so that several CTAs share an SM.
+// 2 * flagMBs progress bytes (rounded to 16), sortInts words for the
+// ordering.  Few tiles take 16 warps per CTA; many tiles fewer, so that
+// several CTAs share an SM.
 template <int W>
 __global__ void __launch_bounds__(32 * W, 16 / W)
-    kIntraRecon(const FrameDesc* frames, const int2* jobs, int njobs, int flagMBs) {
+    kIntraRecon(const FrameDesc* frames, const int2* jobs, int njobs, int flagMBs, int sortInts) {
   waitPreviousGrid();
   extern __shared__ __align__(16) uint8_t sDyn[];
-  __shared__ int sNext, sAbort;
+  __shared__ int sNext, sAbort, sWarpTot[W];
   IntraScratch* sS = reinterpret_cast<IntraScratch*>(sDyn);
   const int j = blockIdx.x;
   if (j >= njobs) return;
@@ -1288,7 +1299,7 @@ __global__ void __launch_bounds__(32 * W, 16 / W)
   const int n = f.tileStat[tile].intraCount;
   if (n == 0) return;
   const TileRange tr = f.tiles[tile];
-  const int tw = tr.mbX1 - tr.mbX0, tmbs = tw * (tr.mbY1 - tr.mbY0);
+  const int tw = tr.mbX1 - tr.mbX0, th = tr.mbY1 - tr.mbY0, tmbs = tw * th;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, tid = threadIdx.x;
   uint8_t* flags;
   if (tmbs <= flagMBs) {
@@ -1325,6 +1336,57 @@ __global__ void __launch_bounds__(32 * W, 16 / W)
     sy.chroma[m] = 0;
   }
   __syncthreads();
+  // Wavefront order: a counting sort of the list by intraKey in shared memory.
+  const uint32_t* order = list;
+  const int nkeys = intraKey(tw - 1, th - 1) + 1;
+  if (nkeys + n <= sortInts) {
+    int* cnt = reinterpret_cast<int*>(sDyn + sizeof(IntraScratch) * W + (((size_t)2 * flagMBs + 15) & ~(size_t)15));
+    uint32_t* out = reinterpret_cast<uint32_t*>(cnt + nkeys);
+    auto keyOf = [&](uint32_t e) {
+      const int idx = (int)(e & kIndexMask);
+      return intraKey(idx % mbCols - tr.mbX0, idx / mbCols - tr.mbY0);
+    };
+    for (int i = tid; i < nkeys; i += blockDim.x) cnt[i] = 0;
+    __syncthreads();
+    for (int i = tid; i < n; i += blockDim.x) atomicAdd(&cnt[keyOf(list[i])], 1);
+    __syncthreads();
+    {  // exclusive scan of cnt: per-thread chunks, then warps, then the CTA
+      const int per = (nkeys + (int)blockDim.x - 1) / (int)blockDim.x;
+      const int b = min(tid * per, nkeys), e = min(b + per, nkeys);
+      int run = 0;
+      for (int i = b; i < e; i++) run += cnt[i];
+      int incl = run;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += v;
+      }
+      if (lane == 31) sWarpTot[warp] = incl;
+      __syncthreads();
+      if (warp == 0) {
+        const int t = lane < W ? sWarpTot[lane] : 0;
+        int it = t;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(kFull, it, o);
+          if (lane >= o) it += v;
+        }
+        if (lane < W) sWarpTot[lane] = it - t;
+      }
+      __syncthreads();
+      int acc = sWarpTot[warp] + incl - run;
+      for (int i = b; i < e; i++) {
+        const int c = cnt[i];
+        cnt[i] = acc;
+        acc += c;
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += blockDim.x) {
+      const uint32_t e = list[i];
+      out[atomicAdd(&cnt[keyOf(e)], 1)] = e;
+    }
+    __syncthreads();
+    order = out;
+  }
   ReconView view;
   view.load(f);
   IntraScratch& S = sS[warp];
@@ -1333,7 +1395,7 @@ __global__ void __launch_bounds__(32 * W, 16 / W)
     if (lane == 0) k = atomicAdd(&sNext, 1);
     k = __shfl_sync(kFull, k, 0);
     if (k >= 2 * n) break;
-    const int idx = (int)(list[k >> 1] & kIndexMask);
+    const int idx = (int)(order[k >> 1] & kIndexMask);
     const int mbx = idx % mbCols, mby = idx / mbCols;
     if (k & 1) {
       intraChroma(view, S, sy, mbx, mby, lane);
@@ -1413,20 +1475,23 @@ void launchInter(const FrameDesc* frames, int nframes, int maxMBs, int phase, cu
 template <int W>
 static void allowIntraSmem() {
   cudaFuncSetAttribute(dev::kIntraRecon<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)(sizeof(dev::IntraScratch) * W + 2 * (size_t)dev::kIntraFlagMBs));
+                       (int)(sizeof(dev::IntraScratch) * W + 2 * (size_t)dev::kIntraFlagMBs + dev::kIntraSortBytes));
 }
 
 template <int W>
-static void launchIntraW(const FrameDesc* frames, const int2* jobs, int njobs, int flagMBs, cudaStream_t s) {
+static void launchIntraW(const FrameDesc* frames, const int2* jobs, int njobs, int flagMBs, int sortInts,
+                         cudaStream_t s) {
   constexpr size_t kScratch = sizeof(dev::IntraScratch) * W;
-  const size_t smem = kScratch + (((size_t)2 * flagMBs + 15) & ~(size_t)15);
-  launchDependent(dev::kIntraRecon<W>, dim3(njobs), dim3(32 * W), smem, s, frames, jobs, njobs, flagMBs);
+  const size_t smem = kScratch + (((size_t)2 * flagMBs + 15) & ~(size_t)15) + 4 * (size_t)sortInts;
+  launchDependent(dev::kIntraRecon<W>, dim3(njobs), dim3(32 * W), smem, s, frames, jobs, njobs, flagMBs, sortInts);
 }
 
-// maxTileMBs: the largest tile of the launch's frames, in macroblocks.  The
-// warps per CTA follow the tile count: 16 up to one CTA per SM, 8 up to two,
-// else 4.
-void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, cudaStream_t s) {
+// maxTileMBs: the largest tile of the launch's frames, in macroblocks;
+// maxTileKeys: the largest wavefront key range of its tiles (4*(w-1) +
+// 11*(h-1) + 1 for a tile of w x h macroblocks).  The warps per CTA follow
+// the tile count: 16 up to one CTA per SM, 8 up to two, else 4.
+void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, int maxTileKeys,
+                 cudaStream_t s) {
   if (njobs <= 0) return;
   static int sms[64] = {0};
   int d = 0;
@@ -1447,12 +1512,14 @@ void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTi
     allowIntraSmem<4>();
   }
   const int flagMBs = std::max(1, std::min(maxTileMBs, dev::kIntraFlagMBs));
+  int sortInts = std::max(0, maxTileMBs) + std::max(0, maxTileKeys);
+  if (4 * (size_t)sortInts > (size_t)dev::kIntraSortBytes) sortInts = 0;  // raster order
   if (njobs <= nsm)
-    launchIntraW<16>(frames, jobs, njobs, flagMBs, s);
+    launchIntraW<16>(frames, jobs, njobs, flagMBs, sortInts, s);
   else if (njobs <= 2 * nsm)
-    launchIntraW<8>(frames, jobs, njobs, flagMBs, s);
+    launchIntraW<8>(frames, jobs, njobs, flagMBs, sortInts, s);
   else
-    launchIntraW<4>(frames, jobs, njobs, flagMBs, s);
+    launchIntraW<4>(frames, jobs, njobs, flagMBs, sortInts, s);
 }
 
 }  // namespace ebiv

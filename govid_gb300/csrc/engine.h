@@ -153,10 +153,13 @@ class Engine {
   cudaStream_t streamES_ = nullptr, streamRS_ = nullptr;  // side lane: entropy, reconstruction
   cudaStream_t planStream_ = nullptr;  // reconstruction stream of the round being planned
   cudaEvent_t sideDone_ = nullptr;
-  // Entropy groups of pipelined main rounds: streams for groups 1.., the
+  // Entropy groups of pipelined main rounds: a pool of streams the groups
+  // take in turn (so the groups of consecutive rounds run side by side), the
   // staging-upload event and one completion event per group.
   static constexpr int kEntropyGroups = 4;
-  cudaStream_t streamEG_[kEntropyGroups - 1] = {};
+  static constexpr int kEntropyStreams = 2 * kEntropyGroups;
+  cudaStream_t streamEG_[kEntropyStreams] = {};
+  int nextEG_ = 0;
   cudaEvent_t evUp_[kMainParities] = {};
   cudaEvent_t evGroup_[kMainParities][kEntropyGroups] = {};
   // Second reconstruction stream of main rounds and its per-step events.

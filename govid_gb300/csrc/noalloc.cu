@@ -33,7 +33,7 @@ namespace ebiv {
 
 void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* next, cudaStream_t s);
 void launchInter(const FrameDesc* frames, int nframes, int maxMBs, int phase, cudaStream_t s);
-void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, cudaStream_t s);
+void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, int maxTileKeys, cudaStream_t s);
 
 namespace {
 
@@ -217,11 +217,15 @@ extern "C" int ebivgpu_decode_key_noalloc(const uint8_t* pkt, size_t n, uint8_t*
   const int4* de = reinterpret_cast<const int4*>(d + kOffEJobs);
   const int nt0 = (int)plan[0].tiles.size();
   auto groups = [](int nt) { return (nt + kEntropyTilesPerJob - 1) / kEntropyTilesPerJob; };
-  int maxTile = 0;
-  for (const TileRange& t : plan[0].tiles) maxTile = std::max(maxTile, (int)(t.mbX1 - t.mbX0) * (int)(t.mbY1 - t.mbY0));
+  int maxTile = 0, maxKeys = 0;
+  for (const TileRange& t : plan[0].tiles) {
+    const int w = t.mbX1 - t.mbX0, h = t.mbY1 - t.mbY0;
+    maxTile = std::max(maxTile, w * h);
+    maxKeys = std::max(maxKeys, 4 * (w - 1) + 11 * (h - 1) + 1);
+  }
   launchEntropy(dd, de, groups(nt0), nullptr, s);
   launchInter(dd, 1, (int)mbs, 0, s);  // the intra macroblocks' residuals
-  launchIntra(dd, dj, nt0, maxTile, s);
+  launchIntra(dd, dj, nt0, maxTile, maxKeys, s);
   if (withOv) launchEntropy(dd, de + kNAMaxEJobs, groups((int)plan[1].tiles.size()), nullptr, s);  // after the key's recon
   if (cudaMemcpyAsync(status, d + kOffStatus, sizeof(status), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess)
