@@ -829,11 +829,20 @@ struct InterScratch {
 
 // Reconstruction kernels are launched with programmatic stream
 // serialisation, so a grid may start while the previous kernel of the stream
-// finishes; this wait (a no-op without a prerequisite grid) holds every
-// thread until that kernel's results are complete and visible.
+// runs; this wait (a no-op without a prerequisite grid) holds every thread
+// until that kernel's results are complete and visible.
 __device__ __forceinline__ void waitPreviousGrid() {
 #ifdef __CUDA_ARCH__
   asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+
+// Lets the next kernel of the stream be scheduled now: its CTAs start and
+// hold in waitPreviousGrid until this grid is complete, so the launch
+// latency overlaps this kernel.
+__device__ __forceinline__ void allowNextGrid() {
+#ifdef __CUDA_ARCH__
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 #endif
 }
 
@@ -875,6 +884,7 @@ __device__ __forceinline__ bool interDepends(const FrameDesc& f, const RecRegs& 
 // stage (all of them when that stage is complete), and the residuals of the
 // intra macroblocks; phase 1: the other inter macroblocks.
 __global__ void __launch_bounds__(32 * kInterWarps, 6) kInterRecon(const FrameDesc* frames, int phase) {
+  allowNextGrid();
   waitPreviousGrid();
   __shared__ InterScratch sS[kInterWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1284,20 +1294,23 @@ __device__ __forceinline__ int intraKey(int x, int y) { return 4 * x + 11 * y; }
 template <int W>
 __global__ void __launch_bounds__(32 * W, 16 / W)
     kIntraRecon(const FrameDesc* frames, const int2* jobs, int njobs, int flagMBs, int sortInts) {
-  waitPreviousGrid();
+  allowNextGrid();
   extern __shared__ __align__(16) uint8_t sDyn[];
   __shared__ int sNext, sAbort, sWarpTot[W];
   IntraScratch* sS = reinterpret_cast<IntraScratch*>(sDyn);
   const int j = blockIdx.x;
   if (j >= njobs) return;
+  // Up to the job loop this kernel reads only what the entropy stage wrote
+  // (tile statistics, the intra list), so it runs ahead of the previous
+  // kernel's completion; the gate and every pixel are read after the wait.
   const FrameDesc& f = frames[jobs[j].x];
-  if (f.gate && *f.gate) {
-    if (threadIdx.x == 0) atomicExch(f.status, kSkipped);
-    return;
-  }
   const int tile = jobs[j].y;
   const int n = f.tileStat[tile].intraCount;
-  if (n == 0) return;
+  if (n == 0) {
+    waitPreviousGrid();
+    if (threadIdx.x == 0 && f.gate && *f.gate) atomicExch(f.status, kSkipped);
+    return;
+  }
   const TileRange tr = f.tiles[tile];
   const int tw = tr.mbX1 - tr.mbX0, th = tr.mbY1 - tr.mbY0, tmbs = tw * th;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, tid = threadIdx.x;
@@ -1386,6 +1399,11 @@ __global__ void __launch_bounds__(32 * W, 16 / W)
     }
     __syncthreads();
     order = out;
+  }
+  waitPreviousGrid();
+  if (f.gate && *f.gate) {
+    if (threadIdx.x == 0) atomicExch(f.status, kSkipped);
+    return;
   }
   ReconView view;
   view.load(f);
