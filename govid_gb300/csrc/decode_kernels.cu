@@ -1173,19 +1173,40 @@ __device__ void intraLuma(const ReconView& f, IntraScratch& S, const IntraSync& 
   const uint32_t resMask = nzm & wm;
   const uint32_t* rg = f.coef + (size_t)idx * kCoefPerMB;
   const bool up = mbTop > tileTop, left = mbLeft > tileLeft, ar = up && mbRight < tileRight;
-  if (resMask & 0xFFFFu)
-    for (int q = lane; q < 256; q += 32) S.res[q] = (int32_t)rg[q];
+  volatile uint8_t* const own = sy.luma + sy.at(mbx, mby);
+  volatile uint8_t* const leftP = left ? sy.luma + sy.at(mbx - 1, mby) : nullptr;
+  // The residual, the row above and, when the left neighbour is complete,
+  // the left column are loaded together (one global latency); otherwise the
+  // left column follows the left neighbour's steps.
+  const bool lumaRes = (resMask & 0xFFFFu) != 0;
+  int32_t rv[8];
+  if (lumaRes)
+#pragma unroll
+    for (int q = 0; q < 8; q++) rv[q] = (int32_t)rg[lane + 32 * q];
   if (up) {
     if (left) sy.wait(sy.luma + sy.at(mbx - 1, mby - 1), kLumaDone);
     sy.wait(sy.luma + sy.at(mbx, mby - 1), kLumaDone);
     if (ar) sy.wait(sy.luma + sy.at(mbx + 1, mby - 1), tx == 0 ? 7 : kLumaDone);
-    for (int i = lane; i < 33; i += 32) {
-      const int x = mbLeft - 1 + i;
-      if (x >= tileLeft && x < tileRight) S.areaY[i] = Y[(size_t)(mbTop - 1) * ys + x];
-    }
   }
-  volatile uint8_t* const own = sy.luma + sy.at(mbx, mby);
-  volatile uint8_t* const leftP = left ? sy.luma + sy.at(mbx - 1, mby) : nullptr;
+  if (left && tx != 0) sy.wait(leftP, kLumaDone);
+  // One decision for the whole warp (lane 0's reading of the flag).
+  bool leftNow = false;
+  if (left) leftNow = __shfl_sync(kFull, *leftP >= kLumaDone ? 1 : 0, 0) != 0;
+  if (leftNow) __threadfence_block();
+  const int xa = mbLeft - 1 + lane;
+  const bool haveA = up && xa >= tileLeft && xa < tileRight;
+  const bool haveB = up && lane == 0 && mbLeft + 31 < tileRight;  // area entry 32
+  const uint8_t* const rowAbove = Y + (size_t)(mbTop - 1) * ys;
+  uint8_t a0 = 0, a1 = 0, lc = 0;
+  if (haveA) a0 = rowAbove[xa];
+  if (haveB) a1 = rowAbove[mbLeft + 31];
+  if (leftNow && lane < 16) lc = Y[(size_t)(mbTop + lane) * ys + mbLeft - 1];
+  if (lumaRes)
+#pragma unroll
+    for (int q = 0; q < 8; q++) S.res[lane + 32 * q] = rv[q];
+  if (haveA) S.areaY[lane] = a0;
+  if (haveB) S.areaY[32] = a1;
+  if (leftNow && lane < 16) S.areaY[(1 + lane) * kAreaW] = lc;
   auto block = [&](int k, int l, int nl, bool active, int half) {
     const int bx = (k % per) * n, by = (k / per) * n;
     const int x0 = mbLeft + bx, y0 = mbTop + by;
@@ -1201,7 +1222,7 @@ __device__ void intraLuma(const ReconView& f, IntraScratch& S, const IntraSync& 
     // skipped; each step is published all the same.
     const int half = lane >> 4;
     for (int t = 0; t < 10; t++) {
-      if (left && !(t & 1) && t <= 6) {  // left column rows 2t..2t+3, for block (0, t/2)
+      if (left && !leftNow && !(t & 1) && t <= 6) {  // left column rows 2t..2t+3, for block (0, t/2)
         sy.wait(leftP, t + 4);
         if (lane < 4) S.areaY[(1 + 2 * t + lane) * kAreaW] = Y[(size_t)(mbTop + 2 * t + lane) * ys + mbLeft - 1];
       }
@@ -1219,11 +1240,7 @@ __device__ void intraLuma(const ReconView& f, IntraScratch& S, const IntraSync& 
       sy.publish(own, t + 1, lane);
     }
   } else {
-    if (left) {
-      sy.wait(leftP, kLumaDone);
-      if (lane < 16) S.areaY[(1 + lane) * kAreaW] = Y[(size_t)(mbTop + lane) * ys + mbLeft - 1];
-    }
-    __syncwarp();
+    __syncwarp();  // the left column was loaded with the row above
     for (int k = 0; k < nb; k++) {
       if (!((wm >> k) & 1)) break;
       block(k, lane, 32, true, 0);
@@ -1244,18 +1261,38 @@ __device__ void intraChroma(const ReconView& f, IntraScratch& S, const IntraSync
   const bool up = mby > sy.y0, left = mbx > sy.x0;
   const int cs = f.strideC;
   const uint32_t* rg = f.coef + (size_t)idx * kCoefPerMB;
-  if ((nzm & wm) >> 16)
-    for (int q = 256 + lane; q < 384; q += 32) S.res[q] = (int32_t)rg[q];
+  const bool chromaRes = ((nzm & wm) >> 16) != 0;
+  int32_t rv[4];
+  if (chromaRes)
+#pragma unroll
+    for (int q = 0; q < 4; q++) rv[q] = (int32_t)rg[256 + lane + 32 * q];
   if (up) {
     if (left) sy.wait(sy.chroma + sy.at(mbx - 1, mby - 1), 1);
     sy.wait(sy.chroma + sy.at(mbx, mby - 1), 1);
   }
   if (left) sy.wait(sy.chroma + sy.at(mbx - 1, mby), 1);
   const int cl = mbx * 8, ct = mby * 8;
-  for (int pl = 0; pl < 2; pl++) {
-    const uint8_t* C = f.rec[1 + pl];
-    if (up && lane < 9 && (lane > 0 || left)) S.areaC[pl][lane] = C[(size_t)(ct - 1) * cs + cl - 1 + lane];
-    if (left && lane < 8) S.areaC[pl][(1 + lane) * 16] = C[(size_t)(ct + lane) * cs + cl - 1];
+  // Both planes' row above and left column, loaded together.
+  const bool haveT = up && lane < 9 && (lane > 0 || left), haveL = left && lane < 8;
+  uint8_t t0 = 0, t1 = 0, l0 = 0, l1 = 0;
+  if (haveT) {
+    t0 = f.rec[1][(size_t)(ct - 1) * cs + cl - 1 + lane];
+    t1 = f.rec[2][(size_t)(ct - 1) * cs + cl - 1 + lane];
+  }
+  if (haveL) {
+    l0 = f.rec[1][(size_t)(ct + lane) * cs + cl - 1];
+    l1 = f.rec[2][(size_t)(ct + lane) * cs + cl - 1];
+  }
+  if (chromaRes)
+#pragma unroll
+    for (int q = 0; q < 4; q++) S.res[256 + lane + 32 * q] = rv[q];
+  if (haveT) {
+    S.areaC[0][lane] = t0;
+    S.areaC[1][lane] = t1;
+  }
+  if (haveL) {
+    S.areaC[0][(1 + lane) * 16] = l0;
+    S.areaC[1][(1 + lane) * 16] = l1;
   }
   __syncwarp();
   const int cmode = r.cmode();
