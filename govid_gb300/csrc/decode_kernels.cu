@@ -913,27 +913,33 @@ __global__ void __launch_bounds__(32 * kInterWarps, 6) kInterRecon(const FrameDe
   const uint8_t* const* refp = golden ? v.gold : v.ref;
   const int part = mode == kRecInter ? r.part() : partWhole;
   const int cbp = mode == kRecInter ? r.cbp() : 0;
+  bool deferred = false;  // phase 0: left to phase 1, whose residual is computed now
   if (intra) {
   } else if (phase == 0) {
-    if (interDepends(f, r, mode, part, mbx, mby)) {
-      if (lane == 0) f.dep[idx] = 1;
-      return;
-    }
-    if (lane == 0 && f.prevRec) f.dep[idx] = 0;
+    deferred = interDepends(f, r, mode, part, mbx, mby);
+    if (lane == 0 && f.prevRec) f.dep[idx] = deferred ? 1 : 0;
   } else if (!f.prevRec || !f.dep[idx]) {
     return;
   }
   const uint32_t nzm = r.nzmask();
   const int tx = r.tx();
 
-  // Residuals of the coded blocks that are written, all at once.
+  // Residuals of the coded blocks that are written, all at once.  Phase 0
+  // computes those of intra and deferred macroblocks and stores them over
+  // the coefficient region (off the critical path); phase 1 reads them back.
   uint32_t resMask = intra ? nzm & wm : 0;
   if (cbp & cbpLuma) resMask |= nzm & wm & 0xFFFFu;
   if (cbp & cbpCb) resMask |= nzm & wm & (1u << 16);
   if (cbp & cbpCr) resMask |= nzm & wm & (1u << 17);
   uint32_t* const cg = v.coef + (size_t)idx * kCoefPerMB;
-  if (resMask) mbResidual(cg, tx, resMask, v.qdc, v.qac, S.res, S.tmp, lane);
-  if (intra) {
+  if (phase == 1) {
+    if (resMask)
+      for (int q = lane; q < 384; q += 32) S.res[q] = (int32_t)cg[q];
+    __syncwarp();
+  } else if (resMask) {
+    mbResidual(cg, tx, resMask, v.qdc, v.qac, S.res, S.tmp, lane);
+  }
+  if (intra || deferred) {
     if (resMask)
       for (int q = lane; q < 384; q += 32) cg[q] = (uint32_t)S.res[q];
     return;
