@@ -15,11 +15,12 @@
 //                     golden reference plus dequantized inverse DCT residual
 //                     (ebiv/quant.go:72-80, ebiv/transform.go:129-194).
 // Stage B2 kIntraRecon one CTA per tile: intra macroblocks reconstructed along
-//                     their true dependencies only, as a wavefront with a
-//                     two-macroblock lag per row (ebiv/predict.go:50-219).
+//                     their true dependencies only, a dataflow schedule over
+//                     the 4x4-block diagonal steps (ebiv/predict.go:50-219).
 //
-// Every wait is a __syncwarp/__syncthreads barrier inside one CTA; no kernel
-// spins on memory written by another CTA.
+// Waits are __syncwarp/__syncthreads barriers inside one CTA, and in
+// kIntraRecon polls of progress bytes written by warps of the same CTA, each
+// bounded (IntraSync); no kernel spins on memory written by another CTA.
 #include <cuda_runtime.h>
 
 #include <algorithm>
