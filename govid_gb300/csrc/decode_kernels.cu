@@ -1072,11 +1072,16 @@ __device__ void intraBlock(int32_t* ref, uint8_t* a, int as, int ax, int ay, uin
     __syncwarp();
     return;
   }
+  // n is 4, 8 or 16: shifts instead of divisions, and the DC sum's loads
+  // issued together (unrolled, predicated past n).
+  const int lg = n == 4 ? 2 : (n == 8 ? 3 : 4);
   int32_t dc = 0;
   if (mode == modeDC) {
     int32_t sum = 0;
-    for (int i = 0; i < n; i++) sum += ref[corner + 1 + i] + ref[corner - 1 - i];
-    dc = (sum + n) / (2 * n);
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+      if (i < n) sum += ref[corner + 1 + i] + ref[corner - 1 - i];
+    dc = (sum + n) >> (lg + 1);  // sum >= 0: the division by 2n
   }
   int angle = 0, inv = 0;
   bool vertical = false;
@@ -1091,7 +1096,7 @@ __device__ void intraBlock(int32_t* ref, uint8_t* a, int as, int ax, int ay, uin
   }
   const int nn = n * n;
   for (int o = l; o < nn; o += nl) {
-    const int r = o / n, c = o - r * n;
+    const int r = o >> lg, c = o & (n - 1);
     int32_t v;
     switch (mode) {
       case modeV: v = ref[corner + 1 + c]; break;
@@ -1215,7 +1220,7 @@ __device__ void intraLuma(const ReconView& f, IntraScratch& S, const IntraSync& 
   if (haveB) S.areaY[32] = a1;
   if (leftNow && lane < 16) S.areaY[(1 + lane) * kAreaW] = lc;
   auto block = [&](int k, int l, int nl, bool active, int half) {
-    const int bx = (k % per) * n, by = (k / per) * n;
+    const int bx = (k & (per - 1)) << (2 + tx), by = (k >> (2 - tx)) << (2 + tx);  // per = 4 >> tx, n = 4 << tx
     const int x0 = mbLeft + bx, y0 = mbTop + by;
     const bool avAbove = y0 > tileTop, avLeft = x0 > tileLeft;
     bool avAR = false;
