@@ -604,7 +604,7 @@ def main():
     ap.add_argument("--mix-lookahead", default="1,4", help="comma list: headline (latency-bounded) first")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-pipeline", action="store_true", help="synchronous rounds (no entropy/recon overlap)")
-    ap.add_argument("--pipeline-depth", type=int, default=2,
+    ap.add_argument("--pipeline-depth", type=int, default=3,
                     help="rounds planned ahead of the one reconstructing (single-stream legs)")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-mv", action="store_true")

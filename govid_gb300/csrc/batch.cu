@@ -179,6 +179,11 @@ Engine::~Engine() {
   }
   if (dOne_) cudaFree(dOne_);
   if (sideDone_) cudaEventDestroy(sideDone_);
+  if (streamC_) {
+    cudaStreamSynchronize(streamC_);
+    cudaStreamDestroy(streamC_);
+  }
+  if (copyDone_) cudaEventDestroy(copyDone_);
   if (streamB_) {
     cudaStreamSynchronize(streamB_);
     cudaStreamDestroy(streamB_);
@@ -214,7 +219,10 @@ int Engine::init(cudaStream_t s) {
   for (auto& row : ev_)
     for (auto& e : row)
       if (cudaEventCreate(&e) != cudaSuccess) return kErrDevice;
-  if (cudaStreamCreateWithFlags(&streamB_, cudaStreamNonBlocking) != cudaSuccess) return kErrDevice;
+  if (cudaStreamCreateWithFlags(&streamB_, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&streamC_, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&copyDone_, cudaEventDisableTiming) != cudaSuccess)
+    return kErrDevice;
   for (int p = 0; p < kMainParities; p++) {
     if (cudaEventCreateWithFlags(&evUp_[p], cudaEventDisableTiming) != cudaSuccess) return kErrDevice;
     for (auto& e : evGroup_[p])  // timed: the entropy time of a grouped round ends at its last group
@@ -328,10 +336,20 @@ int Engine::downloadFrameAsync(const EngineFrameView& v, uint8_t* packed, size_t
   uint8_t* y = packed;
   uint8_t* cb = packed + (size_t)v.width * v.height;
   uint8_t* cr = cb + (size_t)cw * ch;
-  if (cudaMemcpy2DAsync(y, v.width, v.y, v.yStride, v.width, v.height, cudaMemcpyDeviceToHost, stream_) ||
-      cudaMemcpy2DAsync(cb, cw, v.cb, v.cStride, cw, ch, cudaMemcpyDeviceToHost, stream_) ||
-      cudaMemcpy2DAsync(cr, cw, v.cr, v.cStride, cw, ch, cudaMemcpyDeviceToHost, stream_))
+  // A returned frame is complete (its round was collected), so the copy waits
+  // for nothing; device work of later rounds waits for copyDone_.
+  if (cudaMemcpy2DAsync(y, v.width, v.y, v.yStride, v.width, v.height, cudaMemcpyDeviceToHost, streamC_) ||
+      cudaMemcpy2DAsync(cb, cw, v.cb, v.cStride, cw, ch, cudaMemcpyDeviceToHost, streamC_) ||
+      cudaMemcpy2DAsync(cr, cw, v.cr, v.cStride, cw, ch, cudaMemcpyDeviceToHost, streamC_) ||
+      cudaEventRecord(copyDone_, streamC_))
     return kErrDevice;
+  copiesPending_ = true;
+  return kOK;
+}
+
+int Engine::syncCopies() {
+  if (cudaStreamSynchronize(streamC_) != cudaSuccess) return kErrDevice;
+  copiesPending_ = false;
   return kOK;
 }
 
@@ -616,6 +634,9 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
   cudaStream_t se = entropyStream(P);
   cudaStream_t sr = reconStream(P);
   planStream_ = sr;
+  // Frame-buffer writes of this round (raw frames, override copies, the
+  // reconstruction) come after every queued download.
+  if (copiesPending_ && cudaStreamWaitEvent(sr, copyDone_, 0) != cudaSuccess) return -1;
   for (size_t ii = 0; ii < ids.size(); ii++) {
     const int id = ids[ii];
     if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) continue;
@@ -940,6 +961,7 @@ int Engine::launchRecon(Round& R) {
   const bool grouped = R.groups > 1;
   auto entropyDone = [&](int st) { return grouped ? evGroup_[P][st / R.stepsPerGroup] : ev_[P][1]; };
   if (cudaStreamWaitEvent(sr, entropyDone(0), 0) != cudaSuccess) return -1;
+  if (copiesPending_ && cudaStreamWaitEvent(sr, copyDone_, 0) != cudaSuccess) return -1;
   int groupA = 0, groupB = -1;
   const FrameDesc* dd = reinterpret_cast<const FrameDesc*>(d + R.oDesc);
   const int2* dj = reinterpret_cast<const int2*>(d + R.oJobs);
@@ -1341,7 +1363,7 @@ int ebivgpu_batch_result_download_async(ebivgpu_batch* b, int i, uint8_t* packed
 
 int ebivgpu_batch_sync(ebivgpu_batch* b) {
   if (!b) return kErrArg;
-  return cudaStreamSynchronize(b->e.stream()) == cudaSuccess ? kOK : kErrDevice;
+  return b->e.syncCopies();
 }
 
 int ebivgpu_batch_reload_stream(ebivgpu_batch* b, int stream_id, const uint8_t* const* pkts, const size_t* lens,

@@ -81,10 +81,10 @@ class Engine {
   // stream, collects the round in flight (whose results it returns) and then
   // launches the new round's reconstruction, so one round's entropy overlaps
   // the previous round's reconstruction.  drain() collects the last round.
-  // depth 2 keeps two rounds ahead of the one reconstructing: a round's
-  // entropy stage starts two round() calls before its reconstruction, and a
-  // round's results come back two calls after it was planned.  depth 0 is
-  // the synchronous engine.
+  // depth D keeps D rounds in flight: a round's entropy stage starts D - 1
+  // round() calls before its reconstruction, and its results come back D
+  // calls after it was planned.  depth 0 is the synchronous engine; at most
+  // kMaxDepth.
   int setPipelined(int depth);
   bool pipelined() const { return pipeDepth_ > 0; }
   int pipeDepth() const { return pipeDepth_; }
@@ -101,8 +101,11 @@ class Engine {
   int collectSide(std::vector<RoundResult>* results);
 
   int downloadFrame(const EngineFrameView& v, uint8_t* packed, size_t cap);
-  // Queues the copy on the engine's stream; complete after the stream syncs.
+  // Queues the copy on the engine's copy stream, beside the reconstruction;
+  // complete after syncCopies().  Later rounds' device work waits for it
+  // before touching frame buffers.
   int downloadFrameAsync(const EngineFrameView& v, uint8_t* packed, size_t cap);
+  int syncCopies();
   // New packets for a resident stream (its frame pool is kept); no round may
   // be in flight.
   int reloadStream(int id, const uint8_t* const* pkts, const size_t* lens, int n);
@@ -143,7 +146,7 @@ class Engine {
   int mainSets() const { return pipeDepth_ + 1; }
   int slotSet(int parity) const { return parity == kSide ? mainSets() : parity; }
   int slotSets() const { return mainSets() + (side_ ? 1 : 0); }
-  static constexpr int kMaxDepth = 2;
+  static constexpr int kMaxDepth = 3;
   static constexpr int kMainParities = kMaxDepth + 1;  // main rounds in flight at most
   static constexpr int kSide = kMainParities;
   static constexpr int kParities = kMainParities + 1;
@@ -153,6 +156,10 @@ class Engine {
   cudaStream_t streamES_ = nullptr, streamRS_ = nullptr;  // side lane: entropy, reconstruction
   cudaStream_t planStream_ = nullptr;  // reconstruction stream of the round being planned
   cudaEvent_t sideDone_ = nullptr;
+  // Copy stream of downloadFrameAsync and the event after its last copy.
+  cudaStream_t streamC_ = nullptr;
+  cudaEvent_t copyDone_ = nullptr;
+  bool copiesPending_ = false;
   // Entropy groups of pipelined main rounds: a pool of streams the groups
   // take in turn (so the groups of consecutive rounds run side by side), the
   // staging-upload event and one completion event per group.

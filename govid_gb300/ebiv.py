@@ -207,11 +207,11 @@ class Batch:
     next packet of every active stream with one set of kernel launches."""
 
     def __init__(self, lookahead: int = 1, pipeline: bool | int = False):
-        """pipeline (True or a depth of 1 or 2): each round() plans a round
+        """pipeline (True or a depth of 1 to 3): each round() plans a round
         and starts its entropy stage while earlier rounds reconstruct, and
         returns the results of the round planned `depth` calls before; drain()
         returns those of the rounds still in flight (resident streams only).
-        Depth 2 starts a round's entropy stage one round earlier."""
+        Each extra level starts a round's entropy stage one round earlier."""
         L = _native.lib()
         h = C.c_void_p()
         _check(L.ebivgpu_batch_create(C.byref(h)), "batch")

@@ -119,12 +119,12 @@ int ebivgpu_batch_set_lookahead(ebivgpu_batch* b, int frames);
 /* Pipelined rounds (set before adding streams; resident streams only).
  * depth 1: each ebivgpu_batch_round starts the new round's entropy stage,
  * collects the round in flight and returns ITS results, so one round's
- * entropy overlaps the previous round's reconstruction.  depth 2: rounds are
- * planned two calls ahead of their reconstruction, so a round's entropy stage
- * has the two previous rounds' reconstruction to run under, and a call
- * returns the results of the round planned two calls before.  depth 0: the
- * synchronous rounds.  ebivgpu_batch_drain collects every round in flight.
- * Results and frame order per stream are those of the synchronous rounds. */
+ * entropy overlaps the previous round's reconstruction.  depth D (2 or 3):
+ * rounds are planned D calls ahead of their results, so a round's entropy
+ * stage has the D previous rounds' reconstruction to run under.  depth 0:
+ * the synchronous rounds.  ebivgpu_batch_drain collects every round in
+ * flight.  Results and frame order per stream are those of the synchronous
+ * rounds. */
 int ebivgpu_batch_set_pipeline(ebivgpu_batch* b, int depth);
 /* Replaces a resident stream's packets with a new clip of the same size
  * (starting with a key frame) and rewinds it; its frame pool is kept.  No

@@ -38,7 +38,7 @@ def _streams():
     return out
 
 
-@pytest.mark.parametrize("lookahead,pipeline", [(1, False), (4, False), (1, True), (4, True), (1, 2), (4, 2)])
+@pytest.mark.parametrize("lookahead,pipeline", [(1, False), (4, False), (1, True), (4, True), (1, 2), (4, 2), (4, 3)])
 def test_batch_matches_oracle(gpu_required, lookahead, pipeline):
     streams = _streams()
     b = ebiv.Batch(lookahead=lookahead, pipeline=pipeline)
@@ -183,7 +183,7 @@ def test_fuzzed_packets_match_oracle(gpu_required):
             assert g[1] == want[i][1], f"case {case} frame {i}: planes differ from the oracle"
 
 
-@pytest.mark.parametrize("lookahead,depth", [(1, 1), (3, 1), (3, 2)])
+@pytest.mark.parametrize("lookahead,depth", [(1, 1), (3, 1), (3, 2), (2, 3)])
 def test_fuzzed_streams_pipelined_batch_match_oracle(gpu_required, lookahead, depth):
     # Corrupted packets in several streams decoded together by a pipelined
     # batch: every status and plane equals the oracle decoding each stream
@@ -221,3 +221,40 @@ def test_fuzzed_streams_pipelined_batch_match_oracle(gpu_required, lookahead, de
             assert (sid, i) in got, f"stream {sid} frame {i} never delivered"
             assert got[(sid, i)][0] == ws, f"stream {sid} frame {i}: status {got[(sid, i)][0]} vs {ws}"
             assert got[(sid, i)][1] == wp, f"stream {sid} frame {i} differs from the oracle"
+
+
+def test_async_downloads_of_a_deep_pipeline_match_oracle(gpu_required):
+    # Every result of a depth-3 pipelined batch queued into pinned host memory
+    # on the engine's copy stream while later rounds decode: after sync() each
+    # frame equals the oracle (later rounds never overwrite a frame whose copy
+    # is still queued).
+    torch = pytest.importorskip("torch")
+    streams = _streams()
+    b = ebiv.Batch(lookahead=4, pipeline=3)
+    want, dims = {}, {}
+    for cont, w, h in streams:
+        pkts = [p.data for p in ebiv.Reader(cont).packets()]
+        sid = b.add_stream(pkts, ring=3)
+        dims[sid] = (w, h)
+        want[sid] = ebiv_oracle.decode_all(pkts)
+    total = sum(ebiv_frame_bytes(*dims[s]) * len(want[s]) for s in want)
+    host = torch.empty(total, dtype=torch.uint8, pin_memory=True)
+    placed, off = [], 0
+    for r in run_rounds(b):
+        ws, _ = want[r.stream][r.frame_index]
+        assert r.status == ws
+        if ws != 0:
+            continue
+        n = ebiv_frame_bytes(*dims[r.stream])
+        b.download_async(r, host.data_ptr() + off, n)
+        placed.append((r.stream, r.frame_index, off, n))
+        off += n
+    b.sync()
+    data = host.numpy().tobytes()
+    assert placed
+    for sid, i, o, n in placed:
+        assert data[o:o + n] == want[sid][i][1], f"stream {sid} frame {i} differs from the oracle"
+
+
+def ebiv_frame_bytes(w, h):
+    return w * h + 2 * ((w + 1) // 2) * ((h + 1) // 2)
