@@ -403,17 +403,24 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def all_rounds(b, lat=None):
+def all_rounds(b, lat=None, frame_lat=None):
     """Every result of a batch until its streams are exhausted.  A pipelined
     round returns the results of the round planned b.depth calls before, so
     stop after depth + 1 empty rounds and collect the rounds in flight.  lat
-    gets each call's wall time."""
+    gets the wall time of each call that returned results; frame_lat gets,
+    per returned frame, the wall time from the start of the call that planned
+    it to the end of the call that returned it."""
     empty = 0
+    starts = []
     while empty < b.depth + 1:
         t = time.perf_counter()
+        starts.append(t)
         res = b.round()
+        t1 = time.perf_counter()
         if lat is not None and res:
-            lat.append(time.perf_counter() - t)
+            lat.append(t1 - t)
+        if frame_lat is not None and res:
+            frame_lat.extend([t1 - starts[max(0, len(starts) - 1 - b.depth)]] * len(res))
         empty = empty + 1 if not res else 0
         yield from res
     yield from b.drain()
@@ -441,8 +448,10 @@ def run_batched(args):
     except Exception:
         pass
 
+    depth = 0 if args.no_pipeline else args.mix_depth
+
     def one(lookahead):
-        b = ebiv.Batch(lookahead=lookahead, pipeline=not args.no_pipeline)
+        b = ebiv.Batch(lookahead=lookahead, pipeline=depth)
         ids = [b.add_stream(pk, ring=3) for pk in pkts]
         for sid in ids:  # warm-up round
             b.seek(sid, 0)
@@ -451,12 +460,12 @@ def run_batched(args):
         for sid in ids:
             b.seek(sid, 0)
         flush_l2()
-        lat = []
+        lat, flat = [], []
         torch.cuda.synchronize()
         b.timing(1)
         ts = time.perf_counter()
         frames = 0
-        for r in all_rounds(b, lat):
+        for r in all_rounds(b, lat, flat):
             frames += 1
             if r.status != 0:
                 raise RuntimeError(f"batched decode failed: {r}")
@@ -469,6 +478,8 @@ def run_batched(args):
                 "frames_1080p_equiv_per_s": round(fps * (px / totals) / (W * H), 2),
                 "round_latency_ms": {"p50": round(1000 * statistics.median(lat), 3),
                                      "p99": round(1000 * sorted(lat)[int(0.99 * (len(lat) - 1))], 3)},
+                "frame_latency_ms": {"p50": round(1000 * statistics.median(flat), 3),
+                                     "p99": round(1000 * sorted(flat)[int(0.99 * (len(flat) - 1))], 3)},
                 "hbm_gbs_over_kernel_time": round(hbm, 2), "hbm_frac": round(hbm / peak, 4)}
 
     runs = [one(int(k)) for k in str(args.mix_lookahead).split(",")]
@@ -491,7 +502,7 @@ def run_batched(args):
     for r in runs:
         r["speedup_vs_one_stream_per_launch"] = round(r["frames_per_s"] / per_stream_fps, 3)
     out = {"streams": len(streams), "distinct_bitstreams": len({id(c) for _, _, c in streams}),
-           "pipelined_rounds": not args.no_pipeline, "frames_per_stream": args.mix_frames,
+           "pipeline_depth": depth, "frames_per_stream": args.mix_frames,
            "one_stream_per_launch_frames_per_s": round(per_stream_fps, 2)}
     out.update(runs[0])
     if len(runs) > 1:
@@ -604,6 +615,7 @@ def main():
     ap.add_argument("--mix-lookahead", default="1,4", help="comma list: headline (latency-bounded) first")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-pipeline", action="store_true", help="synchronous rounds (no entropy/recon overlap)")
+    ap.add_argument("--mix-depth", type=int, default=2, help="pipeline depth of the 64-stream rounds")
     ap.add_argument("--pipeline-depth", type=int, default=3,
                     help="rounds planned ahead of the one reconstructing (single-stream legs)")
     ap.add_argument("--no-serve", action="store_true")
