@@ -873,6 +873,19 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
     if (j.ovDesc >= 0)
       fill(j, j.ov, j.ovDesc, j.ovBuf, j.work, j.work, true, j.mainDesc, s.slots[(size_t)ovSlot], nullptr);
   }
+  {
+    // Each intra launch takes its tiles largest first, so a large tile never
+    // starts in a late wave.
+    auto tileMBs = [&](const int2& jb) {
+      const TileRange& t = planOf[(size_t)jb.x]->tiles[(size_t)jb.y];
+      return (int)(t.mbX1 - t.mbX0) * (int)(t.mbY1 - t.mbY0);
+    };
+    auto larger = [&](const int2& a, const int2& b) { return tileMBs(a) > tileMBs(b); };
+    for (const StepInfo& si : R.steps) {
+      std::stable_sort(hj + si.jobFirst, hj + si.jobFirst + si.jobCount, larger);
+      std::stable_sort(hj + si.ovJobFirst, hj + si.ovJobFirst + si.ovJobCount, larger);
+    }
+  }
   int groupFirst[kEntropyGroups + 1] = {0};
   {
     // By group, then longest tile first, so the slowest chains start in the
