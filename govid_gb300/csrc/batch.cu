@@ -184,6 +184,10 @@ Engine::~Engine() {
     cudaStreamDestroy(streamC_);
   }
   if (copyDone_) cudaEventDestroy(copyDone_);
+  if (reloadDone_) {
+    cudaEventSynchronize(reloadDone_);
+    cudaEventDestroy(reloadDone_);
+  }
   if (streamB_) {
     cudaStreamSynchronize(streamB_);
     cudaStreamDestroy(streamB_);
@@ -221,7 +225,8 @@ int Engine::init(cudaStream_t s) {
       if (cudaEventCreate(&e) != cudaSuccess) return kErrDevice;
   if (cudaStreamCreateWithFlags(&streamB_, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&streamC_, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&copyDone_, cudaEventDisableTiming) != cudaSuccess)
+      cudaEventCreateWithFlags(&copyDone_, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&reloadDone_, cudaEventDisableTiming) != cudaSuccess)
     return kErrDevice;
   for (int p = 0; p < kMainParities; p++) {
     if (cudaEventCreateWithFlags(&evUp_[p], cudaEventDisableTiming) != cudaSuccess) return kErrDevice;
@@ -323,6 +328,9 @@ int Engine::reloadStream(int id, const uint8_t* const* pkts, const size_t* lens,
     if (lens[i] &&
         cudaMemcpyAsync(s.dPkts + s.dOff[(size_t)i], pkts[i], lens[i], cudaMemcpyHostToDevice, se) != cudaSuccess)
       return kErrDevice;
+  // syncCopies() waits for this event: after it the caller may reuse pkts.
+  if (cudaEventRecord(reloadDone_, se) != cudaSuccess) return kErrDevice;
+  reloadPending_ = true;
   s.next = 0;
   s.hasProv = false;
   s.epoch++;
@@ -350,6 +358,8 @@ int Engine::downloadFrameAsync(const EngineFrameView& v, uint8_t* packed, size_t
 int Engine::syncCopies() {
   if (cudaStreamSynchronize(streamC_) != cudaSuccess) return kErrDevice;
   copiesPending_ = false;
+  if (reloadPending_ && cudaEventSynchronize(reloadDone_) != cudaSuccess) return kErrDevice;
+  reloadPending_ = false;
   return kOK;
 }
 

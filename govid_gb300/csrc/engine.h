@@ -160,6 +160,8 @@ class Engine {
   cudaStream_t streamC_ = nullptr;
   cudaEvent_t copyDone_ = nullptr;
   bool copiesPending_ = false;
+  cudaEvent_t reloadDone_ = nullptr;  // the last reloadStream's host-to-device copies
+  bool reloadPending_ = false;
   // Entropy groups of pipelined main rounds: a pool of streams the groups
   // take in turn (so the groups of consecutive rounds run side by side), the
   // staging-upload event and one completion event per group.

@@ -1,8 +1,12 @@
 // C-ABI over the host tools: encoder, demuxer, synthetic scenes.
+#include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <new>
+#include <thread>
 
 #include "../../include/ebiv_host.h"
 #include "container.h"
@@ -286,24 +290,169 @@ int ebiv_scene_render(ebiv_scene* s, int frame, uint8_t* packed, size_t cap) {
 
 void ebiv_scene_destroy(ebiv_scene* s) { delete s; }
 
+namespace {
+
+int copyOut(const std::vector<uint8_t>& v, uint8_t** out, size_t* n) {
+  *n = v.size();
+  *out = (uint8_t*)std::malloc(*n ? *n : 1);
+  if (!*out) return kErrArg;
+  std::memcpy(*out, v.data(), *n);
+  return kOK;
+}
+
+// Runs fn(0..count-1) on up to `workers` threads.
+void fanOut(int count, int workers, const std::function<void(int)>& fn) {
+  std::atomic<int> next{0};
+  auto loop = [&] {
+    for (int i; (i = next.fetch_add(1)) < count;) fn(i);
+  };
+  std::vector<std::thread> ts;
+  for (int k = 1; k < std::min(workers, count); k++) ts.emplace_back(loop);
+  loop();
+  for (auto& t : ts) t.join();
+}
+
+// The first frame of every GOP the serial encoder would close, from its own
+// two rules (Encoder::writeFrame, after ebiv/encoder.go:189-227): a scene cut
+// (luma SAD against the previous frame above 28 per pixel) ends a GOP of at
+// least 8 pending frames, and a GOP ends when it holds `gop` frames.  The
+// per-frame cut tests run in parallel; each worker renders its run of frames
+// in order, so every frame is rendered about once.
+std::vector<int> gopStarts(const Scene& scene, int frames, int gop, int workers) {
+  std::vector<uint8_t> cut((size_t)frames, 0);
+  const int runs = std::max(1, std::min(workers * 2, frames));
+  fanOut(runs, workers, [&](int r) {
+    const int a = (int)((int64_t)frames * r / runs), b = (int)((int64_t)frames * (r + 1) / runs);
+    PackedImage prev, cur;
+    if (a > 0) scene.render(a - 1, prev);
+    for (int i = a; i < b; i++) {
+      scene.render(i, cur);
+      if (i > 0) {
+        int64_t sad = 0;
+        for (size_t k = 0; k < cur.Y.size(); k++) sad += std::abs((int32_t)cur.Y[k] - (int32_t)prev.Y[k]);
+        cut[i] = sad > (int64_t)cur.W * cur.H * 28;
+      }
+      std::swap(prev, cur);
+    }
+  });
+  std::vector<int> starts{0};
+  int pending = 0;
+  for (int i = 0; i < frames; i++) {
+    if (i > 0 && cut[i] && pending >= 8) {
+      starts.push_back(i);
+      pending = 0;
+    }
+    if (++pending >= gop) {
+      if (i + 1 < frames) starts.push_back(i + 1);
+      pending = 0;
+    }
+  }
+  return starts;
+}
+
+// The frame records of an encoder's container: the bytes between the file
+// header and the index.
+bool frameRecords(const std::vector<uint8_t>& c, const uint8_t** p, size_t* n) {
+  if (c.size() < (size_t)kFileHeaderSize + kFooterSize) return false;
+  uint64_t idx = 0;
+  for (int k = 7; k >= 0; k--) idx = idx << 8 | c[c.size() - kFooterSize + k];
+  if (idx < (uint64_t)kFileHeaderSize || idx > c.size()) return false;
+  *p = c.data() + kFileHeaderSize;
+  *n = (size_t)idx - kFileHeaderSize;
+  return true;
+}
+
+}  // namespace
+
+// GOPs are independent in the encoder (each key frame starts from empty
+// reference and table state, Encoder::flushGOP), so a clip is encoded GOP by
+// GOP on concurrent encoders and the frame records are joined into one
+// container: the output equals the serial encoder's byte for byte.  Each GOP
+// encoder fans its tiles out over its share of the threads.
 int ebiv_encode_scene(const int64_t* spec, int frames, const ebiv_encoder_options* o, uint8_t** out, size_t* n) {
   if (!spec || !o || !out || !n || frames < 0) return kErrArg;
   Scene scene(toSpec(spec));
-  Encoder enc(toOptions(o));
-  if (enc.status() != kOK) return enc.status();
-  PackedImage im;
-  for (int i = 0; i < frames; i++) {
-    scene.render(i, im);
-    const int st = enc.writeFrame(im);
+  const EncoderOptions opt = toOptions(o);
+  const int threads = std::max(1, opt.threads);
+  const bool gopParallel = opt.coded && !opt.keepRecon && opt.search != SearchMode::Proposed && frames > 1 &&
+                           threads > 1;
+  if (!gopParallel) {
+    Encoder enc(opt);
+    if (enc.status() != kOK) return enc.status();
+    PackedImage im;
+    for (int i = 0; i < frames; i++) {
+      scene.render(i, im);
+      const int st = enc.writeFrame(im);
+      if (st != kOK) return st;
+    }
+    const int st = enc.close();
     if (st != kOK) return st;
+    return copyOut(enc.output(), out, n);
   }
-  const int st = enc.close();
-  if (st != kOK) return st;
-  *n = enc.output().size();
-  *out = (uint8_t*)std::malloc(*n ? *n : 1);
-  if (!*out) return kErrArg;
-  std::memcpy(*out, enc.output().data(), *n);
-  return kOK;
+  {
+    Encoder probe(opt);
+    if (probe.status() != kOK) return probe.status();
+  }
+  const std::vector<int> starts = gopStarts(scene, frames, opt.gop, threads);
+  const int gops = (int)starts.size();
+  const int cols = opt.withTilesCols >= 0 ? opt.withTilesCols : opt.tileCols;
+  const int rows = opt.withTilesRows >= 0 ? opt.withTilesRows : opt.tileRows;
+  const int tiles = std::max(1, std::max(cols, 1) * std::max(rows, 1));
+  const int perGop = std::max(1, std::min(threads, tiles));
+  const int conc = std::max(1, std::min(gops, threads / perGop));
+  EncoderOptions gopOpt = opt;
+  gopOpt.threads = perGop;
+  std::vector<std::vector<uint8_t>> parts((size_t)gops);
+  std::vector<int> status((size_t)gops, kOK);
+  fanOut(gops, conc, [&](int g) {
+    const int a = starts[g], b = g + 1 < gops ? starts[g + 1] : frames;
+    Encoder enc(gopOpt);
+    PackedImage im;
+    int st = enc.status();
+    for (int i = a; i < b && st == kOK; i++) {
+      scene.render(i, im);
+      st = enc.writeFrame(im);
+    }
+    if (st == kOK) st = enc.close();
+    status[g] = st;
+    if (st == kOK) parts[g] = enc.output();
+  });
+  for (int s : status)
+    if (s != kOK) return s;
+  // Join: the first part's file header, every part's frame records, then a
+  // new index (offsets shifted) and footer (ebiv/writer.go:92-119).
+  std::vector<uint8_t> c(parts[0].begin(), parts[0].begin() + kFileHeaderSize);
+  for (const auto& part : parts) {
+    const uint8_t* p;
+    size_t len;
+    if (!frameRecords(part, &p, &len)) return kErrConfig;
+    c.insert(c.end(), p, p + len);
+  }
+  const uint64_t indexOffset = c.size();
+  std::vector<uint8_t> idx;
+  uint32_t count = 0;
+  for (size_t off = kFileHeaderSize; off + kFrameRecordSize <= indexOffset; count++) {
+    const uint32_t flags = (uint32_t)c[off + 2] | (uint32_t)c[off + 3] << 8;
+    const uint32_t size = (uint32_t)c[off + 4] | (uint32_t)c[off + 5] << 8 | (uint32_t)c[off + 6] << 16 |
+                          (uint32_t)c[off + 7] << 24;
+    uint8_t e[kIndexEntrySize];
+    wr64(e, off);
+    wr32(e + 8, size);
+    wr32(e + 12, flags & 1u);
+    idx.insert(idx.end(), e, e + kIndexEntrySize);
+    off += kFrameRecordSize + size;
+  }
+  c.insert(c.end(), idx.begin(), idx.end());
+  uint8_t footer[kFooterSize];
+  wr64(footer, indexOffset);
+  wr32(footer + 8, count);
+  wr32(footer + 12, crc32IEEE(idx.data(), idx.size()));
+  footer[16] = 'E';
+  footer[17] = 'B';
+  footer[18] = 'I';
+  footer[19] = 'X';
+  c.insert(c.end(), footer, footer + kFooterSize);
+  return copyOut(c, out, n);
 }
 
 void ebiv_free(void* p) { std::free(p); }

@@ -57,6 +57,7 @@ constexpr size_t kOffIntra = a256(kOffLV + (size_t)kNAMaxMBs * sizeof(int16_t));
 constexpr size_t kOffTS = a256(kOffIntra + 2 * (size_t)kNAMaxMBs * sizeof(uint32_t));
 constexpr size_t kOffPkt = a256(kOffTS + (size_t)kNAMaxMBs * sizeof(TileStat));
 constexpr size_t kNABytes = a256(kOffPkt + kNAMaxPacket);
+static_assert(kNABytes == EBIVGPU_NOALLOC_SCRATCH_BYTES, "the header states the scratch size");
 static_assert(kNABytes < (16u << 20), "the no-allocation scratch stays modest");
 
 }  // namespace
@@ -183,6 +184,9 @@ extern "C" int ebivgpu_decode_key_noalloc(const uint8_t* pkt, size_t n, uint8_t*
   if (fh.goldenOverride) ovPlan = planPayload(pkt, ovOff, ovLen, false, g.mbCols, g.mbRows, hist, &plan[1]);
   const bool withOv = fh.goldenOverride && ovPlan == kOK;
 
+  // An error left pending by earlier work of the caller is not this call's:
+  // fail before launching, without clearing it, so launch errors below are ours.
+  if (cudaPeekAtLastError() != cudaSuccess) return kErrDevice;
   uint8_t* d = nullptr;
   st = noAllocSetup(&d);
   if (st) return st;
@@ -223,12 +227,19 @@ extern "C" int ebivgpu_decode_key_noalloc(const uint8_t* pkt, size_t n, uint8_t*
     maxTile = std::max(maxTile, w * h);
     maxKeys = std::max(maxKeys, 4 * (w - 1) + 11 * (h - 1) + 1);
   }
+  // Each launch is checked where it is made.
   launchEntropy(dd, de, groups(nt0), nullptr, s);
+  if (cudaGetLastError() != cudaSuccess) return kErrDevice;
   launchInter(dd, 1, (int)mbs, 0, s);  // the intra macroblocks' residuals
+  if (cudaGetLastError() != cudaSuccess) return kErrDevice;
   launchIntra(dd, dj, nt0, maxTile, maxKeys, s);
-  if (withOv) launchEntropy(dd, de + kNAMaxEJobs, groups((int)plan[1].tiles.size()), nullptr, s);  // after the key's recon
+  if (cudaGetLastError() != cudaSuccess) return kErrDevice;
+  if (withOv) {  // after the key's reconstruction, which reads the records it overwrites
+    launchEntropy(dd, de + kNAMaxEJobs, groups((int)plan[1].tiles.size()), nullptr, s);
+    if (cudaGetLastError() != cudaSuccess) return kErrDevice;
+  }
   if (cudaMemcpyAsync(status, d + kOffStatus, sizeof(status), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+      cudaStreamSynchronize(s) != cudaSuccess)
     return kErrDevice;
   // Status order of the stateful codec: the key's own, then the override's plan, then its decode.
   if (status[0]) return status[0];

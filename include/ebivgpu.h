@@ -1,9 +1,9 @@
 /*
  * ebivgpu — GB300 (sm_103a) EBIV decoder, C-ABI drop-in boundary.
  *
- * These entry points are what a cgo binding of govid's Codec contract calls
- * (see INTEGRATION.md for the Go side).  Plain pointers and sizes only; no
- * exceptions cross the boundary; every call returns an ebiv status code.
+ * These entry points are what a cgo binding of govid's Codec contract calls.
+ * Plain pointers and sizes only; no exceptions cross the boundary; every call
+ * returns an ebiv status code.
  *
  * Reference interfaces replaced (govid, paths relative to its root):
  *   ebivgpu_create   <- ebiv.NewCodec(WithFrameRing(n))  ebiv/codec.go:48-64
@@ -129,11 +129,14 @@ int ebivgpu_batch_set_pipeline(ebivgpu_batch* b, int depth);
 /* Replaces a resident stream's packets with a new clip of the same size
  * (starting with a key frame) and rewinds it; its frame pool is kept.  No
  * round may be in flight (drain first); the copies from pkts (pinned memory
- * makes them asynchronous) complete before the next round's decode. */
+ * makes them asynchronous) complete before the next round's decode.  The
+ * pkts buffers must stay unchanged until ebivgpu_batch_sync returns (or the
+ * batch is destroyed). */
 int ebivgpu_batch_reload_stream(ebivgpu_batch* b, int stream_id, const uint8_t* const* pkts, const size_t* lens,
                                 int n);
 /* Queues a result's packed-plane copy to host memory without waiting;
- * ebivgpu_batch_sync waits for every queued copy.  A result's frame stays
+ * ebivgpu_batch_sync waits for every queued copy and for the copies of the
+ * last ebivgpu_batch_reload_stream.  A result's frame stays
  * valid until `ring` newer frames of its stream are returned. */
 int ebivgpu_batch_result_download_async(ebivgpu_batch* b, int index, uint8_t* packed, size_t cap);
 int ebivgpu_batch_sync(ebivgpu_batch* b);
@@ -191,8 +194,10 @@ uint64_t ebivgpu_frame_hash(const uint8_t* packed, size_t n);
  *
  * Decodes one key-frame packet, as the first frame of a fresh stream (the
  * result and status equal ebivgpu_decode's on a new codec), into the caller's
- * device planes.  All scratch is one static device array of 8,461,312 bytes
- * per device, so frames are limited to EBIVGPU_NOALLOC_MAX_MBS macroblocks
+ * device planes.  All scratch is one static device array of
+ * EBIVGPU_NOALLOC_SCRATCH_BYTES (8,490,240) bytes per device, held by every
+ * device that loads the library until the process exits, so frames are
+ * limited to EBIVGPU_NOALLOC_MAX_MBS macroblocks
  * (1280x720) and packets to EBIVGPU_NOALLOC_MAX_PACKET bytes; larger ones
  * return EBIV_ERR_TOO_LARGE.  The planes must cover the macroblock-aligned
  * frame: y_stride >= 16*ceil(W/16) and y_cap >= y_stride*16*ceil(H/16);
@@ -205,9 +210,12 @@ uint64_t ebivgpu_frame_hash(const uint8_t* packed, size_t n);
  *
  * The first call on a device resolves the scratch's address and uploads the
  * decoder's constant tables; make it before any stream capture.  Calls that
- * overlap in time on one device share the scratch and race: serialise them. */
+ * overlap in time on one device share the scratch and race: serialise them.
+ * A CUDA error already pending in the calling thread makes the call return
+ * EBIV_ERR_DEVICE before it launches anything, leaving that error in place. */
 #define EBIVGPU_NOALLOC_MAX_MBS 3600
 #define EBIVGPU_NOALLOC_MAX_PACKET (2u << 20)
+#define EBIVGPU_NOALLOC_SCRATCH_BYTES 8490240u
 int ebivgpu_decode_key_noalloc(const uint8_t* pkt, size_t n, uint8_t* y, int32_t y_stride, size_t y_cap, uint8_t* cb,
                                uint8_t* cr, int32_t c_stride, size_t c_cap, void* cuda_stream, int32_t* width,
                                int32_t* height);

@@ -2,8 +2,9 @@
 all scratch in a static device array equal the stateful codec's first frame
 (ebivgpu_decode on a new codec) and the oracle, for two different streams
 decoded back to back through the one scratch, including an alt-ref key packet
-whose golden override is checked too.  Size limits are refused with their own
-status before any device work.
+whose golden override is checked too, and a frame at the limits (3600
+macroblocks, 3600 tiles per payload, a packet near 2 MiB).  Size limits are
+refused with their own status before any device work.
 
 This file is named to be collected last: the entry point's first call on a
 device does its setup, and it must work after every other test has run."""
@@ -109,6 +110,25 @@ def test_consecutive_key_frames_of_one_stream(gpu_required):
     for p in keys:
         st, got = _noalloc(p)
         assert (st, got) == _codec_first(p)
+
+
+@pytest.mark.gpu
+def test_at_the_limits_3600_macroblocks_3600_tiles_near_2mib(gpu_required):
+    # The far end of every scratch region: a 1280x720 key frame (exactly the
+    # 3600-macroblock limit) coded as 80x45 one-macroblock tiles at q2, with an
+    # alt-ref override payload (its own 3600 tiles), in one 1.86 MB packet.
+    from helpers import encode_gen, noisy_gen
+
+    cont, _, _ = encode_gen(1280, 720, 8, noisy_gen, intra=2, gop=8, altref=4, tiles=(80, 45), threads=8,
+                            keep_recon=False, fast=True)
+    p = next(iter(ebiv.Reader(cont).packets())).data
+    hdr = ebiv.parse_frame_header(p)
+    assert hdr["golden_override"] and (hdr["width"], hdr["height"]) == (1280, 720)
+    assert 1_700_000 < len(p) <= 2 << 20
+    want = _codec_first(p)
+    assert want[0] == 0 and want[1] == ebiv_oracle.decode_all([p])[0][1]
+    for _ in range(2):  # two calls in a row through the one scratch
+        assert _noalloc(p) == want
 
 
 def test_size_limits_and_frame_types_are_refused_before_device_work():
