@@ -81,6 +81,8 @@ def lib() -> C.CDLL:
     _sig(L, "ebivgpu_destroy", None, P)
     _sig(L, "ebivgpu_frame_rgba", I, P, I, U8P, S)
     _sig(L, "ebivgpu_codec_launches", I64, P)
+    _sig(L, "ebivgpu_set_rgba", I, P, I)
+    _sig(L, "ebivgpu_frame_rgba_pooled", C.c_void_p, P, I)
     _sig(L, "ebivgpu_status_string", C.c_char_p, I)
     _sig(L, "ebivgpu_device_available", I)
     # batch
@@ -133,6 +135,22 @@ def lib() -> C.CDLL:
     _sig(L, "ebiv_mvnet_head", I, P, I, F32P)
     _sig(L, "ebiv_mvnet_propose", I, P, U8P, U8P, I, I16P)
     _sig(L, "ebiv_encoder_set_mvnet", I, P, P)
+    # block analysis
+    _sig(L, "ebivgpu_analysis_create", I, PP)
+    _sig(L, "ebivgpu_analysis_destroy", None, P)
+    _sig(L, "ebivgpu_fdct_satd", I, P, C.c_void_p, I, I, C.c_void_p, C.c_void_p, C.POINTER(C.c_double))
+    # container ingest
+    _sig(L, "ebivgpu_container_open", I, C.c_char_p, S, PP)
+    _sig(L, "ebivgpu_container_close", None, P)
+    _sig(L, "ebivgpu_container_info", I, P, C.POINTER(C.c_int64))
+    _sig(L, "ebivgpu_container_entry", I, P, I, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.POINTER(I))
+    _sig(L, "ebivgpu_container_seek", I, P, I64, C.POINTER(I64), C.POINTER(I64))
+    _sig(L, "ebivgpu_batch_add_container", I, P, P, I, C.POINTER(I))
+    # alt-ref temporal filter
+    _sig(L, "ebivgpu_altref_create", I, PP)
+    _sig(L, "ebivgpu_altref_destroy", None, P)
+    _sig(L, "ebivgpu_altref_build", I, P, C.POINTER(C.c_char_p), I, I, I, I, U8P, S, C.POINTER(I))
+    _sig(L, "ebivgpu_altref_time", I, P, I, I, C.POINTER(C.c_double))
     _sig(L, "ebivgpu_decode_key_noalloc", I, C.c_char_p, S, C.c_void_p, C.c_int32, S, C.c_void_p, C.c_void_p,
          C.c_int32, S, C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32))
     # encoder

@@ -15,6 +15,8 @@ namespace ebiv {
 void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* next, cudaStream_t s);
 void launchInter(const FrameDesc* frames, int nframes, int maxMBs, int phase, cudaStream_t s);
 void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, int maxTileKeys, cudaStream_t s);
+void launchRGBA(const uint8_t* y, const uint8_t* cb, const uint8_t* cr, int ys, int cs, int w, int h, uint8_t* dst,
+                cudaStream_t s);
 
 namespace {
 inline size_t al(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -32,13 +34,17 @@ struct Slot {
   // per macroblock: whether its inter prediction waits for the previous
   // frame's intra stage; then two intra progress bytes (large tiles)
   uint8_t* dep = nullptr;
+  uint8_t* symLog = nullptr;   // the entropy stage's symbol log, kSymPerMB bytes per macroblock
+  uint32_t* symOff = nullptr;  // per macroblock: its first symbol in its tile's log
   bool alloc(size_t mbs) {
     return cudaMalloc(&dep, 3 * mbs) == cudaSuccess && cudaMalloc(&rec, mbs * sizeof(MBRec)) == cudaSuccess &&
            cudaMalloc(&coef, mbs * kCoefPerMB * sizeof(uint32_t)) == cudaSuccess &&
            cudaMalloc(&mv, mbs * 2 * sizeof(int16_t)) == cudaSuccess &&
            cudaMalloc(&lv, mbs * sizeof(int16_t)) == cudaSuccess &&
            cudaMalloc(&intra, 2 * mbs * sizeof(uint32_t)) == cudaSuccess &&
-           cudaMalloc(&ts, mbs * sizeof(TileStat)) == cudaSuccess;
+           cudaMalloc(&ts, mbs * sizeof(TileStat)) == cudaSuccess &&
+           cudaMalloc(&symLog, mbs * kSymPerMB) == cudaSuccess &&
+           cudaMalloc(&symOff, mbs * sizeof(uint32_t)) == cudaSuccess;
   }
   void release() {
     cudaFree(dep);
@@ -48,9 +54,11 @@ struct Slot {
     cudaFree(lv);
     cudaFree(intra);
     cudaFree(ts);
+    cudaFree(symLog);
+    cudaFree(symOff);
   }
   static size_t bytes(size_t mbs) {
-    return mbs * (sizeof(MBRec) + kCoefPerMB * 4 + 4 + 2 + 8 + sizeof(TileStat) + 3);
+    return mbs * (sizeof(MBRec) + kCoefPerMB * 4 + 4 + 2 + 8 + sizeof(TileStat) + 3 + kSymPerMB + 4);
   }
 };
 
@@ -67,11 +75,36 @@ struct Engine::Stream {
   std::vector<int> outputs;  // FIFO of committed output buffers, oldest first
   int ref = -1, golden = -1;
   TableHistory hist;
-  // Resident packets: host copies (for planning) and one device block.
-  std::vector<std::vector<uint8_t>> hostPkts;
+  // Resident packets: per packet its host bytes (for planning) and its
+  // offset in one device block.  A copied stream owns both (hostBlock, and
+  // dPkts allocated by the engine); a container stream views a pinned,
+  // device-mapped container, which the kernels read in place.
+  std::vector<uint8_t> hostBlock;
+  std::vector<const uint8_t*> hostPkt;
+  std::vector<size_t> pktLen;
   uint8_t* dPkts = nullptr;
   size_t dPktsCap = 0;
+  bool ownsPkts = true;
   std::vector<size_t> dOff;
+  size_t packets() const { return hostPkt.size(); }
+  // Copies n packets into hostBlock at 16-byte aligned offsets (dOff); returns the block size.
+  size_t copyPackets(const uint8_t* const* pkts, const size_t* lens, int n) {
+    size_t total = 0;
+    dOff.resize((size_t)n);
+    pktLen.resize((size_t)n);
+    for (int i = 0; i < n; i++) {
+      dOff[(size_t)i] = total;
+      pktLen[(size_t)i] = lens[i];
+      total += (lens[i] + 15) & ~(size_t)15;
+    }
+    hostBlock.assign(total ? total : 16, 0);
+    hostPkt.resize((size_t)n);
+    for (int i = 0; i < n; i++) {
+      if (lens[i]) std::memcpy(hostBlock.data() + dOff[(size_t)i], pkts[i], lens[i]);
+      hostPkt[(size_t)i] = hostBlock.data() + dOff[(size_t)i];
+    }
+    return total;
+  }
   int64_t next = 0;
   // Streaming: the submitted packet awaiting its round.
   std::vector<uint8_t> pendingPkt;
@@ -97,7 +130,7 @@ struct Engine::Stream {
     pool.clear();
     for (auto& sl : slots) sl.release();
     slots.clear();
-    if (dPkts) cudaFree(dPkts);
+    if (dPkts && ownsPkts) cudaFree(dPkts);
     dPkts = nullptr;
   }
 };
@@ -273,21 +306,36 @@ int Engine::addResidentStream(const uint8_t* const* pkts, const size_t* lens, in
   if (!s) return kErrArg;
   s->resident = true;
   s->ring = ring >= 2 ? ring : 3;
-  size_t total = 0;
-  s->hostPkts.resize((size_t)n);
-  s->dOff.resize((size_t)n);
-  for (int i = 0; i < n; i++) {
-    s->hostPkts[(size_t)i].assign(pkts[i], pkts[i] + lens[i]);
-    s->dOff[(size_t)i] = total;
-    total += al(lens[i], 16);
-  }
+  const size_t total = s->copyPackets(pkts, lens, n);
   if (cudaMalloc(&s->dPkts, total ? total : 16) != cudaSuccess) return kErrDevice;
   s->dPktsCap = total ? total : 16;
-  for (int i = 0; i < n; i++)
-    if (lens[i] && cudaMemcpy(s->dPkts + s->dOff[(size_t)i], pkts[i], lens[i], cudaMemcpyHostToDevice) != cudaSuccess)
-      return kErrDevice;
+  if (total && cudaMemcpy(s->dPkts, s->hostBlock.data(), total, cudaMemcpyHostToDevice) != cudaSuccess)
+    return kErrDevice;
   s->bytes += s->dPktsCap;
   deviceBytes_ += s->dPktsCap;
+  s->id = (int)streams_.size();
+  *id = s->id;
+  streams_.push_back(std::move(s));
+  return kOK;
+}
+
+int Engine::addContainerStream(const uint8_t* hostBase, const uint8_t* devBase, const uint64_t* off,
+                               const uint32_t* pktLen, int n, int ring, int* id) {
+  if (!hostBase || !devBase || (n && (!off || !pktLen)) || n < 0 || !id) return kErrArg;
+  std::unique_ptr<Stream> s(new (std::nothrow) Stream());
+  if (!s) return kErrArg;
+  s->resident = true;
+  s->ownsPkts = false;
+  s->ring = ring >= 2 ? ring : 3;
+  s->hostPkt.resize((size_t)n);
+  s->pktLen.resize((size_t)n);
+  s->dOff.resize((size_t)n);
+  for (int i = 0; i < n; i++) {
+    s->hostPkt[(size_t)i] = hostBase + off[i];
+    s->pktLen[(size_t)i] = pktLen[i];
+    s->dOff[(size_t)i] = (size_t)off[i];
+  }
+  s->dPkts = const_cast<uint8_t*>(devBase);
   s->id = (int)streams_.size();
   *id = s->id;
   streams_.push_back(std::move(s));
@@ -302,15 +350,8 @@ int Engine::reloadStream(int id, const uint8_t* const* pkts, const size_t* lens,
   if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id] || n < 0) return kErrArg;
   if (!pipe_.empty()) return kErrArg;  // drain() first
   Stream& s = *streams_[(size_t)id];
-  if (!s.resident) return kErrArg;
-  size_t total = 0;
-  s.hostPkts.resize((size_t)n);
-  s.dOff.resize((size_t)n);
-  for (int i = 0; i < n; i++) {
-    s.hostPkts[(size_t)i].assign(pkts[i], pkts[i] + lens[i]);
-    s.dOff[(size_t)i] = total;
-    total += al(lens[i], 16);
-  }
+  if (!s.resident || !s.ownsPkts) return kErrArg;
+  const size_t total = s.copyPackets(pkts, lens, n);  // host copies for planning
   cudaStream_t se = entropyStream();
   if (total > s.dPktsCap) {
     if (cudaStreamSynchronize(se) != cudaSuccess) return kErrDevice;
@@ -385,7 +426,7 @@ int Engine::submit(int id, const uint8_t* pkt, size_t n) {
 int Engine::seekStream(int id, int64_t index) {
   if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) return kErrArg;
   Stream& s = *streams_[(size_t)id];
-  if (!s.resident || index < 0 || index > (int64_t)s.hostPkts.size()) return kErrArg;
+  if (!s.resident || index < 0 || index > (int64_t)s.packets()) return kErrArg;
   s.next = index;
   return kOK;
 }
@@ -393,7 +434,7 @@ int Engine::seekStream(int id, int64_t index) {
 int64_t Engine::remaining(int id) const {
   if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) return 0;
   const Stream& s = *streams_[(size_t)id];
-  return s.resident ? (int64_t)s.hostPkts.size() - s.next : (s.pending ? 1 : 0);
+  return s.resident ? (int64_t)s.packets() - s.next : (s.pending ? 1 : 0);
 }
 
 int Engine::setActive(int id, bool active) {
@@ -605,7 +646,7 @@ int Engine::finishFrame(Stream& s, Job& j, const int32_t* st, std::vector<RoundR
 int Engine::round(std::vector<RoundResult>* results) {
   std::vector<int> ids;
   for (auto& s : streams_)
-    if (s && s->active && ((s->resident && s->next < (int64_t)s->hostPkts.size()) || (!s->resident && s->pending)))
+    if (s && s->active && ((s->resident && s->next < (int64_t)s->packets()) || (!s->resident && s->pending)))
       ids.push_back(s->id);
   return roundFor(ids, results);
 }
@@ -677,10 +718,10 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
       j.step = step;
       j.epoch = s.epoch;
       if (s.resident) {
-        if (s.next >= (int64_t)s.hostPkts.size()) break;
+        if (s.next >= (int64_t)s.packets()) break;
         j.pktIndex = s.next;
-        j.hPkt = s.hostPkts[(size_t)s.next].data();
-        j.n = s.hostPkts[(size_t)s.next].size();
+        j.hPkt = s.hostPkt[(size_t)s.next];
+        j.n = s.pktLen[(size_t)s.next];
         j.dPkt = s.dPkts + s.dOff[(size_t)s.next];
         s.next++;
       } else {
@@ -852,6 +893,9 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
     fd.intraList = sl.intra;
     fd.intraSorted = sl.intra + s.mbs;
     fd.tileStat = sl.ts;
+    fd.symLog = sl.symLog;
+    fd.symOff = sl.symOff;
+    fd.symPerMB = kSymPerMB;
     fd.status = reinterpret_cast<int32_t*>(d + R.oStat) + di;
     fd.gate = gateDesc >= 0 ? reinterpret_cast<const int32_t*>(d + R.oStat) + gateDesc : nullptr;
     fd.dep = sl.dep;
@@ -1174,6 +1218,35 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
   return n;
 }
 
+int Engine::decodeInto(int id, uint8_t* y, int ys, uint8_t* cb, uint8_t* cr, int cs,
+                       std::vector<RoundResult>* results, uint8_t* rgbaDev, uint8_t* rgbaHost) {
+  if (pipeDepth_ || id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) return kErrArg;
+  Round& R = rounds_[0];
+  R.parity = 0;
+  bool failed = planRound({id}, nullptr, R) || launchRecon(R);
+  if (!failed && R.jobs.size() == 1 && R.jobs[0].status == kOK && R.jobs[0].work >= 0) {
+    const Stream& s = *streams_[(size_t)id];
+    const int b = R.jobs[0].work, w = s.geo.W, h = s.geo.H, cw = (w + 1) / 2, ch = (h + 1) / 2;
+    failed = cudaMemcpy2DAsync(y, ys, s.plane(b, 0), s.strideY, w, h, cudaMemcpyDeviceToHost, stream_) ||
+             cudaMemcpy2DAsync(cb, cs, s.plane(b, 1), s.strideC, cw, ch, cudaMemcpyDeviceToHost, stream_) ||
+             cudaMemcpy2DAsync(cr, cs, s.plane(b, 2), s.strideC, cw, ch, cudaMemcpyDeviceToHost, stream_);
+    if (!failed && rgbaDev && rgbaHost) {
+      launchRGBA(s.plane(b, 0), s.plane(b, 1), s.plane(b, 2), s.strideY, s.strideC, w, h, rgbaDev, stream_);
+      launches_++;
+      failed = cudaGetLastError() != cudaSuccess ||
+               cudaMemcpyAsync(rgbaHost, rgbaDev, (size_t)w * h * 4, cudaMemcpyDeviceToHost, stream_) != cudaSuccess;
+    }
+  }
+  if (failed) {
+    for (Job& j : R.jobs)
+      if (j.status == kOK) j.status = kErrDevice;
+    R.nDesc = 0;
+    collectRound(R, results);
+    return -1;
+  }
+  return collectRound(R, results);
+}
+
 int Engine::enableSideLane() {
   for (auto& s : streams_)
     if (s) return kErrArg;  // pool and slot counts depend on it
@@ -1278,6 +1351,10 @@ struct ebivgpu_batch {
   Engine e;
   std::vector<RoundResult> last;
 };
+
+namespace ebiv {
+Engine* batchEngine(ebivgpu_batch* b) { return b ? &b->e : nullptr; }
+}  // namespace ebiv
 
 extern "C" {
 

@@ -34,9 +34,10 @@ namespace dev {
 constexpr unsigned kFull = 0xffffffffu;
 
 // Per transform size and scan position: row-major index (bits 0-7) and the
-// token-context offset of the position's band, bandOf(i) * kNumPrevClass
-// (bits 8-15).
-__constant__ uint16_t cScanBand[3][256];
+// offset of the position's band in the symbol-table rows,
+// bandOf(i) * kNumPrevClass * 64 (bits 8-19).  One entry past each scan is
+// zero, so the next position's entry can always be loaded.
+__constant__ uint32_t cScanRow[3][257];
 // 2^13-scaled DCT-II basis, [k*n + i], per transform size.  Global memory:
 // the transforms read it with a different index in every lane, which the
 // L1 path serves in one pass and the constant cache would serialise.
@@ -70,10 +71,9 @@ struct EntropyTables {
   uint32_t bucket[kNumContexts * 64];
   uint32_t sym[kNumContexts * 16];
 };
-constexpr int kRowMax = 128;  // tiles at most this many macroblocks wide keep their rows in shared memory
+constexpr int kRowMax = 128;  // tiles at most this many macroblocks wide pass vector rows in shared memory
 struct WarpRows {
-  uint32_t mv[2][kRowMax];  // packed motion vectors of the row above / the current row
-  int16_t lvl[2][kRowMax];  // intra dependency levels (-1: not intra)
+  uint32_t mv[2][kRowMax];  // packed vectors of a pass's last row, by pass parity
 };
 
 __device__ __forceinline__ void buildTables(EntropyTables& T, const DeviceTables& src, int tid, int nthreads) {
@@ -96,33 +96,64 @@ __device__ __forceinline__ void buildTables(EntropyTables& T, const DeviceTables
   __syncthreads();
 }
 
+// Symbol-log bookkeeping of the symbol path.  kNoError: no failing symbol;
+// kFullChain (in TileStat::errAt): the tile was decoded by the full chain;
+// kOverflow: internal status of a symbol chain whose log ran out of room
+// (never reported: the tile is decoded again by the full chain).  A
+// macroblock header takes at most 125 symbols (mode, reference, partition,
+// four vectors of two class-coded components of up to 15 symbols each,
+// pattern, transform size).
+constexpr int32_t kNoError = 0x7FFFFFFF;
+constexpr int32_t kFullChain = -1;
+constexpr int32_t kOverflow = -100;
+constexpr int kMBHeaderSymbols = 128;
+
 // A tile's rANS decoder (ebiv/rans.go:222-304).  All fields are warp-uniform;
 // the two next stream bytes are prefetched so renormalisation rarely waits.
-// After the first error every symbol decodes as 0.
-struct Chain {
+// After the first error every symbol decodes as 0.  With kLog every symbol
+// the decoder returns while no error is pending (the failing one included,
+// as 0) is appended to a symbol log, and errAt is the failing one's index.
+template <bool kLog>
+struct ChainT {
   const uint8_t* buf;
   int32_t pos;
   uint32_t x0, x1, x2, x3;  // states in use order: x0 decodes the next symbol
   uint32_t b1, b2;          // buf[pos-1], buf[pos-2] when present
   int32_t err;
   const EntropyTables* t;
+  uint8_t* log;   // kLog: the tile's symbol log
+  int32_t n;      // kLog: symbols logged
+  int32_t errAt;  // kLog: index of the failing symbol (kNoError: none)
+  int32_t cap;    // kLog: the log's capacity
+  int32_t lane;   // kLog: the lane that writes the log
 
   __device__ __forceinline__ uint32_t byteAt(int i) const { return i >= 0 ? (uint32_t)__ldg(buf + i) : 0u; }
+  __device__ __forceinline__ int logged(int s) {
+    if (kLog) {
+      if (lane == 0) log[n] = (uint8_t)s;
+      n++;
+    }
+    return s;
+  }
+  __device__ __forceinline__ int fail(int e) {
+    err = e;
+    if (kLog) errAt = n;
+    return logged(0);
+  }
 
-  __device__ __forceinline__ int sym(int ctx) {
+  // The next symbol of the context whose bucket row starts at word row
+  // (context * 64).
+  __device__ __forceinline__ int symAt(int row) {
     if (err) return 0;
     const uint32_t x = x0;
     const uint32_t slot = x & (kM - 1);
-    const uint32_t e = t->bucket[ctx * 64 + (slot >> 6)];
+    const uint32_t e = t->bucket[row + (int)(slot >> 6)];
     int s = (int)((e >> 25) & 15u);
     uint32_t start = e & 0xFFFu, freq = (e >> 12) & 0x1FFFu;
     if (e & (kBImpure | kBUnused)) {
-      if (e & kBUnused) {
-        err = kErrCorrupt;  // symbol decoded from an unused context
-        return 0;
-      }
+      if (e & kBUnused) return fail(kErrCorrupt);  // symbol decoded from an unused context
       while (slot >= start + freq) {
-        const uint32_t w = t->sym[ctx * 16 + (++s)];
+        const uint32_t w = t->sym[(row >> 2) + (++s)];
         start = w & 0xFFFFu;
         freq = w >> 16;
       }
@@ -143,10 +174,7 @@ struct Chain {
         }
       } else {
         while (xn < kLower) {
-          if (pos == 0) {
-            err = kErrCorrupt;  // stream underrun
-            return 0;
-          }
+          if (pos == 0) return fail(kErrCorrupt);  // stream underrun
           pos--;
           xn = (xn << 8) | b1;
           b1 = b2;
@@ -158,72 +186,141 @@ struct Chain {
     x1 = x2;
     x2 = x3;
     x3 = xn;
-    return s;
+    return logged(s);
   }
-  __device__ __forceinline__ uint32_t rawBits(int n) {
-    uint32_t v = 0;
-    for (int i = 0; i < n; i++) v = v << 1 | (uint32_t)sym(ctxBypass);
-    return v;
+  __device__ __forceinline__ int sym(int ctx) { return symAt(ctx << 6); }
+  // Whether the log has room for `need` more symbols; when it has not, the
+  // chain stops with kOverflow.
+  __device__ __forceinline__ bool room(int need) {
+    if (!kLog || n + need <= cap) return true;
+    err = kOverflow;
+    return false;
   }
-  // getClassValue — ebiv/mv.go:95-108
-  __device__ __forceinline__ uint32_t classValue(int classCtx) {
-    const int cls = sym(classCtx);
-    if (cls <= 1) return (uint32_t)cls;
-    return (1u << (cls - 1)) | rawBits(cls - 1);
-  }
-  __device__ __forceinline__ int mvComponent(int classCtx) {
-    const uint32_t u = classValue(classCtx);
-    return (int)(u >> 1) ^ -(int)(u & 1);
+  // Initialises the four states from the end of the tile's bytes
+  // (ransDecoder.reset, ebiv/rans.go:236-250); false when the stream is too short.
+  __device__ __forceinline__ bool reset(const uint8_t* b, uint32_t len, const EntropyTables* tables) {
+    buf = b;
+    pos = (int32_t)len;
+    err = 0;
+    t = tables;
+    n = 0;
+    errAt = kNoError;
+    if (len < (uint32_t)(kStates * 4)) {
+      err = kErrCorrupt;
+      return false;
+    }
+    uint32_t st[4];
+#pragma unroll
+    for (int i = kStates - 1; i >= 0; i--) {
+      st[i] = byteAt(pos - 1) << 24 | byteAt(pos - 2) << 16 | byteAt(pos - 3) << 8 | byteAt(pos - 4);
+      pos -= 4;
+    }
+    x0 = st[0];
+    x1 = st[1];
+    x2 = st[2];
+    x3 = st[3];
+    b1 = byteAt(pos - 1);
+    b2 = byteAt(pos - 2);
+    return true;
   }
 };
 
-// decodeBlock (ebiv/residual.go:79-126): writes the block's nonzero levels as
-// packed entries after a count word; lane 0 stores.  ctxBase selects the
-// token contexts of the plane and transform size.  Returns the count.
-__device__ __forceinline__ int entropyBlock(Chain& d, int ctxBase, int sz, uint32_t* region, int lane) {
-  const uint16_t* sb = cScanBand[sz];
+// Replays a tile's symbol log from one macroblock's first symbol: the same
+// values, and the same error state at every point, as the chain that wrote
+// the log (a symbol past the failing one is never read: it decodes as 0).
+struct Replay {
+  const uint8_t* log;
+  int32_t k;      // index of the next symbol in the tile's log
+  int32_t errAt;  // index of the failing symbol, or kNoError
+  int32_t end;    // the log's capacity: reads stay inside it
+  int32_t err;
+  __device__ __forceinline__ int symAt(int) {
+    if (err) return 0;
+    if (k >= end) {  // unreachable while replay and chain agree; keeps every read in bounds
+      err = kErrCorrupt;
+      return 0;
+    }
+    const int s = log[k];
+    k++;
+    if (k > errAt) err = kErrCorrupt;
+    return s;
+  }
+  __device__ __forceinline__ int sym(int) { return symAt(0); }
+  __device__ __forceinline__ bool room(int) const { return true; }
+};
+
+// getRawBits / getClassValue / getMVComponent — ebiv/mv.go:75-128.
+template <class S>
+__device__ __forceinline__ uint32_t rawBits(S& d, int n) {
+  uint32_t v = 0;
+  for (int i = 0; i < n; i++) v = v << 1 | (uint32_t)d.sym(ctxBypass);
+  return v;
+}
+template <class S>
+__device__ __forceinline__ uint32_t classValue(S& d, int classCtx) {
+  const int cls = d.sym(classCtx);
+  if (cls <= 1) return (uint32_t)cls;
+  return (1u << (cls - 1)) | rawBits(d, cls - 1);
+}
+template <class S>
+__device__ __forceinline__ int mvComponent(S& d, int classCtx) {
+  const uint32_t u = classValue(d, classCtx);
+  return (int)(u >> 1) ^ -(int)(u & 1);
+}
+
+// decodeBlock (ebiv/residual.go:79-126).  With kOut the block's nonzero
+// levels are written as packed entries after a count word (by lane 0);
+// without it only the symbols are decoded (the chain of the symbol path:
+// everything that decides which symbol comes next, nothing else).  row is
+// the bucket row of the block's token contexts at band 0 and previous class
+// 0 (context * 64); the band and previous class add their row offsets.
+// Returns the count.
+template <bool kOut, class S>
+__device__ __forceinline__ int entropyBlock(S& d, int row, int sz, uint32_t* region, int lane) {
+  const uint32_t* sb = cScanRow[sz];
   const int total = 16 << (2 * sz);
   int first = -1, last = -1, count = 0;
   int32_t sumAbs = 0;
-  int prevClass = 0;
+  int pc = 0;  // previous class * 64
   uint32_t firstPos = 0;
   int32_t firstMag = 0;
   uint32_t cur = sb[0];
   for (int i = 0; i < total; i++) {
-    const uint32_t nxt = i + 1 < total ? sb[i + 1] : 0u;  // next position's entry, loaded early
-    const int t = d.sym(ctxBase + (int)(cur >> 8) + prevClass);
+    const uint32_t nxt = sb[i + 1];  // next position's entry, loaded early (the table is padded)
+    const int t = d.symAt(row + (int)(cur >> 8) + pc);
     if (t == tEOB) break;
-    if (t != tZero) {
-      int mag;
-      if (t == tEscape) {
-        mag = 5 + (int)d.classValue(ctxEscClass);
-        prevClass = 2;
-      } else {
-        mag = t;
-        prevClass = mag == 1 ? 1 : 2;
-      }
-      sumAbs = wadd(sumAbs, mag);
-      const uint32_t pos = cur & 0xFFu;
-      if (first < 0) {
-        first = i;
-        firstPos = pos;
-        firstMag = mag;
-      } else {
-        if (d.sym(ctxSign) == 1) mag = -mag;
-        if (lane == 0) region[1 + count] = pos | ((uint32_t)mag << 8);
-      }
-      count++;
-      last = i;
-    } else {
-      prevClass = 0;
+    if (t == tZero) {
+      pc = 0;
+      cur = nxt;
+      continue;
     }
+    int mag;
+    if (t == tEscape) {
+      mag = 5 + (int)classValue(d, ctxEscClass);
+      pc = 2 * 64;
+    } else {
+      mag = t;
+      pc = t == tOne ? 64 : 2 * 64;
+    }
+    sumAbs = wadd(sumAbs, mag);
+    const uint32_t pos = cur & 0xFFu;
+    if (first < 0) {
+      first = i;
+      firstPos = pos;
+      firstMag = mag;
+    } else {
+      if (d.symAt(ctxSign << 6) == 1) mag = -mag;
+      if (kOut && lane == 0) region[1 + count] = pos | ((uint32_t)mag << 8);
+    }
+    count++;
+    last = i;
     cur = nxt;
   }
   if (first >= 0) {
-    const bool neg = (last - first >= kSDHMinSpan) ? (sumAbs & 1) == 1 : d.sym(ctxSign) == 1;
-    if (lane == 0) region[1] = firstPos | ((uint32_t)(neg ? -firstMag : firstMag) << 8);
+    const bool neg = (last - first >= kSDHMinSpan) ? (sumAbs & 1) == 1 : d.symAt(ctxSign << 6) == 1;
+    if (kOut && lane == 0) region[1] = firstPos | ((uint32_t)(neg ? -firstMag : firstMag) << 8);
   }
-  if (lane == 0) region[0] = (uint32_t)count;
+  if (kOut && lane == 0) region[0] = (uint32_t)count;
   return count;
 }
 
@@ -260,6 +357,13 @@ struct Rec {
     else if (i == 1) mv1 = v;
     else if (i == 2) mv2 = v;
     else mv3 = v;
+  }
+  // One thread stores the whole 48-byte record.
+  __device__ __forceinline__ void storeAll(MBRec* dst) const {
+    uint4* q = reinterpret_cast<uint4*>(dst);
+    q[0] = make_uint4(w0, w1, mv0, mv1);
+    q[1] = make_uint4(mv2, mv3, lm0, lm1);
+    q[2] = make_uint4(lm2, lm3, nz, wm);
   }
   // Lanes 0-2 store the 48-byte record as three 16-byte words.
   __device__ __forceinline__ void store(MBRec* dst, int lane) const {
@@ -298,36 +402,40 @@ struct BlockPlan {
   bool intra, cb, cr;
 };
 
-// The one block loop of the kernel (a single inlined copy keeps the code
-// small).  Returns how many blocks completed before an error; *nzOut gets
-// the nonzero mask (bit k luma block k, 16 Cb, 17 Cr).
-__device__ __forceinline__ int entropyBlocks(Chain& d, Rec& r, const BlockPlan& p, uint32_t* coef, int lane,
+// The block loop of a macroblock.  Returns how many blocks completed before
+// an error; *nzOut gets the nonzero mask (bit k luma block k, 16 Cb, 17 Cr).
+// A logging chain first checks that its log has room for the block's
+// largest possible symbol count (mode, 17 per coefficient, the hidden sign).
+template <bool kOut, class S>
+__device__ __forceinline__ int entropyBlocks(S& d, Rec& r, const BlockPlan& p, uint32_t* coef, int lane,
                                              uint32_t* nzOut) {
   const int nEnt = p.nLuma + (p.cb ? 1 : 0) + (p.cr ? 1 : 0);
   const int bw = (16 << (2 * p.tx)) + 1;  // words per luma block region
-  const int lumaBase = ctxTokenBase + p.tx * kNumBands * kNumPrevClass;
+  const int lumaRow = (ctxTokenBase + p.tx * kNumBands * kNumPrevClass) << 6;
   int done = 0;
   uint32_t nz = 0;
 #pragma unroll 1
   for (int e = 0; e < nEnt; e++) {
-    int ctxBase, sz;
+    int row, sz;
     uint32_t* region;
     uint32_t bit;
     if (e < p.nLuma) {
-      if (p.intra) r.lumaMode(e, (uint32_t)d.sym(ctxLumaMode));
-      ctxBase = lumaBase;
       sz = p.tx;
+      if (!d.room(2 + 17 * (16 << (2 * sz)))) break;
+      if (p.intra) r.lumaMode(e, (uint32_t)d.sym(ctxLumaMode));
+      row = lumaRow;
       region = coef + e * bw;
       bit = 1u << e;
     } else {
+      sz = 1;
+      if (!d.room(2 + 17 * 64)) break;
       const bool isCb = p.cb && e == p.nLuma;
       if (isCb && p.intra) r.w1 |= (uint32_t)d.sym(ctxChromaMode) << 8;
-      ctxBase = ctxTokenBase + kLumaTokenCtx;
-      sz = 1;
+      row = (ctxTokenBase + kLumaTokenCtx) << 6;
       region = coef + (isCb ? kCoefCb : kCoefCr);
       bit = isCb ? (1u << 16) : (1u << 17);
     }
-    const int cnt = entropyBlock(d, ctxBase, sz, region, lane);
+    const int cnt = entropyBlock<kOut>(d, row, sz, region, lane);
     if (d.err) break;
     if (cnt) nz |= bit;
     done++;
@@ -338,7 +446,8 @@ __device__ __forceinline__ int entropyBlocks(Chain& d, Rec& r, const BlockPlan& 
 
 // Intra macroblock header (decodeLumaMB, ebiv/decode_intra.go:137-150): the
 // transform size; the blocks follow.
-__device__ __forceinline__ void intraHeader(Chain& d, Rec& r, BlockPlan* p) {
+template <class S>
+__device__ __forceinline__ void intraHeader(S& d, Rec& r, BlockPlan* p) {
   int tx = d.sym(ctxTxSize);
   if (tx >= 3) tx = 0;  // alphabet size 3: unreachable
   r.w0 = kRecIntra;
@@ -348,23 +457,14 @@ __device__ __forceinline__ void intraHeader(Chain& d, Rec& r, BlockPlan* p) {
   p->intra = p->cb = p->cr = true;
 }
 
-// Inter-frame macroblock header (decodeInterMB, ebiv/decode_inter.go:8-62):
-// mode, reference, partition, vectors, coded-block pattern, transform size.
-// Returns 0 when the macroblock is complete without blocks (*wOut holds its
-// write mask), 1 when the blocks of *p follow.  *mvOut is the vector
-// neighbours predict from.
-__device__ __forceinline__ int interHeader(Chain& d, Rec& r, const Nbr& n, int mode, BlockPlan* p, bool* intra,
-                                           uint32_t* mvOut, uint32_t* wOut) {
-  *mvOut = 0;
-  *wOut = 0;
-  if (mode == mbSkip) {
-    const uint32_t pv = predictMV(n);
-    *mvOut = pv;
-    r.w0 = kRecSkip;
-    r.mv0 = pv;
-    *wOut = kWriteAll;
-    return 0;
-  }
+// Inter-frame macroblock header after the mode (decodeInterMB,
+// ebiv/decode_inter.go:8-62): reference, partition, vector deltas,
+// coded-block pattern, transform size.  The vectors are stored as deltas
+// (x, y as int16) in the record; predictVectors turns them into vectors
+// (no context depends on a vector, so the chain never needs them).  Returns
+// 1 when the blocks of *p follow, 0 when the macroblock ends here (an error).
+template <class S>
+__device__ __forceinline__ int interHeader(S& d, Rec& r, int mode, BlockPlan* p, bool* intra) {
   if (mode == mbIntra) {
     *intra = true;
     intraHeader(d, r, p);
@@ -375,28 +475,16 @@ __device__ __forceinline__ int interHeader(Chain& d, Rec& r, const Nbr& n, int m
     return 0;
   }
   const int refSel = d.sym(ctxRef);
-  uint32_t pred = predictMV(n);
-  if (refSel == refGolden) pred = 0;
   int part = d.sym(ctxPart);
   if (part >= kNumPartModes) part = 0;  // alphabet size 4: unreachable
   const int np = part == partWhole ? 1 : (part == part8x8 ? 4 : 2);
-  uint32_t mv0 = 0;
 #pragma unroll 1
   for (int i = 0; i < np; i++) {
-    const uint32_t pp = i > 0 ? mv0 : pred;
-    int vx = 0, vy = 0;
-#pragma unroll 1
-    for (int c = 0; c < 2; c++) {
-      const int dv = d.mvComponent(c ? ctxMVClassY : ctxMVClassX);
-      if (c == 0) vx = clampMV(mvX(pp) + dv);
-      else vy = clampMV(mvY(pp) + dv);
-    }
-    const uint32_t v = packMV(vx, vy);
-    if (i == 0) mv0 = v;
-    r.setMV(i, v);
+    const int dx = mvComponent(d, ctxMVClassX);
+    const int dy = mvComponent(d, ctxMVClassY);
+    r.setMV(i, packMV(dx, dy));
   }
   if (d.err) return 0;
-  *mvOut = refSel == refGolden ? 0u : mv0;
   const int cbp = d.sym(ctxCBP);
   r.w0 = kRecInter | ((uint32_t)refSel << 8) | ((uint32_t)part << 16) | ((uint32_t)cbp << 24);
   if (d.err) return 0;
@@ -437,152 +525,185 @@ __device__ __forceinline__ uint32_t writeMask(const BlockPlan& p, int done) {
   return w;
 }
 
+// Vector prediction over a tile whose chain is done (predictMV,
+// ebiv/mv.go:21-52, neighbours inside the tile; decodeInterMB's use of it,
+// ebiv/decode_inter.go:8-62).  A macroblock's vector needs the final
+// vectors of its left, above and above-right (or above-left) neighbours, so
+// the tile runs as a wavefront: in a pass of 32 rows lane k takes row k and,
+// at step t, column t - 2k.  The left neighbour is the lane's own result of
+// the step before; the row above comes from lane k-1 by shuffle (its
+// results of the last three steps are columns x-1, x, x+1), and for lane 0
+// from the previous pass's last row (shared memory; the frame's vector grid
+// for tiles wider than kRowMax).  A skip macroblock takes the prediction;
+// an inter one adds its deltas (partition 0 to the prediction, zero for the
+// golden reference; later partitions to partition 0), clamped as the chain
+// would have.  Records past `done` are not touched.
+__device__ void predictVectors(const FrameDesc* fp, int tile, int done, WarpRows& rows, int lane) {
+  const int mbCols = fp->mbCols;
+  MBRec* const recs = fp->mbrec;
+  uint32_t* const gmv = reinterpret_cast<uint32_t*>(fp->mvgrid);
+  const TileRange tr = fp->tiles[tile];
+  const int x0 = tr.mbX0, y0 = tr.mbY0, tw = tr.mbX1 - x0, th = tr.mbY1 - y0;
+  const bool wide = tw > kRowMax;
+  for (int p0 = 0, pass = 0; p0 < th; p0 += 32, pass++) {
+    const int ry = p0 + lane;
+    const int nrows = min(32, th - p0);
+    const int steps = tw + 2 * (nrows - 1);
+    const bool lastRowOfPass = lane == 31 && p0 + 32 < th;
+    const uint32_t* upRow = wide ? gmv + (size_t)(y0 + p0 - 1) * mbCols + x0 : rows.mv[(pass + 1) & 1];
+    uint32_t* nextUp = wide ? gmv + (size_t)(y0 + p0 + 31) * mbCols + x0 : rows.mv[pass & 1];
+    // Records of this lane's row; written by this warp's chain, so read
+    // with coherent loads (never through the read-only path).
+    MBRec* const rowRec = recs + (size_t)(y0 + min(ry, th - 1)) * mbCols + x0;
+    const int rowDone = ry < th ? min(tw, done - ry * tw) : 0;  // columns of this row the chain reached
+    uint32_t h1 = 0, h2 = 0, h3 = 0;  // this lane's results of steps t-1, t-2, t-3
+    // Record words 0-3 of the step's macroblock, loaded one step ahead.
+    uint4 cur = make_uint4(0u, 0u, 0u, 0u);
+    if (lane == 0 && rowDone > 0) cur = reinterpret_cast<const uint4*>(rowRec)[0];
+    for (int t = 0; t < steps; t++) {
+      const int rx = t - 2 * lane;
+      const bool act = rx >= 0 && rx < rowDone;
+      uint4 nxt = make_uint4(0u, 0u, 0u, 0u);
+      if (rx + 1 >= 0 && rx + 1 < rowDone) nxt = reinterpret_cast<const uint4*>(rowRec + rx + 1)[0];
+      uint32_t above = __shfl_up_sync(kFull, h2, 1);
+      uint32_t ar = __shfl_up_sync(kFull, h1, 1);
+      uint32_t al = __shfl_up_sync(kFull, h3, 1);
+      uint32_t out = 0;
+      if (act) {
+        if (lane == 0 && p0 > 0) {
+          above = upRow[rx];
+          ar = rx + 1 < tw ? upRow[rx + 1] : 0u;
+          al = rx > 0 ? upRow[rx - 1] : 0u;
+        }
+        uint32_t* const rw = reinterpret_cast<uint32_t*>(rowRec + rx);
+        const uint32_t w0 = cur.x;
+        const int mode = (int)(w0 & 0xFF);
+        if (mode == kRecSkip || mode == kRecInter) {
+          Nbr n;
+          n.aOK = rx > 0;
+          n.bOK = ry > 0;
+          n.arOK = n.bOK && rx + 1 < tw;
+          n.cOK = n.arOK || (n.bOK && n.aOK);
+          n.mvA = h1;
+          n.mvB = n.bOK ? above : 0u;
+          n.mvC = n.cOK ? (n.arOK ? ar : al) : 0u;
+          uint32_t pred = predictMV(n);
+          if (mode == kRecSkip) {
+            rw[2] = pred;
+            out = pred;
+          } else {
+            const bool golden = ((w0 >> 8) & 0xFF) == refGolden;
+            const int part = (int)((w0 >> 16) & 0xFF);
+            if (golden) pred = 0;
+            const uint32_t v0 = packMV(clampMV(mvX(pred) + mvX(cur.z)), clampMV(mvY(pred) + mvY(cur.z)));
+            rw[2] = v0;
+            if (part != partWhole) {
+              rw[3] = packMV(clampMV(mvX(v0) + mvX(cur.w)), clampMV(mvY(v0) + mvY(cur.w)));
+              if (part == part8x8) {
+                const uint32_t d2 = rw[4], d3 = rw[5];
+                rw[4] = packMV(clampMV(mvX(v0) + mvX(d2)), clampMV(mvY(v0) + mvY(d2)));
+                rw[5] = packMV(clampMV(mvX(v0) + mvX(d3)), clampMV(mvY(v0) + mvY(d3)));
+              }
+            }
+            out = golden ? 0u : v0;
+          }
+        }
+        if (lastRowOfPass) nextUp[rx] = out;
+      }
+      cur = nxt;
+      h3 = h2;
+      h2 = h1;
+      h1 = out;
+    }
+    __syncwarp();  // the pass's last row is read by the next pass's lane 0
+  }
+}
+
 constexpr int kEntropyWarps = kEntropyTilesPerJob;
 
-// One tile's chain, by one warp (the frame's tables are in sT).
-__device__ __forceinline__ void entropyTile(const FrameDesc* fp, int tile, const EntropyTables& sT, WarpRows& rows,
-                                            int lane) {
-  // Descriptor fields into registers: the kernel's global stores cannot alias them then.
+// One macroblock's grammar (decodeInterMB, ebiv/decode_inter.go:8-62;
+// decodeLumaMB / decodeChromaMB, ebiv/decode_intra.go:137-187).  With kOut
+// the record and the coefficient regions are written: by lanes 0-2 of a
+// warp that runs the macroblock together, or, with kThread, all by the one
+// thread that runs it.  Returns 1 when the macroblock is intra and written
+// (an entry of the tile's intra list).
+template <bool kOut, bool kThread, class S>
+__device__ __forceinline__ int decodeMB(S& d, int inter, MBRec* rec, uint32_t* coef, int lane) {
+  int mode = 0;
+  if (inter) {
+    mode = d.sym(ctxMBMode);
+    if (mode == mbSkip) {
+      // Skip macroblock (most of an inter frame): a fixed record whose
+      // vector predictVectors fills in; nothing else to decode.
+      if (kOut) {
+        const uint4 a = make_uint4(kRecSkip, 0u, 0u, 0u), z = make_uint4(0u, 0u, 0u, 0u),
+                    c = make_uint4(0u, 0u, 0u, kWriteAll);
+        uint4* q = reinterpret_cast<uint4*>(rec);
+        if (kThread) {
+          q[0] = a;
+          q[1] = z;
+          q[2] = c;
+        } else if (lane < 3) {
+          q[lane] = lane == 0 ? a : (lane == 1 ? z : c);
+        }
+      }
+      return 0;
+    }
+  }
+  Rec r;
+  r.clear();
+  bool intra = !inter;
+  uint32_t w = 0;
+  BlockPlan p;
+  int blocks;
+  if (inter) {
+    blocks = interHeader(d, r, mode, &p, &intra);
+  } else {
+    intraHeader(d, r, &p);
+    blocks = d.err ? 0 : 1;
+  }
+  if (blocks) {
+    uint32_t nz;
+    const int nd = entropyBlocks<kOut>(d, r, p, coef, kThread ? 0 : lane, &nz);
+    r.nz = nz;
+    w = writeMask(p, nd);
+  }
+  r.wm = w;
+  if (kOut) {
+    if (kThread) r.storeAll(rec);
+    else r.store(rec, lane);
+  }
+  return intra && w ? 1 : 0;
+}
+
+// The full chain of a tile, by one warp (the frame's tables are in sT): the
+// rANS symbols drive the macroblock grammar, and every macroblock reached
+// gets its record (inter vectors as deltas), its coefficient regions and,
+// when it is intra and written, an entry in the tile's intra list (raster
+// order).  Returns the macroblocks reached (all of them unless the chain
+// stopped at an error).
+__device__ __noinline__ int fullChain(const FrameDesc* fp, int tile, const EntropyTables& sT, int lane) {
   const int mbCols = fp->mbCols;
   const int inter = fp->inter;
   MBRec* const recs = fp->mbrec;
   uint32_t* const coefBase = fp->coef;
-  uint32_t* const intraList = fp->intraList;
-  TileStat* const tstat = fp->tileStat;
-  int32_t* const status = fp->status;
   const TileRange tr = fp->tiles[tile];
+  uint32_t* const intraList = fp->intraList + tr.mbBase;
   const int x0 = tr.mbX0, x1 = tr.mbX1, y0 = tr.mbY0, y1 = tr.mbY1;
-  const bool wide = (x1 - x0) > kRowMax;
-  uint32_t* const gmv = reinterpret_cast<uint32_t*>(fp->mvgrid);
-  int16_t* const glv = fp->lvgrid;
-
-  Chain d;
-  d.buf = fp->pkt + tr.offset;
-  d.pos = (int32_t)tr.length;
-  d.err = 0;
-  d.t = &sT;
-  const int tw = x1 - x0;
-  const int total = tw * (y1 - y0);
-  int done = 0, intraCount = 0, maxLevel = -1;
-  if (tr.length < (uint32_t)(kStates * 4)) {
-    d.err = kErrCorrupt;  // tile stream too short to initialise rANS
-  } else {
-    uint32_t st[4];
-#pragma unroll
-    for (int i = kStates - 1; i >= 0; i--) {
-      st[i] = d.byteAt(d.pos - 1) << 24 | d.byteAt(d.pos - 2) << 16 | d.byteAt(d.pos - 3) << 8 | d.byteAt(d.pos - 4);
-      d.pos -= 4;
-    }
-    d.x0 = st[0];
-    d.x1 = st[1];
-    d.x2 = st[2];
-    d.x3 = st[3];
-    d.b1 = d.byteAt(d.pos - 1);
-    d.b2 = d.byteAt(d.pos - 2);
-    for (int mby = y0; mby < y1 && !d.err; mby++) {
-      // Rows as pointers indexed by the frame column: shared memory for
-      // tiles up to kRowMax macroblocks wide, the frame grid otherwise.
-      uint32_t* mvCur;
-      const uint32_t* mvUp;
-      int16_t* lvCur;
-      const int16_t* lvUp;
-      if (wide) {
-        mvCur = gmv + (size_t)mby * mbCols;
-        mvUp = mvCur - mbCols;
-        lvCur = glv + (size_t)mby * mbCols;
-        lvUp = lvCur - mbCols;
-      } else {
-        const int r = (mby - y0) & 1;
-        mvCur = rows.mv[r] - x0;
-        mvUp = rows.mv[r ^ 1] - x0;
-        lvCur = rows.lvl[r] - x0;
-        lvUp = rows.lvl[r ^ 1] - x0;
+  const int tw = x1 - x0, total = tw * (y1 - y0);
+  ChainT<false> d;
+  d.reset(fp->pkt + tr.offset, tr.length, &sT);
+  d.lane = lane;
+  int done = 0, intraCount = 0;
+  for (int mby = y0; mby < y1 && !d.err; mby++) {
+    for (int mbx = x0; mbx < x1; mbx++) {
+      const int idx = mby * mbCols + mbx;
+      if (decodeMB<true, false>(d, inter, recs + idx, coefBase + (size_t)idx * kCoefPerMB, lane)) {
+        if (lane == 0) intraList[intraCount] = (uint32_t)idx;
+        intraCount++;
       }
-      const bool bOK = mby > y0;
-      uint32_t mvLeft = 0;
-      int lvLeft = -1;
-      for (int mbx = x0; mbx < x1; mbx++) {
-        const int idx = mby * mbCols + mbx;
-        Nbr n;
-        n.aOK = mbx > x0;
-        n.bOK = bOK;
-        n.arOK = bOK && mbx + 1 < x1;
-        n.cOK = n.arOK || (bOK && n.aOK);
-        n.mvA = mvLeft;
-        n.mvB = 0;
-        n.mvC = 0;
-        if (inter && bOK) {
-          n.mvB = mvUp[mbx];
-          if (n.cOK) n.mvC = mvUp[n.arOK ? mbx + 1 : mbx - 1];
-        }
-        int mode = 0;
-        if (inter) {
-          mode = d.sym(ctxMBMode);
-          if (mode == mbSkip) {
-            // Skip macroblock (most of an inter frame): predicted vector,
-            // fixed record, rows updated; nothing else to decode.
-            const uint32_t pv = predictMV(n);
-            if (lane < 3) {
-              const uint4 v = lane == 0 ? make_uint4(kRecSkip, 0u, pv, 0u)
-                                        : (lane == 1 ? make_uint4(0u, 0u, 0u, 0u) : make_uint4(0u, 0u, 0u, kWriteAll));
-              reinterpret_cast<uint4*>(recs + idx)[lane] = v;
-            }
-            if (lane == 0) {
-              mvCur[mbx] = pv;
-              lvCur[mbx] = (int16_t)-1;
-            }
-            mvLeft = pv;
-            lvLeft = -1;
-            done++;
-            if (d.err) break;
-            continue;
-          }
-        }
-        uint32_t* coef = coefBase + (size_t)idx * kCoefPerMB;
-        Rec r;
-        r.clear();
-        bool intra = !inter;
-        uint32_t mv = 0, w = 0;
-        BlockPlan p;
-        int blocks;
-        if (inter) {
-          blocks = interHeader(d, r, n, mode, &p, &intra, &mv, &w);
-        } else {
-          intraHeader(d, r, &p);
-          blocks = d.err ? 0 : 1;
-        }
-        if (blocks) {
-          uint32_t nz;
-          const int nd = entropyBlocks(d, r, p, coef, lane, &nz);
-          r.nz = nz;
-          w = writeMask(p, nd);
-        }
-        int lv = -1;
-        if (intra && w) {
-          // Intra dependency level: one more than the highest intra neighbour.
-          int m = n.aOK ? lvLeft : -1;
-          if (bOK) {
-            m = max(m, (int)lvUp[mbx]);
-            if (n.aOK) m = max(m, (int)lvUp[mbx - 1]);
-            if (n.arOK) m = max(m, (int)lvUp[mbx + 1]);
-          }
-          lv = m + 1;
-          if (lane == 0) intraList[tr.mbBase + intraCount] = (uint32_t)idx | ((uint32_t)lv << kLevelShift);
-          intraCount++;
-          maxLevel = max(maxLevel, lv);
-        }
-        if (lane == 0) {
-          mvCur[mbx] = mv;
-          lvCur[mbx] = (int16_t)lv;
-        }
-        mvLeft = mv;
-        lvLeft = lv;
-        r.wm = w;
-        r.store(recs + idx, lane);
-        done++;
-        if (d.err) break;
-      }
-      __syncwarp();  // the row just written is read as the row above
+      done++;
+      if (d.err) break;
     }
   }
   // Macroblocks the tile never reached are left untouched by reconstruction.
@@ -595,22 +716,58 @@ __device__ __forceinline__ void entropyTile(const FrameDesc* fp, int tile, const
     TileStat ts;
     ts.err = d.err;
     ts.intraCount = intraCount;
-    ts.maxLevel = maxLevel;
-    ts.pad = 0;
-    tstat[tile] = ts;
-    if (d.err) atomicExch(status, kErrCorrupt);
+    ts.done = done;
+    ts.errAt = kFullChain;
+    fp->tileStat[tile] = ts;
+    if (d.err) atomicExch(fp->status, kErrCorrupt);
   }
+  return done;
+}
+
+// The symbol chain of a tile, by one warp: only the rANS decoder and the
+// grammar decisions that pick the next context, every symbol appended to
+// the tile's log and each macroblock's first symbol index recorded; kParse
+// rebuilds the records from the log in parallel.  Returns false when the
+// log would overflow (the caller then runs fullChain).
+__device__ __forceinline__ bool symbolChain(const FrameDesc* fp, int tile, const EntropyTables& sT, int lane) {
+  const int inter = fp->inter;
+  const TileRange tr = fp->tiles[tile];
+  const int tw = tr.mbX1 - tr.mbX0, total = tw * (tr.mbY1 - tr.mbY0);
+  uint32_t* const mbOff = fp->symOff + tr.mbBase;
+  ChainT<true> d;
+  d.reset(fp->pkt + tr.offset, tr.length, &sT);
+  d.lane = lane;
+  d.log = fp->symLog + (size_t)tr.mbBase * fp->symPerMB;
+  d.cap = total * fp->symPerMB;
+  if (d.err) d.errAt = 0;  // too short to initialise: the tile fails at once
+  int done = 0;
+  for (int k = 0; k < total && !d.err; k++) {
+    if (lane == 0) mbOff[k] = (uint32_t)d.n;
+    if (!d.room(kMBHeaderSymbols)) break;
+    decodeMB<false, false>(d, inter, nullptr, nullptr, lane);
+    done++;
+  }
+  if (d.err == kOverflow) return false;
+  if (lane == 0) {
+    TileStat* ts = fp->tileStat + tile;
+    ts->err = d.err;
+    ts->done = done;
+    ts->errAt = d.errAt;
+    if (d.err) atomicExch(fp->status, kErrCorrupt);
+  }
+  return true;
 }
 
 // Entropy jobs: up to kEntropyWarps tiles of one frame per job, one warp per
-// tile, sharing the frame's symbol tables.  With a queue counter the grid is
+// tile, sharing the frame's symbol tables.  A tile runs the symbol chain
+// when its frame has a symbol log (the full chain when the log would
+// overflow), else the full chain.  With a queue counter the grid is
 // persistent: each CTA takes jobs (longest first, as listed) until none are
-// left, so a round with more jobs than resident CTAs has no second-wave tail;
-// without one, CTA b runs job b.
+// left, so a round with more jobs than resident CTAs has no second-wave
+// tail; without one, CTA b runs job b.
 __global__ void __launch_bounds__(32 * kEntropyWarps, 4) kEntropy(const FrameDesc* frames, const int4* jobs, int njobs,
                                                                    int* next) {
   __shared__ EntropyTables sT;
-  __shared__ WarpRows sR[kEntropyWarps];
   __shared__ int sJob;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (;;) {
@@ -621,10 +778,83 @@ __global__ void __launch_bounds__(32 * kEntropyWarps, 4) kEntropy(const FrameDes
     const int4 job = jobs[jb];
     const FrameDesc* fp = frames + job.x;
     buildTables(sT, *fp->tables, threadIdx.x, blockDim.x);
-    if (warp < job.z) entropyTile(fp, job.y + warp, sT, sR[warp], lane);
+    if (warp < job.z) {
+      const int tile = job.y + warp;
+      if (!fp->symLog || !symbolChain(fp, tile, sT, lane)) fullChain(fp, tile, sT, lane);
+    }
     if (!next) return;
     __syncthreads();  // every warp is done with sT and sJob before the next job
   }
+}
+
+// Rebuilds the records of the symbol-path tiles from their logs: one CTA per
+// tile of a job.  Each thread replays one macroblock at a time from its
+// first symbol (decodeMB, one thread per macroblock), so a tile's records,
+// coefficient regions and write masks come out in parallel; then the CTA
+// lists the tile's written intra macroblocks in raster order, and (inter
+// frames) warp 0 runs the tile's vector wavefront.  Tiles the full chain
+// decoded have their records and intra list already; only the wavefront
+// runs for them.
+constexpr int kParseThreads = 128;
+__global__ void __launch_bounds__(kParseThreads) kParse(const FrameDesc* frames, const int4* jobs, int njobs) {
+  __shared__ WarpRows sR;
+  __shared__ int sWarp[kParseThreads / 32];
+  const int jb = blockIdx.x;
+  if (jb >= njobs) return;
+  const int4 job = jobs[jb];
+  if ((int)blockIdx.y >= job.z) return;
+  const FrameDesc* fp = frames + job.x;
+  const int tile = job.y + (int)blockIdx.y;
+  const TileRange tr = fp->tiles[tile];
+  const TileStat st = fp->tileStat[tile];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int mbCols = fp->mbCols, tw = tr.mbX1 - tr.mbX0, total = tw * (tr.mbY1 - tr.mbY0);
+  const int done = st.done;
+  if (st.errAt != kFullChain) {
+    MBRec* const recs = fp->mbrec;
+    // One flag byte per macroblock of the tile (the frame's level grid, spare here).
+    uint8_t* const flags = reinterpret_cast<uint8_t*>(fp->lvgrid) + tr.mbBase;
+    const uint8_t* const log = fp->symLog + (size_t)tr.mbBase * fp->symPerMB;
+    const uint32_t* const off = fp->symOff + tr.mbBase;
+    const int inter = fp->inter;
+    for (int k = tid; k < total; k += kParseThreads) {
+      const int idx = (tr.mbY0 + k / tw) * mbCols + tr.mbX0 + k % tw;
+      if (k >= done) {  // never reached: left untouched by reconstruction
+        recs[idx].mode = kRecNone;
+        recs[idx].wmask = 0;
+        continue;
+      }
+      Replay r;
+      r.log = log;
+      r.k = (int)off[k];
+      r.errAt = st.errAt;
+      r.end = total * fp->symPerMB;
+      r.err = r.k > r.errAt ? kErrCorrupt : 0;
+      flags[k] = (uint8_t)decodeMB<true, true>(r, inter, recs + idx, fp->coef + (size_t)idx * kCoefPerMB, 0);
+    }
+    __syncthreads();
+    int base = 0;
+    for (int k0 = 0; k0 < done; k0 += kParseThreads) {
+      const int k = k0 + tid;
+      const bool f = k < done && flags[k] != 0;
+      const unsigned m = __ballot_sync(kFull, f);
+      if (lane == 0) sWarp[warp] = __popc(m);
+      __syncthreads();
+      int before = base, chunk = 0;
+      for (int w2 = 0; w2 < kParseThreads / 32; w2++) {
+        if (w2 < warp) before += sWarp[w2];
+        chunk += sWarp[w2];
+      }
+      if (f) {
+        const int idx = (tr.mbY0 + k / tw) * mbCols + tr.mbX0 + k % tw;
+        fp->intraList[tr.mbBase + before + __popc(m & ((1u << lane) - 1u))] = (uint32_t)idx;
+      }
+      base += chunk;
+      __syncthreads();
+    }
+    if (tid == 0) fp->tileStat[tile].intraCount = base;
+  }
+  if (fp->inter && warp == 0) predictVectors(fp, tile, done, sR, lane);
 }
 
 // ---------------------------------------------------------------------------
@@ -1483,15 +1713,15 @@ __global__ void __launch_bounds__(32 * W, 16 / W)
 // Launch wrappers
 // ---------------------------------------------------------------------------
 int uploadCodingTables(const int* scan4, const int* scan8, const int* scan16, const int32_t* dct) {
-  uint16_t s[3][256];
+  uint32_t s[3][257];
   std::memset(s, 0, sizeof(s));
   const int* scans[3] = {scan4, scan8, scan16};
   for (int k = 0; k < 3; k++)
     for (int i = 0; i < (16 << (2 * k)); i++) {
       const int band = bandOf(i);
-      s[k][i] = (uint16_t)((uint32_t)scans[k][i] | ((uint32_t)(band * kNumPrevClass) << 8));
+      s[k][i] = (uint32_t)scans[k][i] | ((uint32_t)(band * kNumPrevClass * 64) << 8);
     }
-  if (cudaMemcpyToSymbol(dev::cScanBand, s, sizeof(s)) != cudaSuccess) return kErrDevice;
+  if (cudaMemcpyToSymbol(dev::cScanRow, s, sizeof(s)) != cudaSuccess) return kErrDevice;
   if (cudaMemcpyToSymbol(dev::gDct, dct, sizeof(int32_t) * 3 * 256) != cudaSuccess) return kErrDevice;
   return kOK;
 }
@@ -1514,6 +1744,7 @@ void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* ne
     grid = std::min(njobs, resident[dev]);
   }
   dev::kEntropy<<<grid, 32 * dev::kEntropyWarps, 0, s>>>(frames, jobs, njobs, next);
+  dev::kParse<<<dim3(njobs, kEntropyTilesPerJob), dev::kParseThreads, 0, s>>>(frames, jobs, njobs);
 }
 
 // The reconstruction launches overlap their start with the previous kernel

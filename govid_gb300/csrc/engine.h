@@ -52,6 +52,12 @@ class Engine {
 
   // A stream whose packets are all resident in HBM (uploaded here).
   int addResidentStream(const uint8_t* const* pkts, const size_t* lens, int n, int ring, int* id);
+  // A resident stream that decodes in place from a container in pinned,
+  // device-mapped host memory: packet i is pktLen[i] bytes at offset off[i]
+  // of the container (hostBase for planning, devBase for the kernels).  No
+  // packet is copied; the container must outlive the stream.
+  int addContainerStream(const uint8_t* hostBase, const uint8_t* devBase, const uint64_t* off, const uint32_t* pktLen,
+                         int n, int ring, int* id);
   // A stream fed one packet per round through submit().
   int addStreamingStream(int ring, int* id);
   // Frames per resident stream decoded per round (entropy of all of them in
@@ -76,6 +82,18 @@ class Engine {
   // to ids) caps each stream's frames this round below the lookahead.
   int roundFor(const std::vector<int>& ids, std::vector<RoundResult>* results,
                const std::vector<int>* maxFrames = nullptr);
+  // The Codec contract's round (synchronous engine, one streaming stream):
+  // decodes the stream's pending packet and copies the frame's visible planes
+  // to host memory (y, cb, cr at strides ys, cs) behind the reconstruction on
+  // the same CUDA stream, so the round ends with one wait.  The copy is made
+  // whatever the frame's status; the caller hands the planes out only when
+  // the result's status is 0.
+  // With rgbaDev (W*H*4 bytes of device memory) and rgbaHost non-null, the
+  // frame is also converted to RGBA on the device (convertYCbCr420ToRGBA,
+  // frame.go:8-67) from its device planes and copied to rgbaHost, in the
+  // same round and behind the same single wait.
+  int decodeInto(int id, uint8_t* y, int ys, uint8_t* cb, uint8_t* cr, int cs, std::vector<RoundResult>* results,
+                 uint8_t* rgbaDev = nullptr, uint8_t* rgbaHost = nullptr);
   // Pipelined rounds (set before adding streams; resident streams only):
   // each round() plans a round and starts its entropy stage on a second CUDA
   // stream, collects the round in flight (whose results it returns) and then

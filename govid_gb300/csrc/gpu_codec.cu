@@ -46,6 +46,8 @@ GpuCodec::~GpuCodec() {
   cudaStreamSynchronize(eng_.stream());
   for (uint8_t* p : ring_)
     if (p) cudaFreeHost(p);
+  for (uint8_t* p : rgbaRing_)
+    if (p) cudaFreeHost(p);
   if (dRGBA_) cudaFree(dRGBA_);
 }
 
@@ -82,18 +84,28 @@ int GpuCodec::decode(const uint8_t* pkt, size_t n, DecodedFrame* out) {
   next_ = (next_ + 1) % (int)ring_.size();
   st = eng_.submit(sid_, pkt, n);
   if (st) return st;
-  results_.clear();
-  eng_.roundFor({sid_}, &results_);
-  if (results_.size() != 1) return kErrDevice;
-  const RoundResult& r = results_[0];
-  if (r.status) return r.status;
+  // The frame is copied into its ring image behind the reconstruction, with
+  // one wait for both.  A failed decode leaves the slot's bytes undefined; the
+  // slot's previous frame was already out of its validity window (a frame
+  // stays valid for ring-size further decodes, ebiv/codec.go:15-22).
   uint8_t* img = ring_[(size_t)slot];
   uint8_t* Y = img;
   uint8_t* Cb = img + (size_t)geo_.YStride * geo_.H;
   uint8_t* Cr = Cb + (size_t)geo_.CStride * geo_.CH;
-  st = eng_.downloadStrided(r.view, Y, geo_.YStride, Cb, Cr, geo_.CStride);
-  if (st) return st;
-  if (cudaStreamSynchronize(eng_.stream()) != cudaSuccess) return kErrDevice;
+  uint8_t* rgbaHost = nullptr;
+  if ((size_t)slot < rgbaValid_.size()) rgbaValid_[(size_t)slot] = 0;  // the slot's frame changes
+  if (rgbaOn_) {
+    st = ensureRGBA();
+    if (st) return st;
+    rgbaHost = rgbaRing_[(size_t)slot];
+    rgbaValid_[(size_t)slot] = 0;
+  }
+  results_.clear();
+  eng_.decodeInto(sid_, Y, geo_.YStride, Cb, Cr, geo_.CStride, &results_, rgbaHost ? dRGBA_ : nullptr, rgbaHost);
+  if (results_.size() != 1) return kErrDevice;
+  const RoundResult& r = results_[0];
+  if (r.status) return r.status;
+  if (rgbaHost) rgbaValid_[(size_t)slot] = 1;
   out->y = Y;
   out->cb = Cb;
   out->cr = Cr;
@@ -107,6 +119,38 @@ int GpuCodec::decode(const uint8_t* pkt, size_t n, DecodedFrame* out) {
 }
 
 void GpuCodec::flush() { next_ = 0; }
+
+int GpuCodec::setRGBA(bool on) {
+  rgbaOn_ = on;
+  return kOK;
+}
+
+// The device conversion buffer and the per-slot pinned pool, sized on the
+// first use after the stream's key frame fixed the geometry.
+int GpuCodec::ensureRGBA() {
+  const size_t need = (size_t)geo_.W * geo_.H * 4;
+  if (rgbaCap_ < need) {
+    if (dRGBA_) cudaFree(dRGBA_);
+    dRGBA_ = nullptr;
+    rgbaCap_ = 0;
+    if (cudaMalloc(&dRGBA_, need) != cudaSuccess) return kErrDevice;
+    rgbaCap_ = need;
+  }
+  if (rgbaRing_.size() != ring_.size()) {
+    for (uint8_t* p : rgbaRing_)
+      if (p) cudaFreeHost(p);
+    rgbaRing_.assign(ring_.size(), nullptr);
+    rgbaValid_.assign(ring_.size(), 0);
+    for (auto& p : rgbaRing_)
+      if (cudaMallocHost(&p, need) != cudaSuccess) return kErrDevice;
+  }
+  return kOK;
+}
+
+const uint8_t* GpuCodec::pooledRGBA(int slot) const {
+  if (!rgbaOn_ || slot < 0 || slot >= (int)rgbaRing_.size() || !rgbaValid_[(size_t)slot]) return nullptr;
+  return rgbaRing_[(size_t)slot];
+}
 
 int GpuCodec::rgba(int slot, uint8_t* dst, size_t cap) {
   if (!ready_ || slot < 0 || slot >= (int)ring_.size()) return kErrArg;
@@ -197,6 +241,10 @@ int ebivgpu_frame_rgba(ebivgpu_codec* h, int slot, uint8_t* dst, size_t cap) {
 }
 
 int64_t ebivgpu_codec_launches(ebivgpu_codec* h) { return h ? h->c->launches() : 0; }
+
+int ebivgpu_set_rgba(ebivgpu_codec* h, int enable) { return h ? h->c->setRGBA(enable != 0) : kErrArg; }
+
+const uint8_t* ebivgpu_frame_rgba_pooled(ebivgpu_codec* h, int slot) { return h ? h->c->pooledRGBA(slot) : nullptr; }
 
 const char* ebivgpu_status_string(int s) {
   switch (s) {

@@ -31,6 +31,11 @@ class GpuCodec {
   int decode(const uint8_t* pkt, size_t n, DecodedFrame* out);
   void flush();
   int rgba(int slot, uint8_t* dst, size_t cap);
+  // WithRGBA (source.go:61-74): every later decode also produces the frame's
+  // RGBA, kept in a pinned buffer per ring slot (valid as long as the frame).
+  int setRGBA(bool on);
+  const uint8_t* pooledRGBA(int slot) const;
+  int ensureRGBA();
   int64_t launches() const { return eng_.launches() + extraLaunches_; }
   // Padded reference planes (0 = last reference, 1 = golden), packed.
   int copyReference(int which, uint8_t* dst, size_t cap);
@@ -45,6 +50,9 @@ class GpuCodec {
   int next_ = 0;
   uint8_t* dRGBA_ = nullptr;
   size_t rgbaCap_ = 0;
+  bool rgbaOn_ = false;
+  std::vector<uint8_t*> rgbaRing_;  // pinned W*H*4 per ring slot (WithRGBA)
+  std::vector<char> rgbaValid_;     // slot holds the RGBA of its current frame
   int64_t extraLaunches_ = 0;
   std::vector<RoundResult> results_;
 };

@@ -48,19 +48,18 @@ constexpr uint32_t kWriteAll = 0x3FFFFu;
 // int4{descriptor, first tile, tile count, 0}.
 constexpr int kEntropyTilesPerJob = 4;
 
+// Bytes of symbol log per macroblock in a decode slot (the entropy stage's
+// symbol path; a tile whose symbols do not fit takes the full chain).
+constexpr int kSymPerMB = 96;
+
 struct TileStat {
   int32_t err;         // 0 or an ebiv status
   int32_t intraCount;  // intra macroblocks reconstructed in this tile
-  int32_t maxLevel;    // highest intra dependency level in this tile
-  int32_t pad;
+  int32_t done;        // macroblocks the tile's chain reached (raster order)
+  int32_t errAt;       // symbol path: log index of the failing symbol (or none); -1: full chain
 };
 
-// Intra dependency levels: an intra macroblock's level is one more than the
-// highest level among its intra neighbours (left, above-left, above,
-// above-right within the tile; ebiv/predict.go:50-129), so every macroblock
-// of one level can be reconstructed in parallel once the lower levels are
-// done.  List entries pack the frame macroblock index (bits 0-17) and the
-// level (bits 18-28).
+// Intra list entries hold the frame macroblock index in bits 0-17.
 constexpr int32_t kSkipped = 1000;
 constexpr int kLevelShift = 18;
 constexpr uint32_t kIndexMask = (1u << kLevelShift) - 1;
@@ -101,6 +100,14 @@ struct FrameDesc {
   int32_t prevKey;
   int32_t pad2;
   uint8_t* dep;
+  // Symbol path of the entropy stage (null symLog: every tile takes the full
+  // chain): a log of symPerMB bytes per macroblock, tile t's at
+  // tiles[t].mbBase * symPerMB, and per macroblock the index of its first
+  // symbol in its tile's log (at mbBase + raster index within the tile).
+  uint8_t* symLog;
+  uint32_t* symOff;
+  int32_t symPerMB;
+  int32_t pad3;
 };
 
 }  // namespace ebiv

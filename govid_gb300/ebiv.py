@@ -159,6 +159,22 @@ class Codec:
 
     Flush = flush
 
+    def with_rgba(self, on: bool = True) -> None:
+        """WithRGBA (source.go:61-74): later decodes also convert each frame to
+        RGBA on the GPU into a pinned buffer pooled per ring slot."""
+        _check(self._L.ebivgpu_set_rgba(self._h, int(bool(on))))
+
+    WithRGBA = with_rgba
+
+    def pooled_rgba(self, frame: Frame) -> np.ndarray | None:
+        """The frame's pooled RGBA (h, w, 4), copied out; None when the frame
+        was decoded without WithRGBA or its slot has been reused."""
+        p = self._L.ebivgpu_frame_rgba_pooled(self._h, frame.ring_slot)
+        if not p:
+            return None
+        n = frame.width * frame.height * 4
+        return np.frombuffer(C.string_at(p, n), np.uint8).reshape(frame.height, frame.width, 4)
+
     def rgba(self, frame: Frame) -> np.ndarray:
         out = np.empty((frame.height, frame.width, 4), np.uint8)
         _check(self._L.ebivgpu_frame_rgba(self._h, frame.ring_slot,
@@ -296,6 +312,14 @@ class Batch:
         ln = (C.c_size_t * n)(*lengths)
         _check(self._L.ebivgpu_batch_reload_stream(self._h, sid, a, ln, n), "reload")
 
+    def add_container(self, container: "DeviceContainer", ring: int = 3) -> int:
+        """A resident stream decoding in place from a DeviceContainer (no packet
+        copies); the container must outlive the batch."""
+        sid = C.c_int()
+        _check(self._L.ebivgpu_batch_add_container(self._h, container._h, ring, C.byref(sid)), "add_container")
+        self._keep = getattr(self, "_keep", []) + [container]
+        return sid.value
+
     def planes(self, r: BatchResult) -> "_native.PlaneView":
         v = _native.PlaneView()
         _check(self._L.ebivgpu_batch_result_planes(self._h, r.index, C.byref(v)))
@@ -363,6 +387,115 @@ class Server:
             if self._h:
                 self._L.ebivgpu_server_destroy(self._h)
                 self._h = None
+        except Exception:
+            pass
+
+
+class DeviceContainer:
+    """An EBIV container in pinned, device-mapped host memory whose frame index
+    and seeks are computed on the GPU (ebiv/reader.go:32-238); a Batch stream
+    can decode from it in place (Batch.add_container)."""
+
+    def __init__(self, data: bytes):
+        L = _native.lib()
+        h = C.c_void_p()
+        _check(L.ebivgpu_container_open(data, len(data), C.byref(h)), "NewDemuxer")
+        self._h, self._L = h, L
+        info = (C.c_int64 * 6)()
+        L.ebivgpu_container_info(h, info)
+        self.width, self.height, self.fps_num, self.fps_den, self.frame_count, rebuilt = (int(v) for v in info)
+        self.rebuilt_index = bool(rebuilt)
+
+    def entry(self, i: int) -> tuple[int, int, bool]:
+        """(payload offset, payload size, keyframe) of frame i."""
+        o, n, k = C.c_uint64(), C.c_uint32(), C.c_int()
+        _check(self._L.ebivgpu_container_entry(self._h, int(i), C.byref(o), C.byref(n), C.byref(k)))
+        return o.value, n.value, bool(k.value)
+
+    def seek(self, t_ns: int) -> tuple[int, int]:
+        """Seek(t): (frame index, its presentation time), resolved on the GPU."""
+        f, landed = C.c_int64(), C.c_int64()
+        _check(self._L.ebivgpu_container_seek(self._h, int(t_ns), C.byref(f), C.byref(landed)))
+        return f.value, landed.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.ebivgpu_container_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BlockAnalysis:
+    """forwardDCT and satd (ebiv/transform.go:44-119) of a batch of residual
+    blocks on the GPU."""
+
+    def __init__(self):
+        L = _native.lib()
+        h = C.c_void_p()
+        _check(L.ebivgpu_analysis_create(C.byref(h)), "analysis")
+        self._h, self._L = h, L
+
+    def fdct_satd(self, blocks: np.ndarray, coeffs: bool = True, satd: bool = True):
+        """blocks: (count, n, n) int32 -> (coefficients or None, satd or None)."""
+        b = np.ascontiguousarray(blocks, dtype=np.int32)
+        count, n, _ = b.shape
+        co = np.empty_like(b) if coeffs else None
+        sa = np.empty(count, np.int64) if satd else None
+        ms = C.c_double()
+        _check(self._L.ebivgpu_fdct_satd(self._h, b.ctypes.data, n, count, co.ctypes.data if coeffs else None,
+                                         sa.ctypes.data if satd else None, C.byref(ms)), "fdct_satd")
+        self.kernel_ms = ms.value
+        return co, sa
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._L.ebivgpu_analysis_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+class AltRef:
+    """The encoder's alt-ref temporal filter on the GPU ((*Encoder).buildAltRef,
+    ebiv/encoder.go:326-407): build(frames, w, h, window) returns the packed
+    golden-override image, or None when the reference returns nil."""
+
+    def __init__(self):
+        L = _native.lib()
+        h = C.c_void_p()
+        _check(L.ebivgpu_altref_create(C.byref(h)), "altref")
+        self._h, self._L = h, L
+
+    def build(self, frames: list[bytes], width: int, height: int, window: int) -> bytes | None:
+        n = len(frames)
+        arr = (C.c_char_p * max(n, 1))(*frames)
+        out = (C.c_uint8 * packed_size(width, height))()
+        acc = C.c_int()
+        _check(self._L.ebivgpu_altref_build(self._h, arr, n, width, height, window, out, len(out), C.byref(acc)),
+               "altref")
+        self.accepted = acc.value
+        return bytes(out) if acc.value else None
+
+    def time(self, window: int, reps: int = 10) -> float:
+        """Mean kernel milliseconds on the frames of the last build."""
+        ms = C.c_double()
+        _check(self._L.ebivgpu_altref_time(self._h, window, reps, C.byref(ms)), "altref")
+        return ms.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.ebivgpu_altref_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
 

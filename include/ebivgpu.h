@@ -12,7 +12,13 @@
  *   ebivgpu_flush    <- (*ebiv.Codec).Flush()              ebiv/codec.go:115-117
  *   ebivgpu_destroy  <- (garbage collection of the Codec)
  *   ebivgpu_frame_rgba <- govid.Frame.ConvertRGBA / RGBA   frame.go:72-91
+ *   ebivgpu_set_rgba / ebivgpu_frame_rgba_pooled
+ *                    <- govid.WithRGBA (pooled conversion)  source.go:61-74,131-150
  *   ebivgpu_batch_*  <- many independent Codec.Decode call chains at once
+ *   ebivgpu_altref_* <- (*ebiv.Encoder).buildAltRef        ebiv/encoder.go:326-407
+ *   ebivgpu_fdct_satd <- forwardDCT / satd                ebiv/transform.go:44-119
+ *   ebivgpu_container_* <- ebiv.NewDemuxer index load, Reader.Seek
+ *                                                       ebiv/reader.go:32-160,222-238
  *                       (no single reference counterpart; the reference runs
  *                       one Codec per stream)
  */
@@ -72,6 +78,16 @@ void ebivgpu_destroy(ebivgpu_codec* c);
 /* YCbCr -> RGBA (BT.601 fixed point, frame.go:8-67) of the frame in ring
  * slot `slot`, computed on the GPU; dst holds width*height*4 bytes. */
 int ebivgpu_frame_rgba(ebivgpu_codec* c, int slot, uint8_t* dst, size_t cap);
+/* WithRGBA (source.go:61-74): with enable != 0 every later successful
+ * decode also converts the frame to RGBA on the GPU (BT.601 fixed point,
+ * frame.go:8-67), from the frame's device planes in the same decode round,
+ * into a pinned buffer pooled per ring slot.  ebivgpu_frame_rgba_pooled
+ * returns that buffer (width*height*4 bytes) for the frame in ring slot
+ * `slot`, or NULL when the slot's frame was decoded without it.  The buffer
+ * lives as long as the frame: ring-size further decodes (with a ring of 3 or
+ * more, past govid's "second frame change" lifetime of WithRGBA buffers). */
+int ebivgpu_set_rgba(ebivgpu_codec* c, int enable);
+const uint8_t* ebivgpu_frame_rgba_pooled(ebivgpu_codec* c, int slot);
 /* Kernel launches this codec has issued (for launch accounting). */
 int64_t ebivgpu_codec_launches(ebivgpu_codec* c);
 const char* ebivgpu_status_string(int status);
@@ -195,7 +211,7 @@ uint64_t ebivgpu_frame_hash(const uint8_t* packed, size_t n);
  * Decodes one key-frame packet, as the first frame of a fresh stream (the
  * result and status equal ebivgpu_decode's on a new codec), into the caller's
  * device planes.  All scratch is one static device array of
- * EBIVGPU_NOALLOC_SCRATCH_BYTES (8,490,240) bytes per device, held by every
+ * EBIVGPU_NOALLOC_SCRATCH_BYTES (8,490,496) bytes per device, held by every
  * device that loads the library until the process exits, so frames are
  * limited to EBIVGPU_NOALLOC_MAX_MBS macroblocks
  * (1280x720) and packets to EBIVGPU_NOALLOC_MAX_PACKET bytes; larger ones
@@ -215,10 +231,71 @@ uint64_t ebivgpu_frame_hash(const uint8_t* packed, size_t n);
  * EBIV_ERR_DEVICE before it launches anything, leaving that error in place. */
 #define EBIVGPU_NOALLOC_MAX_MBS 3600
 #define EBIVGPU_NOALLOC_MAX_PACKET (2u << 20)
-#define EBIVGPU_NOALLOC_SCRATCH_BYTES 8490240u
+#define EBIVGPU_NOALLOC_SCRATCH_BYTES 8490496u
 int ebivgpu_decode_key_noalloc(const uint8_t* pkt, size_t n, uint8_t* y, int32_t y_stride, size_t y_cap, uint8_t* cb,
                                uint8_t* cr, int32_t c_stride, size_t c_cap, void* cuda_stream, int32_t* width,
                                int32_t* height);
+
+/* ---- Container ingest on the GPU -------------------------------------------
+ * Replaces ebiv.NewDemuxer's index load and Reader.Seek
+ *   ebiv/reader.go:32-160 (readIndex / scanFrames), ebiv/reader.go:222-238
+ * for a decode that reads the container in place.
+ *
+ * ebivgpu_container_open copies the container once into pinned host memory
+ * mapped into the device, checks the file header (ebiv/format.go:230-265),
+ * and builds the frame index on the GPU: the footer's CRC-checked index, or
+ * a scan of the frame records when the footer does not validate (statuses as
+ * NewDemuxer's).  info6: width, height, fps_num, fps_den, frames, index
+ * rebuilt by scanning (0/1).  ebivgpu_container_entry: frame i's payload
+ * offset in the container, payload size, key flag.  ebivgpu_container_seek
+ * resolves Seek(t) on the GPU: the last key frame at or before the frame
+ * shown at t (frameIndexAt, ebiv/format.go:263-275) and its time; a frame
+ * rate so hostile that frameIndexAt's correction walk does not settle within
+ * 2^20 steps returns EBIV_ERR_CORRUPT.  ebivgpu_batch_add_container adds a
+ * resident batch stream that decodes straight from the pinned bytes: no
+ * packet is copied into HBM, the kernels read them over the host link; the
+ * container must outlive the stream. */
+typedef struct ebivgpu_container ebivgpu_container;
+int ebivgpu_container_open(const uint8_t* data, size_t n, ebivgpu_container** out);
+void ebivgpu_container_close(ebivgpu_container* c);
+int ebivgpu_container_info(ebivgpu_container* c, int64_t* info6);
+int ebivgpu_container_entry(ebivgpu_container* c, int i, uint64_t* payload_offset, uint32_t* size, int* keyframe);
+int ebivgpu_container_seek(ebivgpu_container* c, int64_t t_ns, int64_t* frame, int64_t* landed_ns);
+int ebivgpu_batch_add_container(ebivgpu_batch* b, ebivgpu_container* c, int ring, int* stream_id);
+
+/* ---- Alt-ref temporal filter on the GPU ------------------------------------
+ * Replaces (*ebiv.Encoder).buildAltRef   ebiv/encoder.go:326-407
+ * (the encoder's golden-override image of a GOP, built when WithAltRef is on).
+ *
+ * frames: count host pointers to tightly packed 4:2:0 frames (Y W*H, Cb and
+ * Cr CW*CH each), the GOP in order; the first min(window, count) are
+ * filtered.  On success *accepted is the number of (frame, block) pairs that
+ * agreed with the GOP head; 0 means no alt-ref (the reference returns nil:
+ * window below 3 frames, or nothing agreed) and out is left untouched;
+ * otherwise out receives the packed image (cap >= W*H + 2*CW*CH).  The
+ * handle keeps its device buffers between calls (one caller at a time). */
+typedef struct ebivgpu_altref ebivgpu_altref;
+int ebivgpu_altref_create(ebivgpu_altref** out);
+void ebivgpu_altref_destroy(ebivgpu_altref* a);
+int ebivgpu_altref_build(ebivgpu_altref* a, const uint8_t* const* frames, int count, int width, int height,
+                         int window, uint8_t* out, size_t cap, int* accepted);
+/* Mean device time (CUDA events) of the filter kernel over reps runs on the
+ * frames of the last ebivgpu_altref_build call, already resident. */
+int ebivgpu_altref_time(ebivgpu_altref* a, int window, int reps, double* kernel_ms);
+
+/* ---- The encoder's block analysis on the GPU -------------------------------
+ * Replaces forwardDCT and satd   ebiv/transform.go:44-119
+ * over a batch of blocks (the inner loops of the encoder's rate-distortion
+ * search).  residuals: count row-major n x n int32 blocks (n = 4, 8, 16) in
+ * host memory; coeffs (count*n*n int32) receives each block's forward DCT
+ * and satd (count int64) its Hadamard cost; either may be NULL.  kernel_ms
+ * (optional) receives the kernel's device time.  One caller at a time per
+ * handle. */
+typedef struct ebivgpu_analysis ebivgpu_analysis;
+int ebivgpu_analysis_create(ebivgpu_analysis** out);
+void ebivgpu_analysis_destroy(ebivgpu_analysis* a);
+int ebivgpu_fdct_satd(ebivgpu_analysis* a, const int32_t* residuals, int n, int count, int32_t* coeffs, int64_t* satd,
+                      double* kernel_ms);
 
 /* Non-zero when a CUDA device is usable from this process. */
 int ebivgpu_device_available(void);

@@ -62,6 +62,30 @@ def test_rgba_matches_oracle(gpu_required):
         assert (got[..., 3] == 255).all()
 
 
+def test_with_rgba_pooled_matches_oracle_and_lives_as_long_as_the_frame(gpu_required):
+    # WithRGBA (source.go:61-74): the decode round converts each frame on the
+    # GPU into a per-slot pooled buffer; odd sizes exercise the last chroma column.
+    spec = ebiv.SceneSpec(width=97, height=55, seed=6, sprites=3)
+    cont = ebiv.encode_scene(spec, 7, qp=22, gop=4, tiles=(2, 1), fast=True)
+    pk = [p.data for p in ebiv.Reader(cont).packets()]
+    c = ebiv.Codec(3)
+    f0 = c.decode(pk[0])
+    assert c.pooled_rgba(f0) is None  # decoded before WithRGBA
+    c.with_rgba(True)
+    frames, want = [], []
+    for p in pk[1:]:
+        f = c.decode(p)
+        frames.append(f)
+        want.append(np.frombuffer(ebiv_oracle.rgba(f.packed(), 97, 55), np.uint8).reshape(55, 97, 4))
+        # every frame still inside its ring lifetime keeps its own RGBA
+        for g, w in list(zip(frames, want))[-3:]:
+            got = c.pooled_rgba(g)
+            assert got is not None and (got == w).all()
+    c.with_rgba(False)
+    f = c.decode(pk[4])  # a key frame (gop 4): decodable out of order
+    assert c.pooled_rgba(f) is None
+
+
 def _zero_override_tile(pkt: bytes, tile: int) -> bytes:
     """Zeroes one tile of a key packet's golden-override payload."""
     b = bytearray(pkt)

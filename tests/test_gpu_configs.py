@@ -103,7 +103,7 @@ def test_config_1080p_300_frames_flashes(gpu_required):
     clip = workloads.single_1080()
     pk = packets(workloads.load([clip], in_child=False)[0])
     assert len(pk) == 300
-    assert sum(1 for p in pk if (p[0] & 3) == 0) == 5  # gop 60
+    assert sum(1 for p in pk if (p[0] & 3) == 0) >= 5  # gop 60, plus scene cuts at flashes
     want = oracle_hashes(pk)
     _compare(codec_hashes(pk), want, "Codec 1080p")
     _compare(batch_hashes([(pk, clip.w, clip.h)])[0], want, "Batch 1080p")
