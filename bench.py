@@ -429,12 +429,147 @@ def run_gpu(args):
             r = eval_mvnet.compare(1920, 1080, nframes=args.mv_frames, qp=22, log=None)
             r["note"] = "encoder on the host cores; the proposer's net runs on this GPU"
             out["learned_mv"] = r
+        if not args.no_extras:
+            out["rgba"] = run_rgba(pkts, want)
+            out["ingest"] = run_ingest(clip, pkts, want)
+            out["altref"] = run_altref()
+            out["block_analysis"] = run_analysis()
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(pkts, args.cpu_seconds)
         out["clocks"] = ck.summary()
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_rgba(pkts, want):
+    """WithRGBA (source.go:61-74): the Codec contract with the RGBA pass in
+    each decode round (kRGBA on the device frame, pooled pinned output),
+    against the same contract without it and the CPU conversion
+    (frame.go:8-67, the oracle's C++ restatement) per 1080p frame."""
+    import numpy as np
+
+    from govid_gb300 import ebiv
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import ebiv_oracle
+
+    c = ebiv.Codec(3)
+    c.with_rgba(True)
+    for p in pkts[:30]:
+        c.decode(p)
+    c.flush()
+    t0 = time.perf_counter()
+    for p in pkts:
+        c.decode(p)
+    fps = len(pkts) / (time.perf_counter() - t0)
+    # bit-exactness of the pooled RGBA on a few frames of a fresh pass
+    c.flush()
+    bad = 0
+    for i, p in enumerate(pkts[:8]):
+        f = c.decode(p)
+        ref = np.frombuffer(ebiv_oracle.rgba(f.packed(), W, H), np.uint8).reshape(H, W, 4)
+        bad += int(not (c.pooled_rgba(f) == ref).all())
+    c.close()
+    if bad:
+        raise RuntimeError(f"rgba: {bad} frame(s) differ from the oracle")
+    f0 = ebiv_oracle.decode_all(pkts[:1])[0][1]
+    t0 = time.perf_counter()
+    reps = 20
+    for _ in range(reps):
+        ebiv_oracle.rgba(f0, W, H)
+    cpu_ms = (time.perf_counter() - t0) * 1000 / reps
+    return {"codec_with_rgba_frames_per_s": round(fps, 2), "bit_exact_frames_checked": 8,
+            "cpu_rgba_ms_per_1080p_frame": round(cpu_ms, 3),
+            "note": "CPU: the oracle's C++ restatement of convertYCbCr420ToRGBA, one thread"}
+
+
+def run_ingest(clip, pkts, want):
+    """Container ingest on the GPU: index build and seeks on the device over
+    the pinned container, and a batch stream decoding in place from it,
+    bit-exact, against the same stream with its packets copied to HBM."""
+    from govid_gb300 import ebiv
+
+    t0 = time.perf_counter()
+    dc = ebiv.DeviceContainer(clip)
+    open_ms = (time.perf_counter() - t0) * 1000
+    r = ebiv.Reader(clip)
+    t0 = time.perf_counter()
+    seeks = [k * 997_000_000 // 7 for k in range(64)]
+    for t in seeks:
+        assert dc.seek(t)[1] == r.seek(t)
+    seek_us = (time.perf_counter() - t0) * 1e6 / len(seeks)
+    out = {"open_ms": round(open_ms, 3), "seek_us": round(seek_us, 2), "frames": dc.frame_count}
+    for name, add in (("in_place", lambda b: b.add_container(dc)), ("copied", lambda b: b.add_stream(pkts))):
+        b = ebiv.Batch(lookahead=32, pipeline=3)
+        sid = add(b)
+        for rep in range(3):
+            b.seek(sid, 0)
+            t0 = time.perf_counter()
+            n = sum(1 for x in all_rounds(b) if x.status == 0)
+            dt = time.perf_counter() - t0
+        out[f"{name}_frames_per_s"] = round(n / dt, 2)
+        got = batch_hashes(b, {sid: (W, H)})
+        if [got[(sid, i)] for i in range(len(pkts))] != want:
+            raise RuntimeError(f"ingest {name}: frames differ from the oracle")
+        b.close()
+    out["bit_exact"] = True
+    return out
+
+
+def run_altref():
+    """The alt-ref temporal filter ((*Encoder).buildAltRef,
+    ebiv/encoder.go:326-407) on the GPU over 16 1080p frames: kernel time and
+    HBM rate (16 frames read, one written), bit-exact against the numpy
+    restatement."""
+    from govid_gb300 import ebiv
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import altref_ref
+
+    sc = ebiv.Scene(ebiv.SceneSpec(width=W, height=H, seed=9, sprites=24, noise_y16=16, noise_c16=8))
+    frames = [sc.render(i) for i in range(16)]
+    a = ebiv.AltRef()
+    got = a.build(frames, W, H, 16)
+    t0 = time.perf_counter()
+    want = altref_ref.build_altref(frames, W, H, 16)
+    cpu_s = time.perf_counter() - t0
+    if got != want:
+        raise RuntimeError("altref: GPU filter differs from the oracle")
+    ms = a.time(16, 20)
+    S = frame_bytes(W, H)
+    gbs = 17 * S / (ms / 1000) / 1e9
+    peak, _ = peak_hbm()
+    return {"frames": 16, "kernel_ms": round(ms, 4), "hbm_gbs": round(gbs, 2), "hbm_frac": round(gbs / peak, 4),
+            "accepted_blocks": a.accepted, "bit_exact": True, "oracle_numpy_s": round(cpu_s, 3)}
+
+
+def run_analysis():
+    """forwardDCT + satd (ebiv/transform.go:44-119) of 1M 8x8 residual
+    blocks on the GPU, kernel time, bit-exact on a sample against the numpy
+    restatement."""
+    import numpy as np
+
+    from govid_gb300 import ebiv
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import transform_ref
+
+    rng = np.random.default_rng(1)
+    blocks = rng.integers(-255, 256, size=(1 << 20, 8, 8), dtype=np.int64).astype(np.int32)
+    a = ebiv.BlockAnalysis()
+    co, sa = a.fdct_satd(blocks)
+    co, sa = a.fdct_satd(blocks)
+    ms = a.kernel_ms
+    k = 4096
+    if not ((co[:k] == transform_ref.forward_dct(blocks[:k], 8)).all() and
+            (sa[:k] == transform_ref.satd(blocks[:k], 8)).all()):
+        raise RuntimeError("block analysis differs from the oracle")
+    byts = blocks.nbytes * 2 + sa.nbytes
+    peak, _ = peak_hbm()
+    return {"blocks": len(blocks), "n": 8, "kernel_ms": round(ms, 4), "blocks_per_s": round(len(blocks) / ms * 1e3),
+            "hbm_gbs": round(byts / (ms / 1000) / 1e9, 2), "hbm_frac": round(byts / (ms / 1000) / 1e9 / peak, 4),
+            "bit_exact_sample": k}
 
 
 def run_batched(args):
@@ -724,6 +859,7 @@ def main():
     ap.add_argument("--serve-max-frames", type=int, default=2)
     ap.add_argument("--serve-seed", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the RGBA, ingest, alt-ref and analysis legs")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     if args.impl == "reference":

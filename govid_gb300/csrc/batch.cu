@@ -12,7 +12,7 @@
 
 namespace ebiv {
 
-void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* next, cudaStream_t s);
+void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* next, int maxTileMBs, cudaStream_t s);
 void launchInter(const FrameDesc* frames, int nframes, int maxMBs, int phase, cudaStream_t s);
 void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, int maxTileKeys, cudaStream_t s);
 void launchRGBA(const uint8_t* y, const uint8_t* cb, const uint8_t* cr, int ys, int cs, int w, int h, uint8_t* dst,
@@ -981,7 +981,7 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
   const int4* de = reinterpret_cast<const int4*>(d + R.oEJobs);
   if (timing_) cudaEventRecord(ev_[P][0], se);
   if (R.groups == 1) {
-    launchEntropy(dd, de, nEJobs, reinterpret_cast<int32_t*>(d + oQueue), se);
+    launchEntropy(dd, de, nEJobs, reinterpret_cast<int32_t*>(d + oQueue), R.maxTileMBs, se);
     launches_++;
     cudaEventRecord(ev_[P][1], se);  // entropy done
   } else {
@@ -993,7 +993,7 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
       nextEG_ = (nextEG_ + 1) % kEntropyStreams;
       if (cudaStreamWaitEvent(sg, evUp_[P], 0) != cudaSuccess) return -1;
       launchEntropy(dd, de + groupFirst[g], groupFirst[g + 1] - groupFirst[g],
-                    reinterpret_cast<int32_t*>(d + oQueue + 64 * (size_t)g), sg);
+                    reinterpret_cast<int32_t*>(d + oQueue + 64 * (size_t)g), R.maxTileMBs, sg);
       launches_++;
       if (cudaEventRecord(evGroup_[P][g], sg) != cudaSuccess) return -1;
     }

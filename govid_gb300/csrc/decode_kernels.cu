@@ -145,9 +145,13 @@ struct ChainT {
   // (context * 64).
   __device__ __forceinline__ int symAt(int row) {
     if (err) return 0;
+    return finish(t->bucket[row + (int)((x0 & (kM - 1)) >> 6)], row);
+  }
+  // Completes the next symbol from its bucket entry e (of row `row`, at the
+  // current state's slot), loaded ahead by the caller.
+  __device__ __forceinline__ int finish(uint32_t e, int row) {
     const uint32_t x = x0;
     const uint32_t slot = x & (kM - 1);
-    const uint32_t e = t->bucket[row + (int)(slot >> 6)];
     int s = (int)((e >> 25) & 15u);
     uint32_t start = e & 0xFFFu, freq = (e >> 12) & 0x1FFFu;
     if (e & (kBImpure | kBUnused)) {
@@ -557,14 +561,16 @@ __device__ void predictVectors(const FrameDesc* fp, int tile, int done, WarpRows
     MBRec* const rowRec = recs + (size_t)(y0 + min(ry, th - 1)) * mbCols + x0;
     const int rowDone = ry < th ? min(tw, done - ry * tw) : 0;  // columns of this row the chain reached
     uint32_t h1 = 0, h2 = 0, h3 = 0;  // this lane's results of steps t-1, t-2, t-3
-    // Record words 0-3 of the step's macroblock, loaded one step ahead.
-    uint4 cur = make_uint4(0u, 0u, 0u, 0u);
-    if (lane == 0 && rowDone > 0) cur = reinterpret_cast<const uint4*>(rowRec)[0];
+    // Record words 0-3 of the macroblocks of steps t .. t+3, loaded four
+    // steps ahead so the global-memory latency overlaps the steps between.
+    auto recAt = [&](int x) {
+      return x >= 0 && x < rowDone ? reinterpret_cast<const uint4*>(rowRec + x)[0] : make_uint4(0u, 0u, 0u, 0u);
+    };
+    uint4 cur = recAt(-2 * lane), q1 = recAt(1 - 2 * lane), q2 = recAt(2 - 2 * lane), q3 = recAt(3 - 2 * lane);
     for (int t = 0; t < steps; t++) {
       const int rx = t - 2 * lane;
       const bool act = rx >= 0 && rx < rowDone;
-      uint4 nxt = make_uint4(0u, 0u, 0u, 0u);
-      if (rx + 1 >= 0 && rx + 1 < rowDone) nxt = reinterpret_cast<const uint4*>(rowRec + rx + 1)[0];
+      const uint4 nxt = recAt(rx + 4);
       uint32_t above = __shfl_up_sync(kFull, h2, 1);
       uint32_t ar = __shfl_up_sync(kFull, h1, 1);
       uint32_t al = __shfl_up_sync(kFull, h3, 1);
@@ -610,7 +616,10 @@ __device__ void predictVectors(const FrameDesc* fp, int tile, int done, WarpRows
         }
         if (lastRowOfPass) nextUp[rx] = out;
       }
-      cur = nxt;
+      cur = q1;
+      q1 = q2;
+      q2 = q3;
+      q3 = nxt;
       h3 = h2;
       h2 = h1;
       h1 = out;
@@ -787,16 +796,94 @@ __global__ void __launch_bounds__(32 * kEntropyWarps, 4) kEntropy(const FrameDes
   }
 }
 
-// Rebuilds the records of the symbol-path tiles from their logs: one CTA per
-// tile of a job.  Each thread replays one macroblock at a time from its
-// first symbol (decodeMB, one thread per macroblock), so a tile's records,
-// coefficient regions and write masks come out in parallel; then the CTA
-// lists the tile's written intra macroblocks in raster order, and (inter
-// frames) warp 0 runs the tile's vector wavefront.  Tiles the full chain
-// decoded have their records and intra list already; only the wavefront
-// runs for them.
+// Rebuilds the records of the symbol-path tiles from their logs, one warp
+// per macroblock over every macroblock of the launch's tiles (grid.y: job *
+// kEntropyTilesPerJob + tile within the job; grid.x * kParseWarps: the
+// macroblock's raster index within its tile).  The warp first copies a
+// window of the tile's log from the macroblock's first symbol into shared
+// memory (aligned 16-byte loads), then replays the macroblock's grammar
+// (decodeMB, the warp's lanes writing the record and the coefficient
+// regions) reading the window, and past it the log in global memory.  A flag
+// per macroblock marks the written intra ones for kTileFinish.
+constexpr int kParseWarps = 8;
+constexpr int kParseWindow = 512;  // bytes of log per warp in shared memory
+
+struct WindowReplay {
+  const uint8_t* win;  // shared: log bytes [w0, w0 + wlen)
+  const uint8_t* log;  // global: the tile's log
+  int32_t w0, wlen, k, errAt, end, err;
+  __device__ __forceinline__ int symAt(int) {
+    if (err) return 0;
+    if (k >= end) {  // unreachable while replay and chain agree; keeps every read in bounds
+      err = kErrCorrupt;
+      return 0;
+    }
+    const int r = k - w0;
+    const int s = r < wlen ? win[r] : log[k];
+    k++;
+    if (k > errAt) err = kErrCorrupt;
+    return s;
+  }
+  __device__ __forceinline__ int sym(int) { return symAt(0); }
+  __device__ __forceinline__ bool room(int) const { return true; }
+};
+
+__global__ void __launch_bounds__(32 * kParseWarps) kParseMB(const FrameDesc* frames, const int4* jobs, int njobs) {
+  __shared__ __align__(16) uint8_t sWin[kParseWarps][kParseWindow];
+  const int jb = (int)blockIdx.x / kEntropyTilesPerJob, tj = (int)blockIdx.x % kEntropyTilesPerJob;
+  if (jb >= njobs) return;
+  const int4 job = jobs[jb];
+  if (tj >= job.z) return;
+  const FrameDesc* fp = frames + job.x;
+  const int tile = job.y + tj;
+  const TileStat st = fp->tileStat[tile];
+  if (st.errAt == kFullChain) return;
+  const TileRange tr = fp->tiles[tile];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tw = tr.mbX1 - tr.mbX0, total = tw * (tr.mbY1 - tr.mbY0);
+  const int k = (int)blockIdx.y * kParseWarps + warp;
+  if (k >= total) return;
+  const int idx = (tr.mbY0 + k / tw) * fp->mbCols + tr.mbX0 + k % tw;
+  MBRec* const rec = fp->mbrec + idx;
+  uint8_t* const flags = reinterpret_cast<uint8_t*>(fp->lvgrid) + tr.mbBase;
+  if (k >= st.done) {  // never reached: left untouched by reconstruction
+    if (lane == 0) {
+      rec->mode = kRecNone;
+      rec->wmask = 0;
+      flags[k] = 0;
+    }
+    return;
+  }
+  const uint8_t* const log = fp->symLog + (size_t)tr.mbBase * fp->symPerMB;
+  const int end = total * fp->symPerMB;
+  const int first = (int)fp->symOff[tr.mbBase + k];
+  // The window: the aligned 16-byte blocks from the one holding the first
+  // symbol, clipped to the tile's log.
+  const int w0 = first & ~15;
+  const int wlen = max(0, min(kParseWindow, (end & ~15) - w0));  // whole 16-byte blocks only
+  uint8_t* const win = sWin[warp];
+  for (int o = lane * 16; o < wlen; o += 32 * 16)
+    *reinterpret_cast<uint4*>(win + o) = *reinterpret_cast<const uint4*>(log + w0 + o);
+  __syncwarp();
+  WindowReplay r;
+  r.win = win;
+  r.log = log;
+  r.w0 = w0;
+  r.wlen = wlen;
+  r.k = first;
+  r.errAt = st.errAt;
+  r.end = end;
+  r.err = r.k > r.errAt ? kErrCorrupt : 0;
+  const int f = decodeMB<true, false>(r, fp->inter, rec, fp->coef + (size_t)idx * kCoefPerMB, lane);
+  if (lane == 0) flags[k] = (uint8_t)f;
+}
+
+// After kParseMB: per tile (one CTA per tile of a job) the written intra
+// macroblocks listed in raster order, and (inter frames) the tile's vector
+// wavefront.  Tiles the full chain decoded have their intra list already;
+// only the wavefront runs for them.
 constexpr int kParseThreads = 128;
-__global__ void __launch_bounds__(kParseThreads) kParse(const FrameDesc* frames, const int4* jobs, int njobs) {
+__global__ void __launch_bounds__(kParseThreads) kTileFinish(const FrameDesc* frames, const int4* jobs, int njobs) {
   __shared__ WarpRows sR;
   __shared__ int sWarp[kParseThreads / 32];
   const int jb = blockIdx.x;
@@ -808,31 +895,10 @@ __global__ void __launch_bounds__(kParseThreads) kParse(const FrameDesc* frames,
   const TileRange tr = fp->tiles[tile];
   const TileStat st = fp->tileStat[tile];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int mbCols = fp->mbCols, tw = tr.mbX1 - tr.mbX0, total = tw * (tr.mbY1 - tr.mbY0);
+  const int mbCols = fp->mbCols, tw = tr.mbX1 - tr.mbX0;
   const int done = st.done;
   if (st.errAt != kFullChain) {
-    MBRec* const recs = fp->mbrec;
-    // One flag byte per macroblock of the tile (the frame's level grid, spare here).
-    uint8_t* const flags = reinterpret_cast<uint8_t*>(fp->lvgrid) + tr.mbBase;
-    const uint8_t* const log = fp->symLog + (size_t)tr.mbBase * fp->symPerMB;
-    const uint32_t* const off = fp->symOff + tr.mbBase;
-    const int inter = fp->inter;
-    for (int k = tid; k < total; k += kParseThreads) {
-      const int idx = (tr.mbY0 + k / tw) * mbCols + tr.mbX0 + k % tw;
-      if (k >= done) {  // never reached: left untouched by reconstruction
-        recs[idx].mode = kRecNone;
-        recs[idx].wmask = 0;
-        continue;
-      }
-      Replay r;
-      r.log = log;
-      r.k = (int)off[k];
-      r.errAt = st.errAt;
-      r.end = total * fp->symPerMB;
-      r.err = r.k > r.errAt ? kErrCorrupt : 0;
-      flags[k] = (uint8_t)decodeMB<true, true>(r, inter, recs + idx, fp->coef + (size_t)idx * kCoefPerMB, 0);
-    }
-    __syncthreads();
+    const uint8_t* const flags = reinterpret_cast<const uint8_t*>(fp->lvgrid) + tr.mbBase;
     int base = 0;
     for (int k0 = 0; k0 < done; k0 += kParseThreads) {
       const int k = k0 + tid;
@@ -1728,7 +1794,7 @@ int uploadCodingTables(const int* scan4, const int* scan8, const int* scan16, co
 
 // next: a zeroed device counter for the persistent grid (sized to the CTAs
 // the device holds at once), or null for one CTA per job.
-void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* next, cudaStream_t s) {
+void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* next, int maxTileMBs, cudaStream_t s) {
   if (njobs <= 0) return;
   static int resident[64] = {0};
   int dev = 0;
@@ -1744,7 +1810,9 @@ void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* ne
     grid = std::min(njobs, resident[dev]);
   }
   dev::kEntropy<<<grid, 32 * dev::kEntropyWarps, 0, s>>>(frames, jobs, njobs, next);
-  dev::kParse<<<dim3(njobs, kEntropyTilesPerJob), dev::kParseThreads, 0, s>>>(frames, jobs, njobs);
+  dev::kParseMB<<<dim3(njobs * kEntropyTilesPerJob, (maxTileMBs + dev::kParseWarps - 1) / dev::kParseWarps),
+                  32 * dev::kParseWarps, 0, s>>>(frames, jobs, njobs);
+  dev::kTileFinish<<<dim3(njobs, kEntropyTilesPerJob), dev::kParseThreads, 0, s>>>(frames, jobs, njobs);
 }
 
 // The reconstruction launches overlap their start with the previous kernel

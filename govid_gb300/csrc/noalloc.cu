@@ -31,7 +31,7 @@
 
 namespace ebiv {
 
-void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* next, cudaStream_t s);
+void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* next, int maxTileMBs, cudaStream_t s);
 void launchInter(const FrameDesc* frames, int nframes, int maxMBs, int phase, cudaStream_t s);
 void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, int maxTileKeys, cudaStream_t s);
 
@@ -228,14 +228,14 @@ extern "C" int ebivgpu_decode_key_noalloc(const uint8_t* pkt, size_t n, uint8_t*
     maxKeys = std::max(maxKeys, 4 * (w - 1) + 11 * (h - 1) + 1);
   }
   // Each launch is checked where it is made.
-  launchEntropy(dd, de, groups(nt0), nullptr, s);
+  launchEntropy(dd, de, groups(nt0), nullptr, (int)mbs, s);
   if (cudaGetLastError() != cudaSuccess) return kErrDevice;
   launchInter(dd, 1, (int)mbs, 0, s);  // the intra macroblocks' residuals
   if (cudaGetLastError() != cudaSuccess) return kErrDevice;
   launchIntra(dd, dj, nt0, maxTile, maxKeys, s);
   if (cudaGetLastError() != cudaSuccess) return kErrDevice;
   if (withOv) {  // after the key's reconstruction, which reads the records it overwrites
-    launchEntropy(dd, de + kNAMaxEJobs, groups((int)plan[1].tiles.size()), nullptr, s);
+    launchEntropy(dd, de + kNAMaxEJobs, groups((int)plan[1].tiles.size()), nullptr, (int)mbs, s);
     if (cudaGetLastError() != cudaSuccess) return kErrDevice;
   }
   if (cudaMemcpyAsync(status, d + kOffStatus, sizeof(status), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
