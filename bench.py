@@ -593,8 +593,9 @@ def run_batched(args):
     peak, _ = peak_hbm()
     depth = 0 if args.no_pipeline else args.mix_depth
 
-    def one(lookahead):
-        b = ebiv.Batch(lookahead=lookahead, pipeline=depth)
+    def one(lookahead, dep=depth, groups=4, warps=0):
+        b = ebiv.Batch(lookahead=lookahead, pipeline=dep)
+        b.set_tuning(groups, warps)
         ids = [b.add_stream(pk, ring=3) for pk in pkts]
         for sid in ids:  # warm-up round
             b.seek(sid, 0)
@@ -617,7 +618,8 @@ def run_batched(args):
         kernel_ms, _, _ = b.timing(-1)
         fps = frames / (te - ts)
         gbs = alg / (te - ts) / 1e9
-        res = {"lookahead_frames": lookahead, "frames": frames, "frames_per_s": round(fps, 2),
+        res = {"lookahead_frames": lookahead, "pipeline_depth": dep, "entropy_groups": groups, "intra_warps": warps,
+               "frames": frames, "frames_per_s": round(fps, 2),
                "frames_1080p_equiv_per_s": round(eq1080 / (te - ts), 2),
                "round_latency_ms": {"p50": round(1000 * statistics.median(lat), 3),
                                     "p99": round(1000 * pct(lat, 0.99), 3)},
@@ -636,6 +638,19 @@ def run_batched(args):
             check_b, check_ids = b, ids
         else:
             b.close()
+    # The autotuner's choice (throughput objective, tried on 16-frame prefixes).
+    tuned = None
+    if not args.no_autotune:
+        from govid_gb300 import autotune
+
+        t0 = time.time()
+        tn = autotune.tune(pkts, frames=16, objective="throughput")
+        c = tn["choice"]
+        res, b, _ = one(c["lookahead"], c["pipeline_depth"], c["entropy_groups"], c["intra_warps"])
+        b.close()
+        tuned = {"choice": {k: c[k] for k in ("lookahead", "pipeline_depth", "entropy_groups", "intra_warps")},
+                 "tuning_s": round(time.time() - t0, 1), "trials": len(tn["trials"]), "run": res,
+                 "vs_hand_picked_throughput_config": round(res["frames_per_s"] / runs[-1]["frames_per_s"], 3)}
     # Bit-exactness of the batched decode: every frame of every stream.
     want = oracle_hashes(pkts, os.cpu_count() or 1)
     got = batch_hashes(check_b, {sid: dims[i] for i, sid in enumerate(check_ids)})
@@ -696,6 +711,9 @@ def run_batched(args):
     out.update(runs[0])
     if len(runs) > 1:
         out["throughput_config"] = runs[-1]
+    if tuned:
+        tuned["run"]["speedup_vs_one_stream_per_launch"] = round(tuned["run"]["frames_per_s"] / per_launch_fps, 3)
+        out["autotuned"] = tuned
     out["packet_bytes"] = totals
     return out
 
@@ -860,6 +878,7 @@ def main():
     ap.add_argument("--serve-seed", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the RGBA, ingest, alt-ref and analysis legs")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     if args.impl == "reference":

@@ -104,6 +104,7 @@ def lib() -> C.CDLL:
     _sig(L, "ebivgpu_batch_timing", I, P, I, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double))
     _sig(L, "ebivgpu_batch_set_lookahead", I, P, I)
     _sig(L, "ebivgpu_batch_set_pipeline", I, P, I)
+    _sig(L, "ebivgpu_batch_set_tuning", I, P, I, I)
     _sig(L, "ebivgpu_batch_reload_stream", I, P, I, C.POINTER(C.c_void_p), C.POINTER(S), I)
     _sig(L, "ebivgpu_batch_result_download_async", I, P, I, C.c_void_p, S)
     _sig(L, "ebivgpu_batch_sync", I, P)

@@ -14,7 +14,8 @@ namespace ebiv {
 
 void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* next, int maxTileMBs, cudaStream_t s);
 void launchInter(const FrameDesc* frames, int nframes, int maxMBs, int phase, cudaStream_t s);
-void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, int maxTileKeys, cudaStream_t s);
+void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, int maxTileKeys, int warps,
+                 cudaStream_t s);
 void launchRGBA(const uint8_t* y, const uint8_t* cb, const uint8_t* cr, int ys, int cs, int w, int h, uint8_t* dst,
                 cudaStream_t s);
 
@@ -828,7 +829,7 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
   // reconstruction waits only for its own group: the long chains of a large
   // frame late in the round do not hold back the steps before it.
   const int nsteps = (int)R.steps.size();
-  R.groups = (P != kSide && pipeDepth_ && streamEG_[0] && nsteps > 1) ? std::min(kEntropyGroups, nsteps) : 1;
+  R.groups = (P != kSide && pipeDepth_ && streamEG_[0] && nsteps > 1) ? std::min(entropyGroups_, nsteps) : 1;
   R.stepsPerGroup = (nsteps + R.groups - 1) / R.groups;
   R.groups = (nsteps + R.stepsPerGroup - 1) / R.stepsPerGroup;
   R.oDesc = 0;
@@ -1073,12 +1074,12 @@ int Engine::launchRecon(Round& R) {
       if (cudaEventRecord(stepB_[P][st + 1], streamB_) != cudaSuccess) return -1;
     }
     if (si.jobCount > 0) {
-      launchIntra(dd, dj + si.jobFirst, si.jobCount, R.maxTileMBs, R.maxTileKeys, sr);
+      launchIntra(dd, dj + si.jobFirst, si.jobCount, R.maxTileMBs, R.maxTileKeys, intraWarps_, sr);
       launches_++;
     }
     if (si.ovCount > 0) {
       launchInter(dd + si.ovFirst, si.ovCount, si.maxOvMBs, 0, sr);
-      launchIntra(dd, dj + si.ovJobFirst, si.ovJobCount, R.maxTileMBs, R.maxTileKeys, sr);
+      launchIntra(dd, dj + si.ovJobFirst, si.ovJobCount, R.maxTileMBs, R.maxTileKeys, intraWarps_, sr);
       launches_ += 2;
     }
   }
@@ -1487,6 +1488,10 @@ int ebivgpu_batch_timing(ebivgpu_batch* b, int enable, double* kernel_ms, double
 int ebivgpu_batch_set_lookahead(ebivgpu_batch* b, int frames) { return b ? b->e.setLookahead(frames) : kErrArg; }
 
 int ebivgpu_batch_set_pipeline(ebivgpu_batch* b, int depth) { return b ? b->e.setPipelined(depth) : kErrArg; }
+
+int ebivgpu_batch_set_tuning(ebivgpu_batch* b, int entropy_groups, int intra_warps) {
+  return b ? b->e.setTuning(entropy_groups, intra_warps) : kErrArg;
+}
 
 int ebivgpu_batch_drain(ebivgpu_batch* b, int* frames) {
   if (!b) return kErrArg;

@@ -1854,9 +1854,10 @@ static void launchIntraW(const FrameDesc* frames, const int2* jobs, int njobs, i
 
 // maxTileMBs: the largest tile of the launch's frames, in macroblocks;
 // maxTileKeys: the largest wavefront key range of its tiles (4*(w-1) +
-// 11*(h-1) + 1 for a tile of w x h macroblocks).  The warps per CTA follow
-// the tile count: 16 up to one CTA per SM, 8 up to two, else 4.
-void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, int maxTileKeys,
+// 11*(h-1) + 1 for a tile of w x h macroblocks).  warps: the warps per CTA
+// (4, 8 or 16; anything else picks by the tile count: 16 up to one CTA per
+// SM, 8 up to two, else 4).
+void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, int maxTileKeys, int warps,
                  cudaStream_t s) {
   if (njobs <= 0) return;
   static int sms[64] = {0};
@@ -1880,9 +1881,10 @@ void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTi
   const int flagMBs = std::max(1, std::min(maxTileMBs, dev::kIntraFlagMBs));
   int sortInts = std::max(0, maxTileMBs) + std::max(0, maxTileKeys);
   if (4 * (size_t)sortInts > (size_t)dev::kIntraSortBytes) sortInts = 0;  // raster order
-  if (njobs <= nsm)
+  if (warps != 4 && warps != 8 && warps != 16) warps = njobs <= nsm ? 16 : (njobs <= 2 * nsm ? 8 : 4);
+  if (warps == 16)
     launchIntraW<16>(frames, jobs, njobs, flagMBs, sortInts, s);
-  else if (njobs <= 2 * nsm)
+  else if (warps == 8)
     launchIntraW<8>(frames, jobs, njobs, flagMBs, sortInts, s);
   else
     launchIntraW<4>(frames, jobs, njobs, flagMBs, sortInts, s);

@@ -94,6 +94,17 @@ class Engine {
   // same round and behind the same single wait.
   int decodeInto(int id, uint8_t* y, int ys, uint8_t* cb, uint8_t* cr, int cs, std::vector<RoundResult>* results,
                  uint8_t* rgbaDev = nullptr, uint8_t* rgbaHost = nullptr);
+  // Launch shapes (the autotuner's knobs; any time): the most entropy
+  // launches a pipelined round splits its steps into (1 to 4), and the warps
+  // per CTA of the intra stage (4, 8, 16; 0 picks by the tile count).
+  int setTuning(int entropyGroups, int intraWarps) {
+    if (entropyGroups < 1 || entropyGroups > kEntropyGroups ||
+        (intraWarps != 0 && intraWarps != 4 && intraWarps != 8 && intraWarps != 16))
+      return kErrArg;
+    entropyGroups_ = entropyGroups;
+    intraWarps_ = intraWarps;
+    return kOK;
+  }
   // Pipelined rounds (set before adding streams; resident streams only):
   // each round() plans a round and starts its entropy stage on a second CUDA
   // stream, collects the round in flight (whose results it returns) and then
@@ -184,6 +195,8 @@ class Engine {
   // take in turn (so the groups of consecutive rounds run side by side), the
   // staging-upload event and one completion event per group.
   static constexpr int kEntropyGroups = 4;
+  int entropyGroups_ = kEntropyGroups;
+  int intraWarps_ = 0;
   static constexpr int kEntropyStreams = 2 * kEntropyGroups;
   cudaStream_t streamEG_[kEntropyStreams] = {};
   int nextEG_ = 0;

@@ -33,7 +33,8 @@ namespace ebiv {
 
 void launchEntropy(const FrameDesc* frames, const int4* jobs, int njobs, int* next, int maxTileMBs, cudaStream_t s);
 void launchInter(const FrameDesc* frames, int nframes, int maxMBs, int phase, cudaStream_t s);
-void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, int maxTileKeys, cudaStream_t s);
+void launchIntra(const FrameDesc* frames, const int2* jobs, int njobs, int maxTileMBs, int maxTileKeys, int warps,
+                 cudaStream_t s);
 
 namespace {
 
@@ -232,7 +233,7 @@ extern "C" int ebivgpu_decode_key_noalloc(const uint8_t* pkt, size_t n, uint8_t*
   if (cudaGetLastError() != cudaSuccess) return kErrDevice;
   launchInter(dd, 1, (int)mbs, 0, s);  // the intra macroblocks' residuals
   if (cudaGetLastError() != cudaSuccess) return kErrDevice;
-  launchIntra(dd, dj, nt0, maxTile, maxKeys, s);
+  launchIntra(dd, dj, nt0, maxTile, maxKeys, 0, s);
   if (cudaGetLastError() != cudaSuccess) return kErrDevice;
   if (withOv) {  // after the key's reconstruction, which reads the records it overwrites
     launchEntropy(dd, de + kNAMaxEJobs, groups((int)plan[1].tiles.size()), nullptr, (int)mbs, s);

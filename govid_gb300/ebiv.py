@@ -238,6 +238,11 @@ class Batch:
         if pipeline:
             _check(L.ebivgpu_batch_set_pipeline(h, self.depth), "pipeline")
 
+    def set_tuning(self, entropy_groups: int = 4, intra_warps: int = 0) -> None:
+        """Launch shapes (results do not depend on them): entropy launches per
+        pipelined round (1-4) and intra-stage warps per CTA (4/8/16, 0 = auto)."""
+        _check(self._L.ebivgpu_batch_set_tuning(self._h, int(entropy_groups), int(intra_warps)), "tuning")
+
     def add_stream(self, packets: list[bytes], ring: int = 3) -> int:
         n = len(packets)
         arr = (C.c_char_p * n)(*packets)

@@ -142,6 +142,11 @@ int ebivgpu_batch_set_lookahead(ebivgpu_batch* b, int frames);
  * flight.  Results and frame order per stream are those of the synchronous
  * rounds. */
 int ebivgpu_batch_set_pipeline(ebivgpu_batch* b, int depth);
+/* Launch shapes, the knobs the autotuner (govid_gb300/autotune.py) searches:
+ * the most entropy launches a pipelined round splits its frames into (1 to
+ * 4, default 4) and the warps per CTA of the intra stage (4, 8 or 16; 0, the
+ * default, picks by the tile count).  Results do not depend on them. */
+int ebivgpu_batch_set_tuning(ebivgpu_batch* b, int entropy_groups, int intra_warps);
 /* Replaces a resident stream's packets with a new clip of the same size
  * (starting with a key frame) and rewinds it; its frame pool is kept.  No
  * round may be in flight (drain first); the copies from pkts (pinned memory

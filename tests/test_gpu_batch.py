@@ -38,10 +38,15 @@ def _streams():
     return out
 
 
-@pytest.mark.parametrize("lookahead,pipeline", [(1, False), (4, False), (1, True), (4, True), (1, 2), (4, 2), (4, 3)])
-def test_batch_matches_oracle(gpu_required, lookahead, pipeline):
+@pytest.mark.parametrize("lookahead,pipeline,tuning", [(1, False, None), (4, False, None), (1, True, None),
+                                                        (4, True, None), (1, 2, None), (4, 2, None), (4, 3, None),
+                                                        (4, 2, (1, 4)), (8, 3, (2, 16)), (2, 1, (4, 8))])
+def test_batch_matches_oracle(gpu_required, lookahead, pipeline, tuning):
+    # Every launch shape the autotuner may pick gives the same frames.
     streams = _streams()
     b = ebiv.Batch(lookahead=lookahead, pipeline=pipeline)
+    if tuning:
+        b.set_tuning(*tuning)
     want, ids, dims = {}, [], {}
     for cont, w, h in streams:
         pkts = [p.data for p in ebiv.Reader(cont).packets()]
