@@ -145,13 +145,9 @@ struct ChainT {
   // (context * 64).
   __device__ __forceinline__ int symAt(int row) {
     if (err) return 0;
-    return finish(t->bucket[row + (int)((x0 & (kM - 1)) >> 6)], row);
-  }
-  // Completes the next symbol from its bucket entry e (of row `row`, at the
-  // current state's slot), loaded ahead by the caller.
-  __device__ __forceinline__ int finish(uint32_t e, int row) {
     const uint32_t x = x0;
     const uint32_t slot = x & (kM - 1);
+    const uint32_t e = t->bucket[row + (int)(slot >> 6)];
     int s = (int)((e >> 25) & 15u);
     uint32_t start = e & 0xFFFu, freq = (e >> 12) & 0x1FFFu;
     if (e & (kBImpure | kBUnused)) {
@@ -561,16 +557,15 @@ __device__ void predictVectors(const FrameDesc* fp, int tile, int done, WarpRows
     MBRec* const rowRec = recs + (size_t)(y0 + min(ry, th - 1)) * mbCols + x0;
     const int rowDone = ry < th ? min(tw, done - ry * tw) : 0;  // columns of this row the chain reached
     uint32_t h1 = 0, h2 = 0, h3 = 0;  // this lane's results of steps t-1, t-2, t-3
-    // Record words 0-3 of the macroblocks of steps t .. t+3, loaded four
-    // steps ahead so the global-memory latency overlaps the steps between.
+    // Record words 0-3 of a step's macroblock, loaded four steps ahead into
+    // one of four registers that nothing touches until its step, so the
+    // global-memory latency overlaps the steps between.
     auto recAt = [&](int x) {
       return x >= 0 && x < rowDone ? reinterpret_cast<const uint4*>(rowRec + x)[0] : make_uint4(0u, 0u, 0u, 0u);
     };
-    uint4 cur = recAt(-2 * lane), q1 = recAt(1 - 2 * lane), q2 = recAt(2 - 2 * lane), q3 = recAt(3 - 2 * lane);
-    for (int t = 0; t < steps; t++) {
+    auto step = [&](int t, const uint4& cur) {
       const int rx = t - 2 * lane;
-      const bool act = rx >= 0 && rx < rowDone;
-      const uint4 nxt = recAt(rx + 4);
+      const bool act = t < steps && rx >= 0 && rx < rowDone;
       uint32_t above = __shfl_up_sync(kFull, h2, 1);
       uint32_t ar = __shfl_up_sync(kFull, h1, 1);
       uint32_t al = __shfl_up_sync(kFull, h3, 1);
@@ -616,13 +611,21 @@ __device__ void predictVectors(const FrameDesc* fp, int tile, int done, WarpRows
         }
         if (lastRowOfPass) nextUp[rx] = out;
       }
-      cur = q1;
-      q1 = q2;
-      q2 = q3;
-      q3 = nxt;
       h3 = h2;
       h2 = h1;
       h1 = out;
+    };
+    const int base = -2 * lane;
+    uint4 q0 = recAt(base), q1 = recAt(base + 1), q2 = recAt(base + 2), q3 = recAt(base + 3);
+    for (int t = 0; t < steps; t += 4) {
+      step(t, q0);
+      q0 = recAt(base + t + 4);
+      step(t + 1, q1);
+      q1 = recAt(base + t + 5);
+      step(t + 2, q2);
+      q2 = recAt(base + t + 6);
+      step(t + 3, q3);
+      q3 = recAt(base + t + 7);
     }
     __syncwarp();  // the pass's last row is read by the next pass's lane 0
   }
