@@ -58,8 +58,8 @@ METRIC = "EBIV 1080p frames/s (batched vs per-stream on GPU, bit-exact; p99 ms; 
 # DRAM read+write bytes per decoded frame of the 1080p clip, summed over the
 # entropy, inter and intra kernels of a pipelined 32-frame-lookahead pass
 # (ncu dram__bytes_read.sum + dram__bytes_write.sum over every launch of a
-# 60-frame pass, scaled per frame; profiles/decode_1080p_traffic.md).
-DRAM_BYTES_PER_FRAME = 4.25e6
+# 60-frame prefix decoded twice, per frame; profiles/decode_1080p_launches_traffic.md).
+DRAM_BYTES_PER_FRAME = 6.42e6
 
 
 def log(*a):
