@@ -18,6 +18,10 @@ Reported (one JSON line on rank 0):
              frame copied back to pinned host memory, inside the timed region;
   codec_api  the govid Codec contract through ebivgpu_decode: one host
              packet in, one host frame out per synchronous call;
+  async_player  govid's AsyncPlayer frame source on the GPU
+             (ebivgpu_source_*): frames decoded ahead and delivered to a host
+             consumer in order, at decode-ahead depths 4 and 32, with and
+             without WithRGBA; seek-to-first-frame time;
   roofline   algorithmic HBM bytes of a step (packets + output written once
              + one reference read per inter frame) over the step time, against
              the measured HBM copy bandwidth; per-kernel figures beside it;
@@ -431,6 +435,7 @@ def run_gpu(args):
             out["learned_mv"] = r
         if not args.no_extras:
             out["rgba"] = run_rgba(pkts, want)
+            out["async_player"] = run_async_source(clip, pkts, want)
             out["ingest"] = run_ingest(clip, pkts, want)
             out["altref"] = run_altref()
             out["block_analysis"] = run_analysis()
@@ -482,6 +487,59 @@ def run_rgba(pkts, want):
     return {"codec_with_rgba_frames_per_s": round(fps, 2), "bit_exact_frames_checked": 8,
             "cpu_rgba_ms_per_1080p_frame": round(cpu_ms, 3),
             "note": "CPU: the oracle's C++ restatement of convertYCbCr420ToRGBA, one thread"}
+
+
+def run_async_source(clip, pkts, want):
+    """govid's AsyncPlayer frame source on the GPU (ebivgpu_source_*): a
+    consumer taking every frame of the clip into host memory through next()
+    and releasing it, at the decode-ahead depth of govid's Ebitengine example
+    (4, with and without WithRGBA) and at 32; plus the time from Seek to the
+    first frame at 16 key frames.  Every frame of one pass is hashed."""
+    import numpy as np
+
+    from govid_gb300 import ebiv
+
+    n = len(pkts)
+    rd = ebiv.Reader(clip)
+    out = {}
+    for depth, rgba in ((4, False), (4, True), (32, False)):
+        src = ebiv.AsyncSource(clip, depth=depth, rgba=rgba)
+        for rep in range(3):  # two warm passes, then the timed one
+            src.seek(0)
+            t0 = time.perf_counter()
+            k = 0
+            for _ in range(n):
+                f = src.next()
+                k += 1
+                src.release(f)
+            dt = time.perf_counter() - t0
+        out[f"depth{depth}{'_rgba' if rgba else ''}_frames_per_s"] = round(k / dt, 2)
+        if not rgba:
+            src.seek(0)
+            got = []
+            for _ in range(n):
+                f = src.next()
+                got.append(sha(f.packed()))
+                src.release(f)
+            if got != want:
+                raise RuntimeError(f"async source depth {depth}: frames differ from the oracle")
+        if depth == 4 and not rgba:
+            keys = [i for i, p in enumerate(pkts) if (p[0] & 3) == 0]
+            lat = []
+            for j in range(16):
+                t = rd.frame_time(keys[j % len(keys)] + 1)
+                t0 = time.perf_counter()
+                src.seek(t)
+                f = src.next()
+                lat.append(time.perf_counter() - t0)
+                src.release(f)
+            out["seek_to_first_frame_ms"] = {"p50": round(1000 * statistics.median(lat), 3),
+                                             "max": round(1000 * max(lat), 3)}
+        src.destroy()
+    out["bit_exact"] = True
+    out["note"] = ("frames delivered to a host consumer in order, each copied to pinned host memory "
+                   "(and converted to RGBA on the GPU with WithRGBA)")
+    return out
 
 
 def run_ingest(clip, pkts, want):

@@ -58,6 +58,17 @@ class Frame(C.Structure):
     ]
 
 
+class SourceFrame(C.Structure):
+    _fields_ = [
+        ("handle", C.c_int64),
+        ("y", C.POINTER(C.c_uint8)), ("cb", C.POINTER(C.c_uint8)), ("cr", C.POINTER(C.c_uint8)),
+        ("y_stride", C.c_int32), ("c_stride", C.c_int32),
+        ("width", C.c_int32), ("height", C.c_int32),
+        ("timestamp_ns", C.c_int64), ("frame_index", C.c_int64), ("keyframe", C.c_int32),
+        ("rgba", C.POINTER(C.c_uint8)),
+    ]
+
+
 def _sig(lib, name, res, *args):
     f = getattr(lib, name)
     f.restype = res
@@ -147,6 +158,18 @@ def lib() -> C.CDLL:
     _sig(L, "ebivgpu_container_entry", I, P, I, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.POINTER(I))
     _sig(L, "ebivgpu_container_seek", I, P, I64, C.POINTER(I64), C.POINTER(I64))
     _sig(L, "ebivgpu_batch_add_container", I, P, P, I, C.POINTER(I))
+    # decode-ahead frame source
+    SFP = C.POINTER(SourceFrame)
+    _sig(L, "ebivgpu_source_create", I, C.c_char_p, S, I, I, PP)
+    _sig(L, "ebivgpu_source_next", I, P, SFP)
+    _sig(L, "ebivgpu_source_poll", I, P, SFP, C.POINTER(I))
+    _sig(L, "ebivgpu_source_seek", I, P, I64, C.POINTER(I64))
+    _sig(L, "ebivgpu_source_release", None, P, I64)
+    _sig(L, "ebivgpu_source_close", I, P)
+    _sig(L, "ebivgpu_source_destroy", None, P)
+    _sig(L, "ebivgpu_source_decoded", I64, P)
+    _sig(L, "ebivgpu_source_duration", I64, P)
+    _sig(L, "ebivgpu_source_lookahead", I, P)
     # alt-ref temporal filter
     _sig(L, "ebivgpu_altref_create", I, PP)
     _sig(L, "ebivgpu_altref_destroy", None, P)

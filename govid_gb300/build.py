@@ -20,7 +20,7 @@ OUT = PKG / "_lib"
 OBJ = OUT / "obj"
 LIB = OUT / "libebivgpu.so"
 
-CUDA_SOURCES = ["decode_kernels.cu", "gpu_codec.cu", "rgba_kernel.cu", "batch.cu", "serve.cu", "noalloc.cu", "mvnet_kernels.cu", "altref.cu", "ingest.cu", "analysis.cu"]
+CUDA_SOURCES = ["decode_kernels.cu", "gpu_codec.cu", "rgba_kernel.cu", "batch.cu", "serve.cu", "noalloc.cu", "mvnet_kernels.cu", "altref.cu", "ingest.cu", "analysis.cu", "source.cu"]
 CXX_SOURCES = ["encoder.cpp", "container.cpp", "synth.cpp", "host_api.cpp", "payload.cpp"]
 
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"

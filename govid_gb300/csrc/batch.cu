@@ -397,6 +397,18 @@ int Engine::downloadFrameAsync(const EngineFrameView& v, uint8_t* packed, size_t
   return kOK;
 }
 
+int Engine::convertFrameAsync(const EngineFrameView& v, uint8_t* rgbaDev, uint8_t* rgbaHost) {
+  if (!v.y || !rgbaDev || !rgbaHost) return kErrArg;
+  launchRGBA(v.y, v.cb, v.cr, v.yStride, v.cStride, v.width, v.height, rgbaDev, streamC_);
+  launches_++;
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpyAsync(rgbaHost, rgbaDev, (size_t)v.width * v.height * 4, cudaMemcpyDeviceToHost, streamC_) ||
+      cudaEventRecord(copyDone_, streamC_))
+    return kErrDevice;
+  copiesPending_ = true;
+  return kOK;
+}
+
 int Engine::syncCopies() {
   if (cudaStreamSynchronize(streamC_) != cudaSuccess) return kErrDevice;
   copiesPending_ = false;

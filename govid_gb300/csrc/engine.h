@@ -134,6 +134,10 @@ class Engine {
   // complete after syncCopies().  Later rounds' device work waits for it
   // before touching frame buffers.
   int downloadFrameAsync(const EngineFrameView& v, uint8_t* packed, size_t cap);
+  // Also on the copy stream: the frame's RGBA (convertYCbCr420ToRGBA,
+  // frame.go:8-67) into rgbaDev (W*H*4 bytes of device memory), then copied
+  // to rgbaHost.  Conversions queued one after another may share rgbaDev.
+  int convertFrameAsync(const EngineFrameView& v, uint8_t* rgbaDev, uint8_t* rgbaHost);
   int syncCopies();
   // New packets for a resident stream (its frame pool is kept); no round may
   // be in flight.

@@ -435,6 +435,103 @@ class DeviceContainer:
             pass
 
 
+@dataclass
+class SourceFrame:
+    """A frame from an AsyncSource: packed planes (and RGBA with rgba=True)
+    in pinned host memory, valid until ``AsyncSource.release(frame)``."""
+    y: np.ndarray
+    cb: np.ndarray
+    cr: np.ndarray
+    timestamp_ns: int
+    width: int
+    height: int
+    frame_index: int
+    keyframe: bool
+    rgba: np.ndarray | None
+    handle: int
+
+    def packed(self) -> bytes:
+        return self.y.tobytes() + self.cb.tobytes() + self.cr.tobytes()
+
+
+class AsyncSource:
+    """govid's decode-ahead frame source (asyncSource, source.go:84-266; the
+    source of NewAsyncPlayer(d, c, depth, WithRGBA), player.go:40-57) on the
+    GPU: a native worker thread decodes the container's frames ahead of the
+    consumer (include/ebivgpu.h, ebivgpu_source_*).
+
+    next() blocks for the next frame; poll() returns None when none is ready.
+    At the end of the stream both raise EOF, after a decode error they raise
+    it; the worker then waits for seek().  Frames stay valid until release().
+    """
+
+    def __init__(self, container: bytes, depth: int = 4, rgba: bool = False):
+        L = _native.lib()
+        h = C.c_void_p()
+        _check(L.ebivgpu_source_create(container, len(container), int(depth), 1 if rgba else 0, C.byref(h)),
+               "NewAsyncPlayer")
+        self._h, self._L = h, L
+        self._f = _native.SourceFrame()
+
+    def _frame(self) -> SourceFrame:
+        f = self._f
+        w, h = f.width, f.height
+        cw, ch = (w + 1) // 2, (h + 1) // 2
+        y = np.ctypeslib.as_array(f.y, shape=(h, w))
+        cb = np.ctypeslib.as_array(f.cb, shape=(ch, cw))
+        cr = np.ctypeslib.as_array(f.cr, shape=(ch, cw))
+        rgba = np.ctypeslib.as_array(f.rgba, shape=(h, w, 4)) if f.rgba else None
+        return SourceFrame(y, cb, cr, f.timestamp_ns, w, h, f.frame_index, bool(f.keyframe), rgba, f.handle)
+
+    def next(self) -> SourceFrame:
+        _check(self._L.ebivgpu_source_next(self._h, C.byref(self._f)), "next")
+        return self._frame()
+
+    def poll(self) -> SourceFrame | None:
+        ready = C.c_int()
+        _check(self._L.ebivgpu_source_poll(self._h, C.byref(self._f), C.byref(ready)), "poll")
+        return self._frame() if ready.value else None
+
+    def seek(self, t_ns: int) -> int:
+        """Repositions at the last key frame at or before t; returns its time."""
+        landed = C.c_int64()
+        _check(self._L.ebivgpu_source_seek(self._h, int(t_ns), C.byref(landed)), "seek")
+        return landed.value
+
+    def release(self, frame: SourceFrame | None) -> None:
+        if frame is not None and getattr(self, "_h", None):
+            self._L.ebivgpu_source_release(self._h, frame.handle)
+
+    @property
+    def decoded(self) -> int:
+        """Frames the worker has decoded so far."""
+        return int(self._L.ebivgpu_source_decoded(self._h))
+
+    @property
+    def lookahead(self) -> int:
+        return int(self._L.ebivgpu_source_lookahead(self._h))
+
+    def duration(self) -> int:
+        return int(self._L.ebivgpu_source_duration(self._h))
+
+    def close(self) -> None:
+        """Stops the worker (idempotent); frames already returned stay valid
+        until destroy()."""
+        if getattr(self, "_h", None):
+            _check(self._L.ebivgpu_source_close(self._h))
+
+    def destroy(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.ebivgpu_source_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
 class BlockAnalysis:
     """forwardDCT and satd (ebiv/transform.go:44-119) of a batch of residual
     blocks on the GPU."""

@@ -17,6 +17,8 @@
  *   ebivgpu_batch_*  <- many independent Codec.Decode call chains at once
  *   ebivgpu_altref_* <- (*ebiv.Encoder).buildAltRef        ebiv/encoder.go:326-407
  *   ebivgpu_fdct_satd <- forwardDCT / satd                ebiv/transform.go:44-119
+ *   ebivgpu_source_* <- govid asyncSource (NewAsyncPlayer's decode-ahead
+ *                       frame source)                     source.go:84-266
  *   ebivgpu_container_* <- ebiv.NewDemuxer index load, Reader.Seek
  *                                                       ebiv/reader.go:32-160,222-238
  *                       (no single reference counterpart; the reference runs
@@ -301,6 +303,58 @@ int ebivgpu_analysis_create(ebivgpu_analysis** out);
 void ebivgpu_analysis_destroy(ebivgpu_analysis* a);
 int ebivgpu_fdct_satd(ebivgpu_analysis* a, const int32_t* residuals, int n, int count, int32_t* coeffs, int64_t* satd,
                       double* kernel_ms);
+
+/* ---- Decode-ahead frame source (govid.NewAsyncPlayer) -----------------------
+ * Replaces asyncSource   source.go:84-266 (newAsyncSource, run, next, poll,
+ * seek, release, close), the frame source of NewAsyncPlayer(d, c, depth,
+ * WithRGBA)   player.go:40-57, with its demuxer (ebiv.NewDemuxer,
+ * ebiv/reader.go:32-258) and codec (ebiv.NewCodec, ebiv/codec.go:48-192).
+ *
+ * The source copies the container, keeps its packets resident on the GPU
+ * and decodes ahead of the consumer on a native worker thread: frames are
+ * decoded min(depth, 32) at a time in pipelined rounds, copied to pinned
+ * host memory (with EBIVGPU_SOURCE_RGBA also converted to RGBA on the GPU,
+ * BT.601 fixed point, frame.go:8-67) and queued, up to depth frames.
+ *
+ * next blocks until a frame or a terminal status is available; poll returns
+ * at once (*ready 0: nothing yet).  A status other than EBIV_OK is
+ * EBIV_ERR_EOF at the end of the stream or the decode error of the next
+ * frame; the worker then parks until a seek (readNextFrame's error,
+ * source.go:164-170), and later calls return the same status.  After close,
+ * next and poll return EBIV_ERR_EOF.  seek: a new generation (frames decoded
+ * before it are never returned), the stream repositioned at the last key
+ * frame at or before t (Seek, ebiv/reader.go:222-238), *landed_ns its time.
+ * A returned frame's planes (strides width and (width+1)/2) and RGBA stay
+ * valid until ebivgpu_source_release(handle).  A consumer holding so many
+ * frames that none can be decoded (more than depth + lookahead + 4) gets
+ * EBIV_ERR_ARG from next and poll rather than a wait that never ends (the
+ * worker resumes at the next release).  close returns once
+ * the worker has stopped; destroy frees everything, returned frames
+ * included.  ebivgpu_source_decoded counts frames the worker has decoded. */
+#define EBIVGPU_SOURCE_RGBA 1
+typedef struct ebivgpu_source ebivgpu_source;
+typedef struct {
+  int64_t handle;
+  const uint8_t* y;
+  const uint8_t* cb;
+  const uint8_t* cr;
+  int32_t y_stride, c_stride;
+  int32_t width, height;
+  int64_t timestamp_ns;
+  int64_t frame_index;
+  int32_t keyframe;
+  const uint8_t* rgba; /* width*height*4 bytes with EBIVGPU_SOURCE_RGBA, else NULL */
+} ebivgpu_source_frame;
+int ebivgpu_source_create(const uint8_t* container, size_t n, int depth, int flags, ebivgpu_source** out);
+int ebivgpu_source_next(ebivgpu_source* s, ebivgpu_source_frame* f);
+int ebivgpu_source_poll(ebivgpu_source* s, ebivgpu_source_frame* f, int* ready);
+int ebivgpu_source_seek(ebivgpu_source* s, int64_t t_ns, int64_t* landed_ns);
+void ebivgpu_source_release(ebivgpu_source* s, int64_t handle);
+int ebivgpu_source_close(ebivgpu_source* s);
+void ebivgpu_source_destroy(ebivgpu_source* s);
+int64_t ebivgpu_source_decoded(ebivgpu_source* s);
+int64_t ebivgpu_source_duration(ebivgpu_source* s);
+int ebivgpu_source_lookahead(ebivgpu_source* s);
 
 /* Non-zero when a CUDA device is usable from this process. */
 int ebivgpu_device_available(void);
