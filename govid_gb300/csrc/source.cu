@@ -119,6 +119,10 @@ class Source {
   int take(bool block, ebivgpu_source_frame* f, int* ready) {
     std::unique_lock<std::mutex> lk(mu_);
     for (;;) {
+      if (closing_) {
+        if (ready) *ready = 1;
+        return kErrEOF;  // source.go:206-208
+      }
       while (!queue_.empty()) {
         const Entry e = queue_.front();
         queue_.pop_front();
@@ -138,10 +142,6 @@ class Source {
         fill(e.slot, s, f);
         if (ready) *ready = 1;
         return kOK;
-      }
-      if (closing_) {
-        if (ready) *ready = 1;
-        return kErrEOF;  // source.go:206-208
       }
       if (parked_ && terminalTaken_) {
         if (ready) *ready = 1;
