@@ -212,6 +212,7 @@ def lib() -> C.CDLL:
     _sig(L, "ebiv_encode_scene", I, C.POINTER(C.c_int64), I, C.POINTER(EncoderOptions), C.POINTER(U8P),
          C.POINTER(S))
     _sig(L, "ebiv_free", None, P)
+    _sig(L, "ebiv_encode_key_from_levels", I, I, I, I, I, C.POINTER(C.c_int32), S, C.POINTER(U8P), C.POINTER(S))
     _sig(L, "ebiv_encode_block", I, C.POINTER(C.c_int32), I, I, I, U8P, S, C.POINTER(S), C.POINTER(C.c_uint32),
          U8P)
     _sig(L, "ebiv_encode_tokens", I, C.POINTER(C.c_uint16), I, U8P, S, C.POINTER(S), C.POINTER(C.c_uint32), U8P)

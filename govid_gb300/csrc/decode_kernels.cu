@@ -1020,6 +1020,47 @@ __device__ void mbResidual(const uint32_t* coef, int tx, uint32_t mask, int32_t 
 // ---------------------------------------------------------------------------
 // Motion compensation samples (clamped form of ebiv/motioncomp.go:49-97)
 // ---------------------------------------------------------------------------
+// A macroblock's residual between kInterRecon phase 0 and its consumer
+// (phase 1, or the intra stage), stored over its coefficient region.  When
+// every value fits in 16 bits (any real stream: a coded sample's residual is
+// within a few thousand), values go in pairs — word w < 128: luma samples w
+// (low half) and w + 128; word 256 + w, w < 64: chroma samples 256 + w and
+// 320 + w — and word kResFormatWord is 1: 768 bytes instead of 1536.
+// Otherwise (a hostile stream whose int32-wrapped arithmetic made a value no
+// 16-bit number reproduces under the reconstruction's wrapping add) the 384
+// words are stored as they are and the format word is 0.  Both formats put
+// the values the readers load first at the same words.
+constexpr int kResFormatWord = kCoefPerMB - 1;
+__device__ __forceinline__ int32_t lo16(uint32_t w) { return (int32_t)(int16_t)(w & 0xFFFFu); }
+__device__ __forceinline__ int32_t hi16(uint32_t w) { return (int32_t)(int16_t)(w >> 16); }
+__device__ __forceinline__ int resWordLo(int w) { return w < 128 ? w : w + 128; }  // w < 192: the low sample
+__device__ __forceinline__ void storeResidual(uint32_t* cg, const int32_t* res, int lane) {
+  bool fits = true;
+  for (int q = lane; q < 384; q += 32) fits = fits && res[q] >= -32768 && res[q] <= 32767;
+  fits = __all_sync(kFull, fits);
+  if (fits) {
+    for (int w = lane; w < 192; w += 32) {
+      const int a = resWordLo(w), b = a + (w < 128 ? 128 : 64);
+      cg[w < 128 ? w : w + 128] = (uint32_t)(uint16_t)res[a] | ((uint32_t)res[b] << 16);
+    }
+  } else {
+    for (int q = lane; q < 384; q += 32) cg[q] = (uint32_t)res[q];
+  }
+  if (lane == 0) cg[kResFormatWord] = fits ? 1u : 0u;
+}
+__device__ __forceinline__ void loadResidual(const uint32_t* cg, int32_t* res, int lane) {
+  if (cg[kResFormatWord]) {
+    for (int w = lane; w < 192; w += 32) {
+      const uint32_t v = cg[w < 128 ? w : w + 128];
+      const int a = resWordLo(w);
+      res[a] = lo16(v);
+      res[a + (w < 128 ? 128 : 64)] = hi16(v);
+    }
+  } else {
+    for (int q = lane; q < 384; q += 32) res[q] = (int32_t)cg[q];
+  }
+}
+
 __device__ __forceinline__ int lumaSample(const uint8_t* p, int stride, int w, int h, int px, int py, int fx, int fy) {
   auto g = [&](int x, int y) -> int32_t { return __ldg(p + (size_t)clampC(y, h) * stride + clampC(x, w)); };
   if (fx == 0 && fy == 0) return g(px, py);
@@ -1233,15 +1274,13 @@ __global__ void __launch_bounds__(32 * kInterWarps, 6) kInterRecon(const FrameDe
   if (cbp & cbpCr) resMask |= nzm & wm & (1u << 17);
   uint32_t* const cg = v.coef + (size_t)idx * kCoefPerMB;
   if (phase == 1) {
-    if (resMask)
-      for (int q = lane; q < 384; q += 32) S.res[q] = (int32_t)cg[q];
+    if (resMask) loadResidual(cg, S.res, lane);
     __syncwarp();
   } else if (resMask) {
     mbResidual(cg, tx, resMask, v.qdc, v.qac, S.res, S.tmp, lane);
   }
   if (intra || deferred) {
-    if (resMask)
-      for (int q = lane; q < 384; q += 32) cg[q] = (uint32_t)S.res[q];
+    if (resMask) storeResidual(cg, S.res, lane);
     return;
   }
 
@@ -1491,9 +1530,26 @@ __device__ void intraLuma(const ReconView& f, IntraScratch& S, const IntraSync& 
   // left column follows the left neighbour's steps.
   const bool lumaRes = (resMask & 0xFFFFu) != 0;
   int32_t rv[8];
-  if (lumaRes)
+  if (lumaRes) {
+    // Words lane + 32q (q < 4) hold samples in either format; the format
+    // word says whether they are pairs or the second half follows.
+    uint32_t w4[4];
 #pragma unroll
-    for (int q = 0; q < 8; q++) rv[q] = (int32_t)rg[lane + 32 * q];
+    for (int q = 0; q < 4; q++) w4[q] = rg[lane + 32 * q];
+    if (rg[kResFormatWord]) {
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        rv[q] = lo16(w4[q]);
+        rv[q + 4] = hi16(w4[q]);
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        rv[q] = (int32_t)w4[q];
+        rv[q + 4] = (int32_t)rg[lane + 32 * (q + 4)];
+      }
+    }
+  }
   if (up) {
     if (left) sy.wait(sy.luma + sy.at(mbx - 1, mby - 1), kLumaDone);
     sy.wait(sy.luma + sy.at(mbx, mby - 1), kLumaDone);
@@ -1574,9 +1630,20 @@ __device__ void intraChroma(const ReconView& f, IntraScratch& S, const IntraSync
   const uint32_t* rg = f.coef + (size_t)idx * kCoefPerMB;
   const bool chromaRes = ((nzm & wm) >> 16) != 0;
   int32_t rv[4];
-  if (chromaRes)
-#pragma unroll
-    for (int q = 0; q < 4; q++) rv[q] = (int32_t)rg[256 + lane + 32 * q];
+  if (chromaRes) {
+    const uint32_t a = rg[256 + lane], b = rg[288 + lane];
+    if (rg[kResFormatWord]) {
+      rv[0] = lo16(a);
+      rv[1] = lo16(b);
+      rv[2] = hi16(a);
+      rv[3] = hi16(b);
+    } else {
+      rv[0] = (int32_t)a;
+      rv[1] = (int32_t)b;
+      rv[2] = (int32_t)rg[320 + lane];
+      rv[3] = (int32_t)rg[352 + lane];
+    }
+  }
   if (up) {
     if (left) sy.wait(sy.chroma + sy.at(mbx - 1, mby - 1), 1);
     sy.wait(sy.chroma + sy.at(mbx, mby - 1), 1);

@@ -1824,6 +1824,62 @@ int encodeBlockStream(int32_t* levels, int n, int plane, int txIdx, std::vector<
                            (int)ts.toks.size(), stream, freqs, used);
 }
 
+// A one-tile intra key frame built from chosen levels: every macroblock
+// codes its luma as sixteen 4x4 blocks (16 levels each, raster order within
+// the macroblock) and its chroma as one 8x8 Cb and one 8x8 Cr block (64
+// levels each), all with intra mode `mode`; tokens follow the grammar of
+// decodeLumaMB/decodeChromaMB (ebiv/decode_intra.go:121-187) after sign-data
+// hiding, tables are normalized from the frame's own counts, and the packet
+// is header + assemblePayload (ebiv/frame.go:224-236).  It makes test
+// streams with coefficients no real source produces.
+int encodeKeyFromLevels(int w, int h, int qp, int mode, const int32_t* levels, size_t nlevels,
+                        std::vector<uint8_t>* pkt) {
+  if (w <= 0 || h <= 0 || qp < 0 || qp > 255 || mode < 0 || mode >= kNumIntraModes) return kErrArg;
+  const Geometry g = Geometry::of(w, h);
+  const size_t perMB = 16 * 16 + 2 * 64;
+  if (nlevels != perMB * (size_t)g.mbCols * g.mbRows) return kErrArg;
+  TokStream ts;
+  int32_t lv[64];
+  const int32_t* src = levels;
+  for (int m = 0; m < g.mbCols * g.mbRows; m++) {
+    ts.put(ctxTxSize, 0);
+    for (int k = 0; k < 16; k++, src += 16) {
+      ts.put(ctxLumaMode, mode);
+      std::memcpy(lv, src, 16 * sizeof(int32_t));
+      applySignDataHiding(lv, 4);
+      encodeBlock(ts, kPlaneLuma, 0, lv, 4);
+    }
+    ts.put(ctxChromaMode, mode);
+    for (int c = 0; c < 2; c++, src += 64) {
+      std::memcpy(lv, src, 64 * sizeof(int32_t));
+      applySignDataHiding(lv, 8);
+      encodeBlock(ts, kPlaneChroma, 0, lv, 8);
+    }
+  }
+  std::vector<std::vector<uint32_t>> counts(kNumContexts);
+  for (int c = 0; c < kNumContexts; c++) counts[c].assign((size_t)alphabetSize(c), 0);
+  for (const Tok& t : ts.toks) counts[t.ctx][t.sym]++;
+  std::vector<Freqs> freqs(kNumContexts);
+  std::vector<EncTable> tables(kNumContexts);
+  for (int c = 0; c < kNumContexts; c++) {
+    if (c == ctxBypass) continue;
+    freqs[c] = normalizeFreqs(counts[c]);
+    tables[c] = buildEncTable(freqs[c].empty() ? Freqs((size_t)alphabetSize(c), 0) : freqs[c], alphabetSize(c));
+  }
+  tables[ctxBypass] = buildEncTable(Freqs{kM / 2, kM / 2}, 2);
+  const std::vector<uint8_t> tableBytes = serializeTables(freqs, nullptr);
+  const std::vector<uint8_t> tile = ransEncode(ts.toks, tables);
+  *pkt = frameHeaderBytes(kFrameKey, kCodingIntra, g, false);
+  pkt->push_back((uint8_t)qp);
+  putUvarint(*pkt, 1);
+  putUvarint(*pkt, 1);
+  putUvarint(*pkt, tableBytes.size());
+  pkt->insert(pkt->end(), tableBytes.begin(), tableBytes.end());
+  putUvarint(*pkt, tile.size());
+  pkt->insert(pkt->end(), tile.begin(), tile.end());
+  return kOK;
+}
+
 // rANS-encodes a (context, symbol) token list with tables normalized from its
 // own counts; the bypass context is the fixed uniform table.
 int encodeTokenStream(const uint16_t* pairs, int count, std::vector<uint8_t>* stream, std::vector<uint32_t>* freqs,

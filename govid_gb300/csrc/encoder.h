@@ -106,6 +106,8 @@ class Encoder {
 // Single-block and token-stream coding hooks (see encoder.cpp).
 int encodeBlockStream(int32_t* levels, int n, int plane, int txIdx, std::vector<uint8_t>* stream,
                       std::vector<uint32_t>* freqs, std::vector<uint8_t>* used);
+int encodeKeyFromLevels(int w, int h, int qp, int mode, const int32_t* levels, size_t nlevels,
+                        std::vector<uint8_t>* pkt);
 int encodeTokenStream(const uint16_t* pairs, int count, std::vector<uint8_t>* stream, std::vector<uint32_t>* freqs,
                       std::vector<uint8_t>* used);
 

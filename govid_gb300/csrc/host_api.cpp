@@ -471,6 +471,14 @@ int ebiv_encode_block(int32_t* levels, int n, int plane, int tx_idx, uint8_t* st
   return kOK;
 }
 
+int ebiv_encode_key_from_levels(int w, int h, int qp, int mode, const int32_t* levels, size_t nlevels, uint8_t** out,
+                                size_t* n) {
+  if (!levels || !out || !n) return kErrArg;
+  std::vector<uint8_t> pkt;
+  if (int st = encodeKeyFromLevels(w, h, qp, mode, levels, nlevels, &pkt)) return st;
+  return copyOut(pkt, out, n);
+}
+
 int ebiv_encode_tokens(const uint16_t* pairs, int count, uint8_t* stream, size_t cap, size_t* len, uint32_t* freqs,
                        uint8_t* used) {
   std::vector<uint8_t> st, u;

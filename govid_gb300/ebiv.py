@@ -905,3 +905,21 @@ def encode_scene(spec: SceneSpec, frames: int, qp: int, gop: int, tiles: tuple[i
         return C.string_at(d, n.value)
     finally:
         L.ebiv_free(d)
+
+
+def encode_key_from_levels(width: int, height: int, qp: int, mode: int, levels: np.ndarray) -> bytes:
+    """A one-tile intra key frame packet with chosen levels (include/ebiv_host.h,
+    ebiv_encode_key_from_levels): levels has 384 entries per macroblock in
+    raster order — sixteen 4x4 luma blocks of 16, then 64 Cb and 64 Cr."""
+    L = _native.lib()
+    lv = np.ascontiguousarray(levels, dtype=np.int32).ravel()
+    d = C.POINTER(C.c_uint8)()
+    n = C.c_size_t()
+    _check(L.ebiv_encode_key_from_levels(int(width), int(height), int(qp), int(mode),
+                                         lv.ctypes.data_as(C.POINTER(C.c_int32)), lv.size, C.byref(d), C.byref(n)),
+           "encode_key_from_levels")
+    try:
+        return C.string_at(d, n.value)
+    finally:
+        L.ebiv_free(d)
+

@@ -110,6 +110,14 @@ void ebiv_free(void* p);
  * entries per context (72 contexts), used one flag per context. */
 int ebiv_encode_block(int32_t* levels, int n, int plane, int tx_idx, uint8_t* stream, size_t cap, size_t* len,
                       uint32_t* freqs, uint8_t* used);
+/* One packet: a one-tile intra key frame of w x h whose macroblocks (raster
+ * order) take their levels from `levels` — sixteen 4x4 luma blocks of 16
+ * levels, then 64 Cb and 64 Cr levels, 384 per macroblock — all blocks with
+ * intra mode `mode` (the token grammar of decodeLumaMB/decodeChromaMB,
+ * ebiv/decode_intra.go:121-187, tables from the frame's own counts).  For
+ * test streams with chosen coefficients.  *out is freed with ebiv_free. */
+int ebiv_encode_key_from_levels(int w, int h, int qp, int mode, const int32_t* levels, size_t nlevels, uint8_t** out,
+                                size_t* n);
 /* rANS-codes `count` (context, symbol) pairs with tables normalized from
  * their own counts (ebiv/rans.go:46-85, 186-214). */
 int ebiv_encode_tokens(const uint16_t* pairs, int count, uint8_t* stream, size_t cap, size_t* len, uint32_t* freqs,

@@ -637,13 +637,24 @@ static void predictIntra(const PlaneView& p, int x0, int y0, int n, int mode, bo
   }
 }
 
+// Test statistic (no counterpart in the reference): intra residual samples
+// outside the 16-bit range reconstructed so far, so a test can show that its
+// corpus reaches the GPU decoder's wide-residual path.
+static std::atomic<long> gWideResiduals{0};
+
 // reconstruct — ebiv/predict.go:209-219
 static void reconstruct(const PlaneView& p, int x0, int y0, int n, const int32_t* pred,
                         const int32_t* residual) {
+  long wide = 0;
   for (int r = 0; r < n; r++) {
     uint8_t* dst = p.data + (size_t)(y0 + r) * p.stride + x0;
-    for (int c = 0; c < n; c++) dst[c] = clampByte(add32(pred[r * n + c], residual[r * n + c]));
+    for (int c = 0; c < n; c++) {
+      const int32_t v = residual[r * n + c];
+      wide += (v < -32768 || v > 32767) ? 1 : 0;
+      dst[c] = clampByte(add32(pred[r * n + c], v));
+    }
   }
+  if (wide) gWideResiduals += wide;
 }
 
 // ---- motion compensation: ebiv/motioncomp.go -------------------------------
@@ -1319,6 +1330,10 @@ int eo_codec_decode(eo_codec* c, const uint8_t* pkt, size_t n, int* slot, int* w
   if (w) *w = c->geo.W;
   if (h) *h = c->geo.H;
   return st;
+}
+
+long eo_wide_residuals(int reset) {
+  return reset ? gWideResiduals.exchange(0) : gWideResiduals.load();
 }
 
 void eo_codec_flush(eo_codec* c) {

@@ -48,6 +48,9 @@ int eo_codec_decode(eo_codec* c, const uint8_t* pkt, size_t n, int* slot, int* w
 
 /* Codec.Flush — ebiv/codec.go:115-117. */
 void eo_codec_flush(eo_codec* c);
+/* Test statistic: intra residual samples outside [-32768, 32767] that every
+ * codec of the process has reconstructed (reset != 0 clears the count). */
+long eo_wide_residuals(int reset);
 
 /* Copies ring image `slot` out as tightly packed Y, Cb, Cr planes. */
 int eo_codec_ring_image(eo_codec* c, int slot, uint8_t* packed, size_t cap);

@@ -37,6 +37,8 @@ def lib() -> C.CDLL:
         L.eo_codec_reference.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_size_t]
         L.eo_decode_streams.restype = C.c_long
         L.eo_rgba.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_char_p]
+        L.eo_wide_residuals.restype = C.c_long
+        L.eo_wide_residuals.argtypes = [C.c_int]
         _lib = L
     return _lib
 
@@ -105,3 +107,9 @@ def decode_streams(streams: list[list[bytes]], threads: int) -> int:
         arr_n[i] = C.cast(ns, C.POINTER(C.c_size_t))
         nfr[i] = len(s)
     return int(L.eo_decode_streams(arr_p, arr_n, nfr, len(streams), threads))
+
+
+def wide_residuals(reset: bool = False) -> int:
+    """Intra residual samples outside the 16-bit range reconstructed so far
+    (all oracle codecs of the process); reset clears the count."""
+    return int(lib().eo_wide_residuals(1 if reset else 0))

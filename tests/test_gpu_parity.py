@@ -5,6 +5,7 @@ Clip shapes and options restate the reference's own decode tests
 (ebiv/coded_test.go, ebiv/tile_test.go, ebiv/regression_test.go,
 ebiv/codec_test.go) plus the sprite-scene workloads' shapes at small sizes.
 """
+import numpy as np
 import pytest
 
 import ebiv_oracle
@@ -102,3 +103,47 @@ def test_fast_encode_scene_flash(gpu_required):
     spec = ebiv.SceneSpec(width=320, height=192, seed=3, sprites=4, flash_period=8, flash_start=3)
     cont = ebiv.encode_scene(spec, 16, qp=22, gop=16, tiles=(4, 3), fast=True, threads=4)
     _check(cont, 320, 192)
+
+
+def _wide_levels(w, h, seed, dense):
+    """Levels for ebiv.encode_key_from_levels: even macroblocks get escape
+    levels near the grammar's largest (their residuals leave the 16-bit range;
+    with `dense`, every coefficient is huge, so the transform's int32
+    narrowing wraps), odd ones small levels."""
+    rng = np.random.default_rng(seed)
+    mbs = ((w + 15) // 16) * ((h + 15) // 16)
+    lv = np.zeros((mbs, 384), np.int32)
+    for m in range(mbs):
+        if m % 2 == 0:
+            n = 16 if dense else 2
+            for b in range(16):
+                lv[m, b * 16:b * 16 + n] = rng.choice([-1, 1], n) * rng.integers(20000, 32773, n)
+            lv[m, 256:256 + (64 if dense else 1)] = 32772
+            lv[m, 320] = -30000
+        else:
+            for b in range(16):
+                lv[m, b * 16 + rng.integers(0, 16)] = rng.integers(-3, 4)
+    return lv
+
+
+@pytest.mark.parametrize("qp,dense", [(22, False), (51, False), (63, True), (40, True)])
+def test_hostile_wide_residuals_match_oracle(gpu_required, qp, dense):
+    # Residuals beyond 16 bits (only crafted streams have them) take the
+    # reconstruction's int32 path between the residual and intra stages;
+    # macroblocks with small residuals in the same frame take the 16-bit one.
+    w, h = 80, 48
+    pkts = [ebiv.encode_key_from_levels(w, h, qp, mode, _wide_levels(w, h, 7 + mode, dense)) for mode in range(4)]
+    ebiv_oracle.wide_residuals(True)
+    want = ebiv_oracle.decode_all(pkts)
+    assert all(st == 0 for st, _ in want)
+    assert ebiv_oracle.wide_residuals() > 0
+    got = gpu_decode_all(pkts)
+    for i, ((gs, gp), (ws, wp)) in enumerate(zip(got, want)):
+        assert gs == ws and gp == wp, f"frame {i}: {first_diff(gp, wp, w, h) if gp and wp else (gs, ws)}"
+    b = ebiv.Batch(lookahead=4, pipeline=2)
+    sid = b.add_stream(pkts)
+    res = []
+    for _ in range(len(pkts) + 8):  # every frame is back after depth + frames rounds
+        res += [(x.frame_index, x.status, b.download(x, w, h)) for x in b.round()]
+    res += [(x.frame_index, x.status, b.download(x, w, h)) for x in b.drain()]
+    assert sorted((i, s, p) for i, s, p in res) == [(i, 0, want[i][1]) for i in range(len(pkts))]

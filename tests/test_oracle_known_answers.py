@@ -243,3 +243,24 @@ def test_zigzag_is_a_permutation_starting_at_dc():
     for n in (4, 8, 16):
         z = _scan(n)
         assert sorted(z) == list(range(n * n)) and z[0] == 0
+
+
+def test_key_frames_from_chosen_levels_decode_in_the_oracle():
+    # ebiv_encode_key_from_levels builds a key frame from given levels; the
+    # oracle decodes it, and its wide-residual count sees the huge ones.
+    from govid_gb300 import ebiv
+
+    w, h = 48, 32
+    mbs = 3 * 2
+    small = np.zeros((mbs, 384), np.int32)
+    small[:, 0] = 3
+    small[:, 256] = -2
+    ebiv_oracle.wide_residuals(True)
+    st, planes = ebiv_oracle.decode_all([ebiv.encode_key_from_levels(w, h, 22, 0, small)])[0]
+    assert st == 0 and ebiv_oracle.wide_residuals() == 0
+    huge = small.copy()
+    huge[::2, 0:16] = 32772
+    st, planes = ebiv_oracle.decode_all([ebiv.encode_key_from_levels(w, h, 51, 0, huge)])[0]
+    assert st == 0 and ebiv_oracle.wide_residuals() > 0
+    with pytest.raises(ebiv.ErrArgument):
+        ebiv.encode_key_from_levels(w, h, 22, 0, small[:-1])
