@@ -805,7 +805,7 @@ def run_serve(args):
         srv = ebiv.Server(duration_s=seconds, frames_per_stream=args.serve_frames, seek_prob=0.05,
                           seed=args.serve_seed, hbm_budget_bytes=120 << 30,
                           max_frames_per_round=args.serve_max_frames, ring=3, key_lane=True,
-                          start_spread_s=1.0, record=record)
+                          start_spread_s=1.0, record=record, decode_ahead=args.serve_ahead)
         counts, which = {}, []
         for i in range(args.serve_streams):
             k = i % len(clips)
@@ -825,7 +825,11 @@ def run_serve(args):
         "requests": st["requests"], "frames": st["frames"], "errors": st["errors"], "seeks": st["seeks"],
         "loops": st["loops"], "rounds": st["rounds"], "frames_per_s": round(st["frames_per_s"], 2),
         "latency_ms": {"p50": round(st["latency_p50_ms"], 3), "p99": round(st["latency_p99_ms"], 3),
-                       "max": round(st["latency_max_ms"], 3)},
+                       "max": round(st["latency_max_ms"], 3), "mean": round(st["latency_mean_ms"], 3)},
+        "seek_latency_ms": {"p50": round(st["seek_latency_p50_ms"], 3), "p99": round(st["seek_latency_p99_ms"], 3)},
+        "ready_at_arrival_frac": round(st["ready_at_arrival"] / max(1, st["frames"]), 4),
+        "unserved_past_clip_end": st["unserved"],
+        "frames_per_round": args.serve_max_frames, "decode_ahead": args.serve_ahead,
         "key_lane": True, "start_spread_s": 1.0, "key_frames": st["key_frames"],
     }
     del srv
@@ -932,7 +936,8 @@ def main():
     ap.add_argument("--serve-frames", type=int, default=600)
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--serve-check-seconds", type=float, default=1.5)
-    ap.add_argument("--serve-max-frames", type=int, default=2)
+    ap.add_argument("--serve-max-frames", type=int, default=4, help="frames of one stream per serving round")
+    ap.add_argument("--serve-ahead", type=int, default=8, help="frames decoded ahead of each stream's requests")
     ap.add_argument("--serve-seed", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the RGBA, ingest, alt-ref and analysis legs")

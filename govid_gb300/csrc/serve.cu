@@ -3,24 +3,26 @@
 // per-request latency.
 //
 // Each stream issues frame requests as a Poisson process at its frame rate.
-// A round decodes, for every admitted stream with queued requests, the run
-// of requested frames at its head (one frame for a stream that keeps up, a
-// few for one that fell behind — the engine's per-stream lookahead), all in
-// one set of kernel launches; requests that arrive while a round runs join
-// the next one.  A seek request moves the stream to a key frame
-// (ebiv/reader.go:222-238 semantics: decoding restarts there exactly); a
-// looping stream seeks back to its first frame at the end.  Streams are
-// admitted while the sum of their HBM footprints (frame pool + scratch)
-// fits the budget; a finished stream releases its memory and the next
-// waiting stream is admitted.
+// A decode thread keeps every admitted stream a few frames ahead of its
+// requests (govid's AsyncPlayer keeps `depth` frames ready the same way,
+// source.go:84-187), batching all streams' next frames into shared rounds;
+// requests are served in order from the decoded frames as they arrive.  A
+// seek request moves the stream to a key frame (ebiv/reader.go:222-238
+// semantics: decoding restarts there exactly); a looping stream continues
+// from its first frame at the end.  Streams are admitted while the sum of
+// their HBM footprints (frame pool + scratch + packets) fits the budget; a
+// finished stream releases its memory and the next waiting stream is
+// admitted.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
 #include <cmath>
 #include <cstring>
 #include <deque>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <random>
 #include <thread>
@@ -51,11 +53,12 @@ struct ServeOptionsC {
   double seekProb = 0.05;
   uint64_t seed = 1;
   uint64_t hbmBudget = 120ull << 30;
-  int maxFramesPerRound = 4;
+  int maxFramesPerRound = 4;  // frames of one stream per round (the engine's lookahead)
   int ring = 3;
   int record = 0;
-  int keyLane = 1;  // key frames decode on the engine's side lane
+  int keyLane = 1;  // long key frames decode on the engine's side lane
   double startSpread = 0;  // streams admitted at start begin at a uniform offset in [0, startSpread) s
+  int decodeAhead = 0;     // frames decoded ahead of each stream's requests (0: twice the lookahead)
 };
 
 struct ServeStatsC {
@@ -64,13 +67,30 @@ struct ServeStatsC {
   double elapsed = 0, p50 = 0, p99 = 0, pmax = 0, mean = 0, framesPerSec = 0, kernelMs = 0, entropyMs = 0, reconMs = 0;
   int64_t keyFrames = 0;
   uint64_t peakBytes = 0;
+  int64_t readyAtArrival = 0, unserved = 0;
+  double seekP50 = 0, seekP99 = 0;
 };
 
+// Two threads.  The decode thread owns the engine: it keeps every admitted
+// stream up to `decodeAhead` frames ahead of its requests, in rounds of up
+// to `maxFramesPerRound` frames per stream (their entropy stages in one
+// launch); key frames whose tiles carry long entropy chains go to the
+// engine's side lane so they never hold up a round.  It also admits streams
+// (HBM budget) and removes finished ones.  The request thread generates
+// each stream's Poisson requests, serves them in order from the decoded
+// frames, and applies seeks (a new epoch: frames decoded for the old
+// position are dropped, decoding restarts at the key frame).  A request's
+// latency runs from its arrival to the moment its frame is decoded and
+// handed out (zero wait when the frame was ready before it was asked for).
 class Server {
  public:
-  explicit Server(const ServeOptionsC& o) : opt_(o), rng_(o.seed) {}
+  explicit Server(const ServeOptionsC& o) : opt_(o), rng_(o.seed) {
+    lookahead_ = std::max(1, opt_.maxFramesPerRound);
+    ahead_ = opt_.decodeAhead > 0 ? opt_.decodeAhead : 2 * lookahead_;
+    ahead_ = std::max(ahead_, lookahead_);
+  }
   int init() {
-    int st = eng_.setLookahead(std::max(1, opt_.maxFramesPerRound));
+    int st = eng_.setLookahead(lookahead_);
     if (st) return st;
     st = eng_.init();
     if (st) return st;
@@ -81,238 +101,70 @@ class Server {
 
   int addStream(const uint8_t* const* pkts, const size_t* lens, int n, double fps, bool loop) {
     if (n <= 0 || fps <= 0) return kErrArg;
-    Spec sp;
-    sp.pkts.resize((size_t)n);
-    for (int i = 0; i < n; i++) sp.pkts[(size_t)i].assign(pkts[i], pkts[i] + lens[i]);
+    std::unique_ptr<Spec> sp(new (std::nothrow) Spec());
+    if (!sp) return kErrArg;
+    sp->pkts.resize((size_t)n);
+    for (int i = 0; i < n; i++) sp->pkts[(size_t)i].assign(pkts[i], pkts[i] + lens[i]);
     FrameHeader fh;
-    if (parseFrameHeader(sp.pkts[0].data(), sp.pkts[0].size(), &fh) || fh.type != kFrameKey) return kErrCorrupt;
-    sp.w = fh.width;
-    sp.h = fh.height;
+    if (parseFrameHeader(sp->pkts[0].data(), sp->pkts[0].size(), &fh) || fh.type != kFrameKey) return kErrCorrupt;
+    sp->w = fh.width;
+    sp->h = fh.height;
     for (int i = 0; i < n; i++) {
       FrameHeader f;
-      if (parseFrameHeader(sp.pkts[(size_t)i].data(), sp.pkts[(size_t)i].size(), &f) == kOK && f.type == kFrameKey)
-        sp.keys.push_back(i);
+      if (parseFrameHeader(sp->pkts[(size_t)i].data(), sp->pkts[(size_t)i].size(), &f) == kOK && f.type == kFrameKey)
+        sp->keys.push_back(i);
     }
-    sp.fps = fps;
-    sp.loop = loop;
-    sp.footprint = Engine::footprint(sp.w, sp.h, opt_.ring, std::max(1, opt_.maxFramesPerRound), false,
-                                     opt_.keyLane != 0) +
-                   [&] {
-                     size_t b = 0;
-                     for (auto& p : sp.pkts) b += (p.size() + 15) / 16 * 16;
-                     return b;
-                   }();
+    sp->longKey = opt_.keyLane && maxTileMBs(sp->pkts[0], fh) > kLongKeyMBs;
+    sp->fps = fps;
+    sp->loop = loop;
+    sp->footprint = Engine::footprint(sp->w, sp->h, ringOf(), lookahead_, 0, opt_.keyLane != 0);
+    for (auto& p : sp->pkts) sp->footprint += (p.size() + 15) / 16 * 16;
     specs_.push_back(std::move(sp));
     return kOK;
   }
 
   int run(ServeStatsC* out) {
-    std::deque<int> waiting;
-    for (size_t i = 0; i < specs_.size(); i++) waiting.push_back((int)i);
-    std::vector<int> admitted;  // spec indices
-    std::vector<int> specOf;    // engine stream id -> spec index
-    uint64_t used = 0;
-    ServeStatsC st;
-    const double t0 = nowSec();
-    auto admit = [&] {
-      while (!waiting.empty() && used + specs_[(size_t)waiting.front()].footprint <= opt_.hbmBudget) {
-        const int si = waiting.front();
-        waiting.pop_front();
-        Spec& sp = specs_[(size_t)si];
-        std::vector<const uint8_t*> ptrs;
-        std::vector<size_t> lens;
-        for (auto& p : sp.pkts) {
-          ptrs.push_back(p.data());
-          lens.push_back(p.size());
-        }
-        if (eng_.addResidentStream(ptrs.data(), lens.data(), (int)ptrs.size(), opt_.ring, &sp.engineId)) break;
-        if ((int)specOf.size() <= sp.engineId) specOf.resize((size_t)sp.engineId + 1, -1);
-        specOf[(size_t)sp.engineId] = si;
-        sp.nextArrival = nowSec() - t0;
-        if (opt_.startSpread > 0 && st.rounds == 0)
-          sp.nextArrival += std::uniform_real_distribution<double>(0, opt_.startSpread)(rng_);
-        sp.pos = 0;
-        used += sp.footprint;
-        admitted.push_back(si);
-        st.admittedTotal++;
-        st.admittedPeak = std::max<int64_t>(st.admittedPeak, (int64_t)admitted.size());
-        st.peakBytes = std::max<uint64_t>(st.peakBytes, used);
-      }
-    };
-    admit();
-    std::vector<double> lat;
-    // Each result answers the head request of its stream.
-    auto deliver = [&](const std::vector<RoundResult>& rs, double done) {
-      for (const RoundResult& r : rs) {
-        const int si = r.stream >= 0 && r.stream < (int)specOf.size() ? specOf[(size_t)r.stream] : -1;
-        if (si < 0) continue;
-        Spec& sp = specs_[(size_t)si];
-        if (sp.queue.empty()) continue;
-        const Request req = sp.queue.front();
-        sp.queue.pop_front();
-        sp.pos = r.frameIndex + 1;
-        if (r.status != kOK) {
-          st.errors++;
-          continue;
-        }
-        st.frames++;
-        if (r.keyframe) st.keyFrames++;
-        lat.push_back(done - req.arrival);
-        if (opt_.record) {
-          const int cw = (r.view.width + 1) / 2, ch = (r.view.height + 1) / 2;
-          std::vector<uint8_t> buf((size_t)r.view.width * r.view.height + 2 * (size_t)cw * ch);
-          eng_.downloadFrame(r.view, buf.data(), buf.size());
-          hashes_.push_back({si, r.frameIndex, fnv1a(buf.data(), buf.size())});
-        }
-      }
-    };
-    // Applies the head request's seek and the clip end (loop, or drop the
-    // requests of a finished clip); false when there is nothing to decode.
-    auto prepareHead = [&](Spec& sp) -> bool {
-      if (sp.queue.empty()) return false;
-      Request& head = sp.queue.front();
-      if (head.seekTo >= 0) {
-        eng_.seekStream(sp.engineId, head.seekTo);
-        sp.pos = head.seekTo;
-        head.seekTo = -1;
-        st.seeks++;
-      }
-      if (sp.pos >= (int64_t)sp.pkts.size()) {
-        if (!sp.loop) {
-          sp.queue.clear();  // the clip ended: the remaining requests cannot be served
-          return false;
-        }
-        eng_.seekStream(sp.engineId, 0);
-        sp.pos = 0;
-        st.loops++;
-      }
-      return true;
-    };
-    auto isKey = [](const Spec& sp, int64_t i) { return std::binary_search(sp.keys.begin(), sp.keys.end(), i); };
-    std::vector<RoundResult> res;
-    std::vector<int> sideSpecs;
-    for (;;) {
-      const double now = nowSec() - t0;
-      // Arrivals up to now.
-      for (int si : admitted) {
-        Spec& sp = specs_[(size_t)si];
-        while (sp.nextArrival <= now && sp.nextArrival <= opt_.duration && sp.issued < opt_.framesPerStream &&
-               !sp.done) {
-          Request r;
-          r.arrival = sp.nextArrival;
-          if (std::uniform_real_distribution<double>(0, 1)(rng_) < opt_.seekProb && !sp.keys.empty()) {
-            r.seekTo = sp.keys[std::uniform_int_distribution<size_t>(0, sp.keys.size() - 1)(rng_)];
-          }
-          sp.queue.push_back(r);
-          sp.issued++;
-          st.requests++;
-          sp.nextArrival += std::exponential_distribution<double>(sp.fps)(rng_);
-        }
-      }
-      // Key lane: collect a finished side round, then send every stream whose
-      // next frame is a key frame (start, seek, loop, GOP boundary) to it, so
-      // no main round waits for a key frame's long entropy chains.
-      if (opt_.keyLane && eng_.sideBusy() && eng_.sideReady()) {
-        res.clear();
-        eng_.collectSide(&res);
-        deliver(res, nowSec() - t0);
-        for (int si : sideSpecs) specs_[(size_t)si].inSide = false;
-        sideSpecs.clear();
-        st.rounds++;
-      }
-      if (opt_.keyLane && !eng_.sideBusy()) {
-        std::vector<int> kids, kcap;
-        for (int si : admitted) {
-          Spec& sp = specs_[(size_t)si];
-          if (sp.inSide || !prepareHead(sp) || !isKey(sp, sp.pos)) continue;
-          kids.push_back(sp.engineId);
-          kcap.push_back(1);
-          sideSpecs.push_back(si);
-          sp.inSide = true;
-        }
-        if (!kids.empty() && eng_.launchSide(kids, &kcap)) return kErrDevice;
-      }
-      // Main round: each stream's run of plain requests at its queue head,
-      // ending before a seek and (with the key lane) before a key frame.
-      std::vector<int> ids, counts;
-      for (int si : admitted) {
-        Spec& sp = specs_[(size_t)si];
-        if (sp.inSide || !prepareHead(sp)) continue;
-        if (opt_.keyLane && isKey(sp, sp.pos)) continue;  // waits for the key lane
-        int n = 0;
-        for (const Request& r : sp.queue) {
-          if (n > 0 && r.seekTo >= 0) break;
-          if (++n >= opt_.maxFramesPerRound) break;
-        }
-        n = (int)std::min<int64_t>(n, (int64_t)sp.pkts.size() - sp.pos);
-        if (opt_.keyLane) {
-          const auto nk = std::upper_bound(sp.keys.begin(), sp.keys.end(), sp.pos);
-          if (nk != sp.keys.end()) n = (int)std::min<int64_t>(n, *nk - sp.pos);
-        }
-        ids.push_back(sp.engineId);
-        counts.push_back(n);
-      }
-      if (ids.empty()) {
-        // Finished streams release their memory; admit waiting ones.
-        bool changed = false;
-        for (size_t k = 0; k < admitted.size();) {
-          Spec& sp = specs_[(size_t)admitted[k]];
-          const bool ended = !sp.inSide && sp.queue.empty() &&
-                             (sp.issued >= opt_.framesPerStream || sp.nextArrival > opt_.duration ||
-                              (!sp.loop && sp.pos >= (int64_t)sp.pkts.size()));
-          if (ended) {
-            eng_.removeStream(sp.engineId);
-            used -= sp.footprint;
-            sp.done = true;
-            admitted.erase(admitted.begin() + (long)k);
-            changed = true;
-          } else {
-            k++;
-          }
-        }
-        if (changed) admit();
-        if (admitted.empty() && waiting.empty()) break;
-        if (now > opt_.duration && admitted.empty()) break;
-        double nextT = 1e30;
-        for (int si : admitted) nextT = std::min(nextT, specs_[(size_t)si].nextArrival);
-        if (nextT > opt_.duration + 1 && waiting.empty() && !eng_.sideBusy()) {
-          bool pending = false;
-          for (int si : admitted) pending |= !specs_[(size_t)si].queue.empty();
-          if (!pending) break;
-        }
-        double wait = nextT - (nowSec() - t0);
-        if (eng_.sideBusy()) wait = std::min(wait, 0.0002);  // poll the key lane
-        if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.005)));
-        continue;
-      }
-      res.clear();
-      eng_.roundFor(ids, &res, &counts);
-      st.rounds++;
-      deliver(res, nowSec() - t0);
+    for (size_t i = 0; i < specs_.size(); i++) waiting_.push_back((int)i);
+    if (cudaGetDevice(&device_) != cudaSuccess) return kErrDevice;
+    t0_ = nowSec();
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      admit(true);
     }
-    if (eng_.sideBusy()) {
-      res.clear();
-      eng_.collectSide(&res);
-      deliver(res, nowSec() - t0);
+    std::thread dec([this] { decodeLoop(); });
+    requestLoop();
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
     }
-    st.elapsed = nowSec() - t0;
-    st.waitingAtEnd = (int64_t)waiting.size();
-    std::sort(lat.begin(), lat.end());
+    cvDecode_.notify_all();
+    dec.join();
+    ServeStatsC st = st_;
+    st.elapsed = endTime_;
+    st.waitingAtEnd = (int64_t)waiting_.size();
+    auto pctl = [](std::vector<double>& v, double q) {
+      if (v.empty()) return 0.0;
+      std::sort(v.begin(), v.end());
+      return v[(size_t)std::min<double>(v.size() - 1, std::floor(q * (v.size() - 1)))] * 1000;
+    };
+    std::vector<double> lat = lat_;
     latencies_ = lat;
     if (!lat.empty()) {
-      st.p50 = lat[lat.size() / 2] * 1000;
-      st.p99 = lat[(size_t)std::min<double>(lat.size() - 1, std::floor(0.99 * (lat.size() - 1)))] * 1000;
+      st.p50 = pctl(lat, 0.5);
+      st.p99 = pctl(lat, 0.99);
       st.pmax = lat.back() * 1000;
-      double s = 0;
-      for (double v : lat) s += v;
-      st.mean = s / lat.size() * 1000;
+      double sum = 0;
+      for (double v : lat) sum += v;
+      st.mean = sum / lat.size() * 1000;
     }
+    st.seekP50 = pctl(seekLat_, 0.5);
+    st.seekP99 = pctl(seekLat_, 0.99);
     st.framesPerSec = st.elapsed > 0 ? st.frames / st.elapsed : 0;
     st.kernelMs = eng_.kernelMillis();
     st.entropyMs = eng_.entropyMillis();
     st.reconMs = eng_.reconMillis();
     *out = st;
-    return kOK;
+    return decodeStatus_;
   }
 
   const std::vector<double>& latencies() const { return latencies_; }
@@ -324,31 +176,371 @@ class Server {
   const std::vector<Hash>& hashes() const { return hashes_; }
 
  private:
+  // A key frame whose largest tile has more macroblocks than this takes
+  // longer to entropy-decode (about 4.6 us per macroblock on one warp) than
+  // a round of the longest inter chains in a mixed set of streams, so it
+  // goes to the side lane.
+  static constexpr int kLongKeyMBs = 1500;
+
   struct Request {
     double arrival = 0;
     int64_t seekTo = -1;
+  };
+  struct Ready {
+    int64_t frame = -1;
+    int status = kOK;
+    bool keyframe = false;
+    uint64_t hash = 0;
+    double at = 0;  // when it was decoded
   };
   struct Spec {
     std::vector<std::vector<uint8_t>> pkts;
     std::vector<int64_t> keys;
     int w = 0, h = 0;
     double fps = 30;
-    bool loop = false;
+    bool loop = false, longKey = false;
     uint64_t footprint = 0;
+    // shared (mu_)
     int engineId = -1;
+    bool admitted = false, done = false, finished = false;
+    double startAt = 0;
+    uint64_t epoch = 0;       // bumped by a seek
+    int64_t seekTarget = 0;   // where the newest epoch starts
+    std::deque<Ready> ready;  // decoded frames of the current epoch, in order
+    int inflight = 0;         // frames in a round of the current epoch
+    // request thread
+    bool started = false;
     double nextArrival = 0;
-    int64_t issued = 0;
-    int64_t pos = 0;
-    bool done = false;
-    bool inSide = false;  // its key frame is on the side lane
+    int64_t issued = 0, consumePos = 0;
     std::deque<Request> queue;
+    // decode thread
+    uint64_t decEpoch = 0;
+    bool inSide = false;
   };
+
+  int ringOf() const { return std::max(opt_.ring, ahead_ + 2); }
+
+  // The largest tile of a key frame's coded payload: frame header, then the
+  // override length when present, qp, tile columns, tile rows
+  // (ebiv/frame.go:224-236), split as tileGrid does.
+  static int maxTileMBs(const std::vector<uint8_t>& pkt, const FrameHeader& fh) {
+    const Geometry g = Geometry::of(fh.width, fh.height);
+    size_t p = fh.bodyOffset;
+    auto uv = [&](uint64_t* v) {
+      *v = 0;
+      for (int sh = 0; p < pkt.size() && sh < 64; sh += 7) {
+        const uint8_t c = pkt[p++];
+        *v |= (uint64_t)(c & 0x7F) << sh;
+        if (c < 0x80) return true;
+      }
+      return false;
+    };
+    uint64_t skip = 0, cols = 1, rows = 1;
+    if (fh.coding != kCodingIntra) return g.mbCols * g.mbRows;
+    if (fh.goldenOverride && !uv(&skip)) return g.mbCols * g.mbRows;
+    p++;  // qp
+    if (!uv(&cols) || !uv(&rows)) return g.mbCols * g.mbRows;
+    const TileGrid grid(g.mbCols, g.mbRows, (int)std::min<uint64_t>(cols, 1 << 16),
+                        (int)std::min<uint64_t>(rows, 1 << 16));
+    int m = 0;
+    for (int t = 0; t < grid.count(); t++) {
+      int x0, x1, y0, y1;
+      grid.bounds(t, &x0, &x1, &y0, &y1);
+      m = std::max(m, (x1 - x0) * (y1 - y0));
+    }
+    return m;
+  }
+
+  bool isKey(const Spec& sp, int64_t i) const { return std::binary_search(sp.keys.begin(), sp.keys.end(), i); }
+  double now() const { return nowSec() - t0_; }
+
+  // Admits waiting streams while their footprints fit (decode thread, or
+  // before it starts; mu_ held).
+  void admit(bool initial) {
+    while (!waiting_.empty() && used_ + specs_[(size_t)waiting_.front()]->footprint <= opt_.hbmBudget) {
+      const int si = waiting_.front();
+      Spec& sp = *specs_[(size_t)si];
+      std::vector<const uint8_t*> ptrs;
+      std::vector<size_t> lens;
+      for (auto& p : sp.pkts) {
+        ptrs.push_back(p.data());
+        lens.push_back(p.size());
+      }
+      if (eng_.addResidentStream(ptrs.data(), lens.data(), (int)ptrs.size(), ringOf(), &sp.engineId)) break;
+      waiting_.pop_front();
+      if ((int)specOf_.size() <= sp.engineId) specOf_.resize((size_t)sp.engineId + 1, -1);
+      specOf_[(size_t)sp.engineId] = si;
+      sp.startAt = now();
+      if (initial && opt_.startSpread > 0)
+        sp.startAt += std::uniform_real_distribution<double>(0, opt_.startSpread)(rng_);
+      sp.admitted = true;
+      used_ += sp.footprint;
+      admitted_.push_back(si);
+      st_.admittedTotal++;
+      st_.admittedPeak = std::max<int64_t>(st_.admittedPeak, (int64_t)admitted_.size());
+      st_.peakBytes = std::max<uint64_t>(st_.peakBytes, used_);
+    }
+  }
+
+  // Publishes a round's results (mu_ held): frames of a stream's current
+  // epoch join its ready list; the rest are dropped.
+  void publish(const std::vector<RoundResult>& rs, const std::vector<uint64_t>& hashes,
+               const std::vector<std::pair<int, uint64_t>>& planned) {
+    const double t = now();
+    for (size_t i = 0; i < rs.size(); i++) {
+      const RoundResult& r = rs[i];
+      const int si = r.stream >= 0 && r.stream < (int)specOf_.size() ? specOf_[(size_t)r.stream] : -1;
+      if (si < 0) continue;
+      Spec& sp = *specs_[(size_t)si];
+      uint64_t ep = ~0ull;
+      for (const auto& pl : planned)
+        if (pl.first == si) ep = pl.second;
+      if (ep != sp.epoch) continue;
+      Ready rd;
+      rd.frame = r.frameIndex;
+      rd.status = r.status;
+      rd.keyframe = r.keyframe;
+      rd.hash = i < hashes.size() ? hashes[i] : 0;
+      rd.at = t;
+      sp.ready.push_back(rd);
+    }
+    for (const auto& pl : planned) {
+      Spec& sp = *specs_[(size_t)pl.first];
+      if (pl.second == sp.epoch) sp.inflight = 0;
+    }
+  }
+
+  void hashResults(const std::vector<RoundResult>& rs, std::vector<uint64_t>* out) {
+    out->assign(rs.size(), 0);
+    if (!opt_.record) return;
+    std::vector<uint8_t> buf;
+    for (size_t i = 0; i < rs.size(); i++) {
+      const RoundResult& r = rs[i];
+      if (r.status != kOK) continue;
+      const int cw = (r.view.width + 1) / 2, ch = (r.view.height + 1) / 2;
+      buf.resize((size_t)r.view.width * r.view.height + 2 * (size_t)cw * ch);
+      if (eng_.downloadFrame(r.view, buf.data(), buf.size()) == kOK) (*out)[i] = fnv1a(buf.data(), buf.size());
+    }
+  }
+
+  void decodeLoop() {
+    cudaSetDevice(device_);
+    std::vector<RoundResult> res;
+    std::vector<uint64_t> hashes;
+    std::vector<std::pair<int, uint64_t>> sidePlanned;
+    for (;;) {
+      std::vector<int> ids, counts, kids, kcap, reposition;
+      std::vector<int64_t> repoTo;
+      std::vector<std::pair<int, uint64_t>> planned;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        if (stop_) break;
+        // Finished streams leave; waiting ones come in.
+        bool removed = false;
+        for (size_t k = 0; k < admitted_.size();) {
+          Spec& sp = *specs_[(size_t)admitted_[k]];
+          if (sp.finished && !sp.inSide) {
+            eng_.removeStream(sp.engineId);
+            used_ -= sp.footprint;
+            sp.done = true;
+            admitted_.erase(admitted_.begin() + (long)k);
+            removed = true;
+          } else {
+            k++;
+          }
+        }
+        if (removed) admit(false);
+        for (int si : admitted_) {
+          Spec& sp = *specs_[(size_t)si];
+          if (sp.inSide || sp.finished) continue;
+          if (sp.decEpoch != sp.epoch) {  // a seek: restart at its key frame
+            sp.decEpoch = sp.epoch;
+            reposition.push_back(sp.engineId);
+            repoTo.push_back(sp.seekTarget);
+            continue;  // planned next time round, after the engine moved
+          }
+          const int room = ahead_ - (int)sp.ready.size() - sp.inflight;
+          if (room <= 0) continue;
+          int64_t pos = (int64_t)sp.pkts.size() - eng_.remaining(sp.engineId);
+          if (pos >= (int64_t)sp.pkts.size()) {
+            if (!sp.loop) continue;
+            reposition.push_back(sp.engineId);  // looping: on from the first frame
+            repoTo.push_back(0);
+            st_.loops++;
+            continue;
+          }
+          if (sp.longKey && isKey(sp, pos)) {
+            if (!eng_.sideBusy() && kids.size() < 64) {
+              kids.push_back(sp.engineId);
+              kcap.push_back(1);
+              sp.inSide = true;
+              sp.inflight = 1;
+              sidePlanned.push_back({si, sp.epoch});
+            }
+            continue;
+          }
+          int n = std::min(room, lookahead_);
+          n = (int)std::min<int64_t>(n, (int64_t)sp.pkts.size() - pos);
+          if (sp.longKey) {  // stop before the next long key frame
+            const auto nk = std::upper_bound(sp.keys.begin(), sp.keys.end(), pos);
+            if (nk != sp.keys.end()) n = (int)std::min<int64_t>(n, *nk - pos);
+          }
+          ids.push_back(sp.engineId);
+          counts.push_back(n);
+          sp.inflight = n;
+          planned.push_back({si, sp.epoch});
+        }
+        if (ids.empty() && kids.empty() && reposition.empty() && !eng_.sideBusy()) {
+          cvDecode_.wait_for(lk, std::chrono::microseconds(500));
+          continue;
+        }
+      }
+      for (size_t k = 0; k < reposition.size(); k++) eng_.seekStream(reposition[k], repoTo[k]);
+      if (!kids.empty() && eng_.launchSide(kids, &kcap)) {
+        std::lock_guard<std::mutex> lk(mu_);
+        decodeStatus_ = kErrDevice;
+        stop_ = true;
+        cvRequest_.notify_all();
+        break;
+      }
+      if (!ids.empty()) {
+        res.clear();
+        if (eng_.roundFor(ids, &res, &counts) < 0) {
+          std::lock_guard<std::mutex> lk(mu_);
+          decodeStatus_ = kErrDevice;
+          stop_ = true;
+          cvRequest_.notify_all();
+          break;
+        }
+        hashResults(res, &hashes);
+        std::lock_guard<std::mutex> lk(mu_);
+        st_.rounds++;
+        publish(res, hashes, planned);
+        cvRequest_.notify_all();
+      } else if (eng_.sideBusy() && !eng_.sideReady()) {
+        std::this_thread::sleep_for(std::chrono::microseconds(100));
+      }
+      if (eng_.sideBusy() && eng_.sideReady()) {
+        res.clear();
+        eng_.collectSide(&res);
+        hashResults(res, &hashes);
+        std::lock_guard<std::mutex> lk(mu_);
+        st_.rounds++;
+        publish(res, hashes, sidePlanned);
+        for (const auto& pl : sidePlanned) specs_[(size_t)pl.first]->inSide = false;
+        sidePlanned.clear();
+        cvRequest_.notify_all();
+      }
+    }
+    if (eng_.sideBusy()) {
+      res.clear();
+      eng_.collectSide(&res);
+    }
+  }
+
+  // Serves the head requests of a stream from its ready frames (mu_ held).
+  void serve(Spec& sp, int si, double t) {
+    while (!sp.queue.empty()) {
+      Request& head = sp.queue.front();
+      if (head.seekTo >= 0) {  // Seek: a new epoch at the key frame
+        sp.epoch++;
+        sp.seekTarget = head.seekTo;
+        sp.ready.clear();
+        sp.inflight = 0;
+        sp.consumePos = head.seekTo;
+        head.seekTo = -2;  // applied; the request wants the key frame
+        st_.seeks++;
+        cvDecode_.notify_all();
+      }
+      if (sp.consumePos >= (int64_t)sp.pkts.size()) {
+        if (!sp.loop) {  // the clip ended: the remaining requests cannot be served
+          st_.unserved += (int64_t)sp.queue.size();
+          sp.queue.clear();
+          return;
+        }
+        sp.consumePos = 0;
+      }
+      while (!sp.ready.empty() && sp.ready.front().frame != sp.consumePos) sp.ready.pop_front();
+      if (sp.ready.empty()) return;
+      const Ready rd = sp.ready.front();
+      sp.ready.pop_front();
+      const bool wasSeek = head.seekTo == -2;
+      const double arrival = head.arrival;
+      sp.queue.pop_front();
+      sp.consumePos++;
+      cvDecode_.notify_all();
+      if (rd.status != kOK) {
+        st_.errors++;
+        continue;
+      }
+      st_.frames++;
+      if (rd.keyframe) st_.keyFrames++;
+      const double l = std::max(0.0, std::max(t, rd.at) - arrival);
+      lat_.push_back(l);
+      if (wasSeek) seekLat_.push_back(l);
+      if (rd.at <= arrival) st_.readyAtArrival++;
+      if (opt_.record) hashes_.push_back({si, rd.frame, rd.hash});
+    }
+  }
+
+  void requestLoop() {
+    std::unique_lock<std::mutex> lk(mu_);
+    for (;;) {
+      if (stop_) break;
+      const double t = now();
+      double nextT = 1e30;
+      bool live = !waiting_.empty() && (!admitted_.empty() || t <= opt_.duration);
+      for (size_t si = 0; si < specs_.size(); si++) {
+        Spec& sp = *specs_[si];
+        if (!sp.admitted || sp.done || sp.finished) continue;
+        live = true;
+        if (!sp.started) {
+          sp.started = true;
+          sp.nextArrival = sp.startAt;
+        }
+        while (sp.nextArrival <= t && sp.nextArrival <= opt_.duration && sp.issued < opt_.framesPerStream) {
+          Request r;
+          r.arrival = sp.nextArrival;
+          if (sp.issued > 0 && std::uniform_real_distribution<double>(0, 1)(rng_) < opt_.seekProb && !sp.keys.empty())
+            r.seekTo = sp.keys[std::uniform_int_distribution<size_t>(0, sp.keys.size() - 1)(rng_)];
+          sp.queue.push_back(r);
+          sp.issued++;
+          st_.requests++;
+          sp.nextArrival += std::exponential_distribution<double>(sp.fps)(rng_);
+        }
+        serve(sp, (int)si, t);
+        const bool noMore = sp.issued >= opt_.framesPerStream || sp.nextArrival > opt_.duration;
+        if (noMore && sp.queue.empty()) {
+          sp.finished = true;  // the decode thread removes it and admits the next
+          cvDecode_.notify_all();
+          continue;
+        }
+        if (!noMore) nextT = std::min(nextT, sp.nextArrival);
+      }
+      if (!live) break;
+      const double wait = std::min(nextT - now(), 0.002);
+      if (wait > 0) cvRequest_.wait_for(lk, std::chrono::duration<double>(wait));
+    }
+    endTime_ = now();
+  }
+
   ServeOptionsC opt_;
+  int lookahead_ = 1, ahead_ = 2;
   Engine eng_;
   std::mt19937_64 rng_;
-  std::vector<Spec> specs_;
-  std::vector<RoundResult> results_;
-  std::vector<double> latencies_;
+  std::vector<std::unique_ptr<Spec>> specs_;
+  std::mutex mu_;
+  std::condition_variable cvDecode_, cvRequest_;
+  std::deque<int> waiting_;
+  std::vector<int> admitted_;
+  std::vector<int> specOf_;  // engine stream id -> spec index
+  uint64_t used_ = 0;
+  bool stop_ = false;
+  int decodeStatus_ = kOK;
+  int device_ = 0;
+  double t0_ = 0, endTime_ = 0;
+  ServeStatsC st_;
+  std::vector<double> lat_, seekLat_, latencies_;
   std::vector<Hash> hashes_;
 };
 
@@ -378,6 +570,7 @@ int ebivgpu_server_create(const ebivgpu_serve_options* o, ebivgpu_server** out) 
   c.record = o->record;
   c.keyLane = o->key_lane;
   c.startSpread = o->start_spread_s > 0 ? o->start_spread_s : 0;
+  c.decodeAhead = o->decode_ahead > 0 ? o->decode_ahead : 0;
   ebivgpu_server* h = new (std::nothrow) ebivgpu_server();
   if (!h) return kErrDevice;
   h->s.reset(new Server(c));
@@ -420,6 +613,10 @@ int ebivgpu_server_run(ebivgpu_server* h, ebivgpu_serve_stats* out) {
   out->recon_ms = st.reconMs;
   out->key_frames = st.keyFrames;
   out->peak_bytes = st.peakBytes;
+  out->ready_at_arrival = st.readyAtArrival;
+  out->unserved = st.unserved;
+  out->seek_latency_p50_ms = st.seekP50;
+  out->seek_latency_p99_ms = st.seekP99;
   return r;
 }
 

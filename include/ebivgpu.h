@@ -170,12 +170,17 @@ uint64_t ebivgpu_batch_device_bytes(ebivgpu_batch* b);
 uint64_t ebivgpu_stream_footprint(int width, int height, int ring, int lookahead);
 /* ---- Serving loop --------------------------------------------------------
  * Continuous batching of per-frame requests from many streams: each stream
- * issues requests as a Poisson process at its frame rate; every round
- * decodes the requested frames of all streams with queued requests in one
- * set of launches; seeks go to key frames, looping streams restart at the
- * end; streams are admitted while their HBM footprints fit the budget and
- * release it when they finish.  No single reference counterpart: the
- * reference serves one Player per stream (player.go, source.go). */
+ * issues requests as a Poisson process at its frame rate; a decode thread
+ * keeps every admitted stream up to decode_ahead frames ahead of its
+ * requests, all streams' next frames (max_frames_per_round each) in shared
+ * rounds, key frames with long entropy chains on a side lane; requests are
+ * served in order as their frames are ready (latency: arrival to hand-out,
+ * zero wait when the frame was decoded before it was asked for); seeks go
+ * to key frames (frames decoded for the old position are dropped), looping
+ * streams continue from their first frame; streams are admitted while their
+ * HBM footprints fit the budget and release it when they finish.  No single
+ * reference counterpart: the reference serves one Player per stream, each
+ * an AsyncPlayer decoding ahead (player.go, source.go). */
 typedef struct ebivgpu_server ebivgpu_server;
 typedef struct {
   double duration_s;           /* requests arrive during this many seconds */
@@ -188,6 +193,7 @@ typedef struct {
   int32_t record;              /* hash every delivered frame (testing) */
   int32_t key_lane;            /* key frames decode on a side lane beside the main rounds (1 = on) */
   double start_spread_s;       /* streams admitted at start begin uniformly within this many seconds */
+  int32_t decode_ahead;        /* frames decoded ahead of each stream's requests (0: twice max_frames_per_round) */
 } ebivgpu_serve_options;
 typedef struct {
   int64_t requests, frames, errors, seeks, loops, rounds;
@@ -196,6 +202,9 @@ typedef struct {
   double entropy_ms, recon_ms; /* kernel_ms split: entropy stage, reconstruction stages */
   int64_t key_frames;          /* key frames decoded (stream starts, seeks, loops) */
   uint64_t peak_bytes;
+  int64_t ready_at_arrival;    /* requests whose frame was decoded before they arrived */
+  int64_t unserved;            /* requests past the end of a clip that does not loop */
+  double seek_latency_p50_ms, seek_latency_p99_ms; /* requests that were seeks */
 } ebivgpu_serve_stats;
 int ebivgpu_server_create(const ebivgpu_serve_options* o, ebivgpu_server** out);
 int ebivgpu_server_add_stream(ebivgpu_server* s, const uint8_t* const* pkts, const size_t* lens, int n, double fps,

@@ -51,3 +51,30 @@ def test_admission_respects_hbm_budget(gpu_required):
     st = srv.run()
     assert st["admitted_peak"] <= 2
     assert st["admitted_total"] == 4 and st["errors"] == 0
+
+
+def test_decode_ahead_serves_requests_from_ready_frames(gpu_required):
+    # Under a light load every stream is kept ahead of its requests, so most
+    # requests find their frame already decoded; seeks restart decoding at
+    # their key frame and the frames that follow match the stream alone.
+    streams = _streams()
+    srv = ebiv.Server(duration_s=1.0, frames_per_stream=30, seek_prob=0.05, seed=11, record=True,
+                      max_frames_per_round=2, decode_ahead=6)
+    for i, (pk, w, h) in enumerate(streams):
+        srv.add_stream(pk, fps=30, loop=True)
+    st = srv.run()
+    assert st["errors"] == 0 and st["frames"] > 0
+    assert st["ready_at_arrival"] >= st["frames"] // 2, st
+    assert st["frames"] + st["unserved"] == st["requests"]
+    alone = [[ebiv.frame_hash(p) for _, p in ebiv_oracle.decode_all(pk)] for pk, _, _ in streams]
+    for s, f, h in srv.frame_hashes():
+        assert h == alone[s][f]
+
+
+def test_stream_larger_than_the_budget_is_never_admitted(gpu_required):
+    s0 = _streams()[0]
+    srv = ebiv.Server(duration_s=0.3, frames_per_stream=10, seed=2, hbm_budget_bytes=1 << 20,
+                      max_frames_per_round=2)
+    srv.add_stream(s0[0], fps=60)
+    st = srv.run()
+    assert st["admitted_total"] == 0 and st["waiting_at_end"] == 1 and st["frames"] == 0
