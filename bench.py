@@ -830,6 +830,11 @@ def run_serve(args):
         "ready_at_arrival_frac": round(st["ready_at_arrival"] / max(1, st["frames"]), 4),
         "unserved_past_clip_end": st["unserved"],
         "frames_per_round": args.serve_max_frames, "decode_ahead": args.serve_ahead,
+        "elapsed_s": round(st["elapsed_s"], 3),
+        "decode_thread": {"main_rounds": st["main_rounds"], "side_rounds": st["side_rounds"],
+                          "main_round_frames": st["main_frames"], "main_round_s": round(st["main_round_s"], 3),
+                          "idle_s": round(st["idle_s"], 3), "kernel_ms": round(st["kernel_ms"], 1),
+                          "entropy_ms": round(st["entropy_ms"], 1), "recon_ms": round(st["recon_ms"], 1)},
         "key_lane": True, "start_spread_s": 1.0, "key_frames": st["key_frames"],
     }
     del srv
@@ -937,7 +942,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--serve-check-seconds", type=float, default=1.5)
     ap.add_argument("--serve-max-frames", type=int, default=4, help="frames of one stream per serving round")
-    ap.add_argument("--serve-ahead", type=int, default=8, help="frames decoded ahead of each stream's requests")
+    ap.add_argument("--serve-ahead", type=int, default=6, help="frames decoded ahead of each stream's requests")
     ap.add_argument("--serve-seed", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the RGBA, ingest, alt-ref and analysis legs")

@@ -37,7 +37,7 @@ class ServeOptions(C.Structure):
     _fields_ = [("duration_s", C.c_double), ("frames_per_stream", C.c_int64), ("seek_prob", C.c_double),
                 ("seed", C.c_uint64), ("hbm_budget_bytes", C.c_uint64), ("max_frames_per_round", C.c_int32),
                 ("ring", C.c_int32), ("record", C.c_int32), ("key_lane", C.c_int32),
-                ("start_spread_s", C.c_double), ("decode_ahead", C.c_int32)]
+                ("start_spread_s", C.c_double), ("decode_ahead", C.c_int32), ("decode_lanes", C.c_int32)]
 
 
 class ServeStats(C.Structure):
@@ -47,7 +47,10 @@ class ServeStats(C.Structure):
                                           "latency_mean_ms", "frames_per_s", "kernel_ms", "entropy_ms",
                                           "recon_ms")] + [("key_frames", C.c_int64)] + \
                [("peak_bytes", C.c_uint64), ("ready_at_arrival", C.c_int64), ("unserved", C.c_int64),
-                ("seek_latency_p50_ms", C.c_double), ("seek_latency_p99_ms", C.c_double)]
+                ("seek_latency_p50_ms", C.c_double), ("seek_latency_p99_ms", C.c_double),
+                ("main_rounds", C.c_int64), ("side_rounds", C.c_int64), ("main_frames", C.c_int64),
+                ("main_round_s", C.c_double), ("idle_s", C.c_double), ("plan_s", C.c_double),
+                ("launch_s", C.c_double), ("collect_s", C.c_double)]
 
 
 class Frame(C.Structure):

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <new>
 
@@ -1180,14 +1181,23 @@ int Engine::roundFor(const std::vector<int>& ids, std::vector<RoundResult>* resu
   if (!pipeDepth_) {
     Round& R = rounds_[0];
     R.parity = 0;
-    if (planRound(ids, maxFrames, R) || launchRecon(R)) {
+    const auto t0 = std::chrono::steady_clock::now();
+    const bool failed = planRound(ids, maxFrames, R) != 0;
+    const auto t1 = std::chrono::steady_clock::now();
+    if (failed || launchRecon(R)) {
       for (Job& j : R.jobs)
         if (j.status == kOK) j.status = kErrDevice;
       R.nDesc = 0;
       collectRound(R, results);
       return -1;
     }
-    return collectRound(R, results);
+    const auto t2 = std::chrono::steady_clock::now();
+    const int n = collectRound(R, results);
+    const auto t3 = std::chrono::steady_clock::now();
+    planSec_ += std::chrono::duration<double>(t1 - t0).count();
+    launchSec_ += std::chrono::duration<double>(t2 - t1).count();
+    collectSec_ += std::chrono::duration<double>(t3 - t2).count();
+    return n;
   }
   // Pipelined: plan this round and start its entropy stage; when more than
   // depth rounds are in flight, collect the oldest (whose results this call

@@ -154,6 +154,12 @@ class Engine {
   // kernels on the engine's stream.
   void enableTiming(bool on) { timing_ = on; }
   double kernelMillis() const { return kernelMs_; }
+  // Host time of synchronous rounds: planning (headers, tables, descriptors,
+  // the staging upload and the entropy launch), the reconstruction launches,
+  // and the wait for the round to finish.
+  double planSeconds() const { return planSec_; }
+  double launchSeconds() const { return launchSec_; }
+  double collectSeconds() const { return collectSec_; }
   double entropyMillis() const { return entropyMs_; }
   double reconMillis() const { return reconMs_; }
   void resetTiming() { kernelMs_ = entropyMs_ = reconMs_ = 0; }
@@ -230,6 +236,7 @@ class Engine {
   bool timing_ = false;
   cudaEvent_t ev_[kParities][4] = {};
   double kernelMs_ = 0, entropyMs_ = 0, reconMs_ = 0;
+  double planSec_ = 0, launchSec_ = 0, collectSec_ = 0;
 };
 
 }  // namespace ebiv

@@ -49,8 +49,11 @@ constexpr uint32_t kWriteAll = 0x3FFFFu;
 constexpr int kEntropyTilesPerJob = 4;
 
 // Bytes of symbol log per macroblock in a decode slot (the entropy stage's
-// symbol path; a tile whose symbols do not fit takes the full chain).
-constexpr int kSymPerMB = 96;
+// symbol path; a tile whose symbols do not fit takes the full chain, which
+// decodes it a second time).  Key frames coded at q18 average about 80
+// symbols per macroblock and more in textured areas, and the chain also
+// reserves room for a whole block before decoding it, so the log holds 192.
+constexpr int kSymPerMB = 192;
 
 struct TileStat {
   int32_t err;         // 0 or an ebiv status

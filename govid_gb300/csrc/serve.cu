@@ -59,6 +59,7 @@ struct ServeOptionsC {
   int keyLane = 1;  // long key frames decode on the engine's side lane
   double startSpread = 0;  // streams admitted at start begin at a uniform offset in [0, startSpread) s
   int decodeAhead = 0;     // frames decoded ahead of each stream's requests (0: twice the lookahead)
+  int lanes = 0;           // decode lanes (engines with their own thread and side lane); 0: 1
 };
 
 struct ServeStatsC {
@@ -69,6 +70,9 @@ struct ServeStatsC {
   uint64_t peakBytes = 0;
   int64_t readyAtArrival = 0, unserved = 0;
   double seekP50 = 0, seekP99 = 0;
+  int64_t mainRounds = 0, sideRounds = 0, mainFrames = 0;
+  double mainRoundSec = 0, idleSec = 0;  // decode thread: inside main rounds, waiting for work
+  double planSec = 0, launchSec = 0, collectSec = 0;  // inside main rounds: host planning, launches, wait
 };
 
 // Two threads.  The decode thread owns the engine: it keeps every admitted
@@ -90,12 +94,19 @@ class Server {
     ahead_ = std::max(ahead_, lookahead_);
   }
   int init() {
-    int st = eng_.setLookahead(lookahead_);
-    if (st) return st;
-    st = eng_.init();
-    if (st) return st;
-    if (opt_.keyLane && (st = eng_.enableSideLane())) return st;
-    eng_.enableTiming(true);
+    const int n = opt_.lanes > 0 ? std::min(opt_.lanes, 16) : 1;
+    for (int i = 0; i < n; i++) {
+      std::unique_ptr<Lane> L(new (std::nothrow) Lane());
+      if (!L) return kErrDevice;
+      int st = L->eng.setLookahead(lookahead_);
+      if (st) return st;
+      st = L->eng.init();
+      if (st) return st;
+      if (opt_.keyLane && (st = L->eng.enableSideLane())) return st;
+      L->eng.enableTiming(true);
+      L->index = i;
+      lanes_.push_back(std::move(L));
+    }
     return kOK;
   }
 
@@ -129,16 +140,20 @@ class Server {
     t0_ = nowSec();
     {
       std::lock_guard<std::mutex> lk(mu_);
-      admit(true);
+      admit(nullptr, true);
     }
-    std::thread dec([this] { decodeLoop(); });
+    std::vector<std::thread> dec;
+    for (auto& L : lanes_) {
+      Lane* lp = L.get();
+      dec.emplace_back([this, lp] { decodeLoop(*lp); });
+    }
     requestLoop();
     {
       std::lock_guard<std::mutex> lk(mu_);
       stop_ = true;
     }
     cvDecode_.notify_all();
-    dec.join();
+    for (auto& t : dec) t.join();
     ServeStatsC st = st_;
     st.elapsed = endTime_;
     st.waitingAtEnd = (int64_t)waiting_.size();
@@ -160,9 +175,14 @@ class Server {
     st.seekP50 = pctl(seekLat_, 0.5);
     st.seekP99 = pctl(seekLat_, 0.99);
     st.framesPerSec = st.elapsed > 0 ? st.frames / st.elapsed : 0;
-    st.kernelMs = eng_.kernelMillis();
-    st.entropyMs = eng_.entropyMillis();
-    st.reconMs = eng_.reconMillis();
+    for (auto& L : lanes_) {
+      st.planSec += L->eng.planSeconds();
+      st.launchSec += L->eng.launchSeconds();
+      st.collectSec += L->eng.collectSeconds();
+      st.kernelMs += L->eng.kernelMillis();
+      st.entropyMs += L->eng.entropyMillis();
+      st.reconMs += L->eng.reconMillis();
+    }
     *out = st;
     return decodeStatus_;
   }
@@ -201,7 +221,7 @@ class Server {
     bool loop = false, longKey = false;
     uint64_t footprint = 0;
     // shared (mu_)
-    int engineId = -1;
+    int lane = -1, engineId = -1;
     bool admitted = false, done = false, finished = false;
     double startAt = 0;
     uint64_t epoch = 0;       // bumped by a seek
@@ -216,6 +236,18 @@ class Server {
     // decode thread
     uint64_t decEpoch = 0;
     bool inSide = false;
+  };
+
+  // A decode lane: an engine (with its own CUDA streams and side lane), the
+  // streams admitted to it and the thread that drives it.  Lanes run side
+  // by side on the GPU, so a long key frame holds up only its own lane's
+  // side round and its rounds only its own streams.
+  struct Lane {
+    Engine eng;
+    int index = 0;
+    std::vector<int> admitted;  // spec indices
+    std::vector<int> specOf;    // engine stream id -> spec index
+    std::vector<std::pair<int, uint64_t>> sidePlanned;
   };
 
   int ringOf() const { return std::max(opt_.ring, ahead_ + 2); }
@@ -254,42 +286,46 @@ class Server {
   bool isKey(const Spec& sp, int64_t i) const { return std::binary_search(sp.keys.begin(), sp.keys.end(), i); }
   double now() const { return nowSec() - t0_; }
 
-  // Admits waiting streams while their footprints fit (decode thread, or
-  // before it starts; mu_ held).
-  void admit(bool initial) {
+  // Admits waiting streams while their footprints fit (mu_ held): into
+  // `only` (a lane whose stream finished), or round-robin over the lanes at
+  // start.
+  void admit(Lane* only, bool initial) {
     while (!waiting_.empty() && used_ + specs_[(size_t)waiting_.front()]->footprint <= opt_.hbmBudget) {
       const int si = waiting_.front();
       Spec& sp = *specs_[(size_t)si];
+      Lane& L = only ? *only : *lanes_[(size_t)(nextLane_++ % lanes_.size())];
       std::vector<const uint8_t*> ptrs;
       std::vector<size_t> lens;
       for (auto& p : sp.pkts) {
         ptrs.push_back(p.data());
         lens.push_back(p.size());
       }
-      if (eng_.addResidentStream(ptrs.data(), lens.data(), (int)ptrs.size(), ringOf(), &sp.engineId)) break;
+      if (L.eng.addResidentStream(ptrs.data(), lens.data(), (int)ptrs.size(), ringOf(), &sp.engineId)) break;
       waiting_.pop_front();
-      if ((int)specOf_.size() <= sp.engineId) specOf_.resize((size_t)sp.engineId + 1, -1);
-      specOf_[(size_t)sp.engineId] = si;
+      sp.lane = L.index;
+      if ((int)L.specOf.size() <= sp.engineId) L.specOf.resize((size_t)sp.engineId + 1, -1);
+      L.specOf[(size_t)sp.engineId] = si;
       sp.startAt = now();
       if (initial && opt_.startSpread > 0)
         sp.startAt += std::uniform_real_distribution<double>(0, opt_.startSpread)(rng_);
       sp.admitted = true;
       used_ += sp.footprint;
-      admitted_.push_back(si);
+      L.admitted.push_back(si);
+      admittedCount_++;
       st_.admittedTotal++;
-      st_.admittedPeak = std::max<int64_t>(st_.admittedPeak, (int64_t)admitted_.size());
+      st_.admittedPeak = std::max<int64_t>(st_.admittedPeak, admittedCount_);
       st_.peakBytes = std::max<uint64_t>(st_.peakBytes, used_);
     }
   }
 
   // Publishes a round's results (mu_ held): frames of a stream's current
   // epoch join its ready list; the rest are dropped.
-  void publish(const std::vector<RoundResult>& rs, const std::vector<uint64_t>& hashes,
+  void publish(const Lane& L, const std::vector<RoundResult>& rs, const std::vector<uint64_t>& hashes,
                const std::vector<std::pair<int, uint64_t>>& planned) {
     const double t = now();
     for (size_t i = 0; i < rs.size(); i++) {
       const RoundResult& r = rs[i];
-      const int si = r.stream >= 0 && r.stream < (int)specOf_.size() ? specOf_[(size_t)r.stream] : -1;
+      const int si = r.stream >= 0 && r.stream < (int)L.specOf.size() ? L.specOf[(size_t)r.stream] : -1;
       if (si < 0) continue;
       Spec& sp = *specs_[(size_t)si];
       uint64_t ep = ~0ull;
@@ -310,7 +346,7 @@ class Server {
     }
   }
 
-  void hashResults(const std::vector<RoundResult>& rs, std::vector<uint64_t>* out) {
+  void hashResults(Lane& L, const std::vector<RoundResult>& rs, std::vector<uint64_t>* out) {
     out->assign(rs.size(), 0);
     if (!opt_.record) return;
     std::vector<uint8_t> buf;
@@ -319,15 +355,14 @@ class Server {
       if (r.status != kOK) continue;
       const int cw = (r.view.width + 1) / 2, ch = (r.view.height + 1) / 2;
       buf.resize((size_t)r.view.width * r.view.height + 2 * (size_t)cw * ch);
-      if (eng_.downloadFrame(r.view, buf.data(), buf.size()) == kOK) (*out)[i] = fnv1a(buf.data(), buf.size());
+      if (L.eng.downloadFrame(r.view, buf.data(), buf.size()) == kOK) (*out)[i] = fnv1a(buf.data(), buf.size());
     }
   }
 
-  void decodeLoop() {
+  void decodeLoop(Lane& L) {
     cudaSetDevice(device_);
     std::vector<RoundResult> res;
     std::vector<uint64_t> hashes;
-    std::vector<std::pair<int, uint64_t>> sidePlanned;
     for (;;) {
       std::vector<int> ids, counts, kids, kcap, reposition;
       std::vector<int64_t> repoTo;
@@ -337,20 +372,21 @@ class Server {
         if (stop_) break;
         // Finished streams leave; waiting ones come in.
         bool removed = false;
-        for (size_t k = 0; k < admitted_.size();) {
-          Spec& sp = *specs_[(size_t)admitted_[k]];
+        for (size_t k = 0; k < L.admitted.size();) {
+          Spec& sp = *specs_[(size_t)L.admitted[k]];
           if (sp.finished && !sp.inSide) {
-            eng_.removeStream(sp.engineId);
+            L.eng.removeStream(sp.engineId);
             used_ -= sp.footprint;
             sp.done = true;
-            admitted_.erase(admitted_.begin() + (long)k);
+            L.admitted.erase(L.admitted.begin() + (long)k);
+            admittedCount_--;
             removed = true;
           } else {
             k++;
           }
         }
-        if (removed) admit(false);
-        for (int si : admitted_) {
+        if (removed) admit(&L, false);
+        for (int si : L.admitted) {
           Spec& sp = *specs_[(size_t)si];
           if (sp.inSide || sp.finished) continue;
           if (sp.decEpoch != sp.epoch) {  // a seek: restart at its key frame
@@ -361,7 +397,7 @@ class Server {
           }
           const int room = ahead_ - (int)sp.ready.size() - sp.inflight;
           if (room <= 0) continue;
-          int64_t pos = (int64_t)sp.pkts.size() - eng_.remaining(sp.engineId);
+          int64_t pos = (int64_t)sp.pkts.size() - L.eng.remaining(sp.engineId);
           if (pos >= (int64_t)sp.pkts.size()) {
             if (!sp.loop) continue;
             reposition.push_back(sp.engineId);  // looping: on from the first frame
@@ -370,12 +406,12 @@ class Server {
             continue;
           }
           if (sp.longKey && isKey(sp, pos)) {
-            if (!eng_.sideBusy() && kids.size() < 64) {
+            if (!L.eng.sideBusy() && kids.size() < 64) {
               kids.push_back(sp.engineId);
               kcap.push_back(1);
               sp.inSide = true;
               sp.inflight = 1;
-              sidePlanned.push_back({si, sp.epoch});
+              L.sidePlanned.push_back({si, sp.epoch});
             }
             continue;
           }
@@ -390,13 +426,15 @@ class Server {
           sp.inflight = n;
           planned.push_back({si, sp.epoch});
         }
-        if (ids.empty() && kids.empty() && reposition.empty() && !eng_.sideBusy()) {
+        if (ids.empty() && kids.empty() && reposition.empty() && !L.eng.sideBusy()) {
+          const double w0 = nowSec();
           cvDecode_.wait_for(lk, std::chrono::microseconds(500));
+          st_.idleSec += nowSec() - w0;
           continue;
         }
       }
-      for (size_t k = 0; k < reposition.size(); k++) eng_.seekStream(reposition[k], repoTo[k]);
-      if (!kids.empty() && eng_.launchSide(kids, &kcap)) {
+      for (size_t k = 0; k < reposition.size(); k++) L.eng.seekStream(reposition[k], repoTo[k]);
+      if (!kids.empty() && L.eng.launchSide(kids, &kcap)) {
         std::lock_guard<std::mutex> lk(mu_);
         decodeStatus_ = kErrDevice;
         stop_ = true;
@@ -405,36 +443,43 @@ class Server {
       }
       if (!ids.empty()) {
         res.clear();
-        if (eng_.roundFor(ids, &res, &counts) < 0) {
+        const double r0 = nowSec();
+        const int rc = L.eng.roundFor(ids, &res, &counts);
+        const double r1 = nowSec();
+        if (rc < 0) {
           std::lock_guard<std::mutex> lk(mu_);
           decodeStatus_ = kErrDevice;
           stop_ = true;
           cvRequest_.notify_all();
           break;
         }
-        hashResults(res, &hashes);
+        hashResults(L, res, &hashes);
         std::lock_guard<std::mutex> lk(mu_);
         st_.rounds++;
-        publish(res, hashes, planned);
+        st_.mainRounds++;
+        st_.mainFrames += (int64_t)res.size();
+        st_.mainRoundSec += r1 - r0;
+        publish(L, res, hashes, planned);
         cvRequest_.notify_all();
-      } else if (eng_.sideBusy() && !eng_.sideReady()) {
+      } else if (L.eng.sideBusy() && !L.eng.sideReady()) {
         std::this_thread::sleep_for(std::chrono::microseconds(100));
       }
-      if (eng_.sideBusy() && eng_.sideReady()) {
+      if (L.eng.sideBusy() && L.eng.sideReady()) {
         res.clear();
-        eng_.collectSide(&res);
-        hashResults(res, &hashes);
+        L.eng.collectSide(&res);
+        hashResults(L, res, &hashes);
         std::lock_guard<std::mutex> lk(mu_);
         st_.rounds++;
-        publish(res, hashes, sidePlanned);
-        for (const auto& pl : sidePlanned) specs_[(size_t)pl.first]->inSide = false;
-        sidePlanned.clear();
+        st_.sideRounds++;
+        publish(L, res, hashes, L.sidePlanned);
+        for (const auto& pl : L.sidePlanned) specs_[(size_t)pl.first]->inSide = false;
+        L.sidePlanned.clear();
         cvRequest_.notify_all();
       }
     }
-    if (eng_.sideBusy()) {
+    if (L.eng.sideBusy()) {
       res.clear();
-      eng_.collectSide(&res);
+      L.eng.collectSide(&res);
     }
   }
 
@@ -489,7 +534,7 @@ class Server {
       if (stop_) break;
       const double t = now();
       double nextT = 1e30;
-      bool live = !waiting_.empty() && (!admitted_.empty() || t <= opt_.duration);
+      bool live = !waiting_.empty() && (admittedCount_ > 0 || t <= opt_.duration);
       for (size_t si = 0; si < specs_.size(); si++) {
         Spec& sp = *specs_[si];
         if (!sp.admitted || sp.done || sp.finished) continue;
@@ -526,14 +571,14 @@ class Server {
 
   ServeOptionsC opt_;
   int lookahead_ = 1, ahead_ = 2;
-  Engine eng_;
+  std::vector<std::unique_ptr<Lane>> lanes_;
   std::mt19937_64 rng_;
   std::vector<std::unique_ptr<Spec>> specs_;
   std::mutex mu_;
   std::condition_variable cvDecode_, cvRequest_;
   std::deque<int> waiting_;
-  std::vector<int> admitted_;
-  std::vector<int> specOf_;  // engine stream id -> spec index
+  int64_t admittedCount_ = 0;
+  size_t nextLane_ = 0;
   uint64_t used_ = 0;
   bool stop_ = false;
   int decodeStatus_ = kOK;
@@ -571,6 +616,7 @@ int ebivgpu_server_create(const ebivgpu_serve_options* o, ebivgpu_server** out) 
   c.keyLane = o->key_lane;
   c.startSpread = o->start_spread_s > 0 ? o->start_spread_s : 0;
   c.decodeAhead = o->decode_ahead > 0 ? o->decode_ahead : 0;
+  c.lanes = o->decode_lanes > 0 ? o->decode_lanes : 0;
   ebivgpu_server* h = new (std::nothrow) ebivgpu_server();
   if (!h) return kErrDevice;
   h->s.reset(new Server(c));
@@ -617,6 +663,14 @@ int ebivgpu_server_run(ebivgpu_server* h, ebivgpu_serve_stats* out) {
   out->unserved = st.unserved;
   out->seek_latency_p50_ms = st.seekP50;
   out->seek_latency_p99_ms = st.seekP99;
+  out->main_rounds = st.mainRounds;
+  out->side_rounds = st.sideRounds;
+  out->main_frames = st.mainFrames;
+  out->main_round_s = st.mainRoundSec;
+  out->idle_s = st.idleSec;
+  out->plan_s = st.planSec;
+  out->launch_s = st.launchSec;
+  out->collect_s = st.collectSec;
   return r;
 }
 

@@ -173,7 +173,8 @@ uint64_t ebivgpu_stream_footprint(int width, int height, int ring, int lookahead
  * issues requests as a Poisson process at its frame rate; a decode thread
  * keeps every admitted stream up to decode_ahead frames ahead of its
  * requests, all streams' next frames (max_frames_per_round each) in shared
- * rounds, key frames with long entropy chains on a side lane; requests are
+ * rounds, key frames with long entropy chains on a side lane; decode_lanes
+ * such threads, each with its own engine, split the streams; requests are
  * served in order as their frames are ready (latency: arrival to hand-out,
  * zero wait when the frame was decoded before it was asked for); seeks go
  * to key frames (frames decoded for the old position are dropped), looping
@@ -194,6 +195,7 @@ typedef struct {
   int32_t key_lane;            /* key frames decode on a side lane beside the main rounds (1 = on) */
   double start_spread_s;       /* streams admitted at start begin uniformly within this many seconds */
   int32_t decode_ahead;        /* frames decoded ahead of each stream's requests (0: twice max_frames_per_round) */
+  int32_t decode_lanes;        /* engines decoding side by side, each with its own thread and side lane (0: 1) */
 } ebivgpu_serve_options;
 typedef struct {
   int64_t requests, frames, errors, seeks, loops, rounds;
@@ -205,6 +207,9 @@ typedef struct {
   int64_t ready_at_arrival;    /* requests whose frame was decoded before they arrived */
   int64_t unserved;            /* requests past the end of a clip that does not loop */
   double seek_latency_p50_ms, seek_latency_p99_ms; /* requests that were seeks */
+  int64_t main_rounds, side_rounds, main_frames;    /* rounds of the decode thread, frames of main rounds */
+  double main_round_s, idle_s;  /* decode threads: time inside main rounds, time with nothing to decode */
+  double plan_s, launch_s, collect_s; /* main rounds: host planning, launches, waiting for the GPU */
 } ebivgpu_serve_stats;
 int ebivgpu_server_create(const ebivgpu_serve_options* o, ebivgpu_server** out);
 int ebivgpu_server_add_stream(ebivgpu_server* s, const uint8_t* const* pkts, const size_t* lens, int n, double fps,

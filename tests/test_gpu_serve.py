@@ -21,10 +21,11 @@ def _streams():
     return out
 
 
-def test_mix_equals_alone_with_seeks_and_loops(gpu_required):
+@pytest.mark.parametrize("lanes", [1, 3])
+def test_mix_equals_alone_with_seeks_and_loops(gpu_required, lanes):
     streams = _streams()
     srv = ebiv.Server(duration_s=1.5, frames_per_stream=40, seek_prob=0.1, seed=3, record=True,
-                      max_frames_per_round=3)
+                      max_frames_per_round=3, decode_lanes=lanes)
     for i, (pk, w, h) in enumerate(streams):
         srv.add_stream(pk, fps=60 if i % 2 else 30, loop=(i % 3 == 0))
     st = srv.run()
