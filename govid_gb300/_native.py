@@ -37,7 +37,8 @@ class ServeOptions(C.Structure):
     _fields_ = [("duration_s", C.c_double), ("frames_per_stream", C.c_int64), ("seek_prob", C.c_double),
                 ("seed", C.c_uint64), ("hbm_budget_bytes", C.c_uint64), ("max_frames_per_round", C.c_int32),
                 ("ring", C.c_int32), ("record", C.c_int32), ("key_lane", C.c_int32),
-                ("start_spread_s", C.c_double), ("decode_ahead", C.c_int32), ("decode_lanes", C.c_int32)]
+                ("start_spread_s", C.c_double), ("decode_ahead", C.c_int32), ("decode_lanes", C.c_int32),
+                ("long_key_mbs", C.c_int32)]
 
 
 class ServeStats(C.Structure):
@@ -129,6 +130,7 @@ def lib() -> C.CDLL:
     _sig(L, "ebivgpu_stream_footprint", C.c_uint64, I, I, I, I)
     # serving
     _sig(L, "ebivgpu_server_create", I, C.POINTER(ServeOptions), PP)
+    _sig(L, "ebivgpu_server_stream_footprint", C.c_uint64, C.POINTER(ServeOptions), I, I, C.c_uint64)
     _sig(L, "ebivgpu_server_add_stream", I, P, C.POINTER(C.c_char_p), C.POINTER(S), I, C.c_double, I)
     _sig(L, "ebivgpu_server_run", I, P, C.POINTER(ServeStats))
     _sig(L, "ebivgpu_server_frame_hashes", I64, P, C.POINTER(C.c_int32), C.POINTER(I64), C.POINTER(C.c_uint64), I64)

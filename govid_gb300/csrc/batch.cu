@@ -203,8 +203,10 @@ Engine::~Engine() {
   if (stream_) cudaStreamSynchronize(stream_);
   for (auto& s : streams_)
     if (s) s->release();
-  if (streamES_) cudaStreamSynchronize(streamES_);
-  if (streamRS_) cudaStreamSynchronize(streamRS_);
+  for (int l = 0; l < kSideLanes; l++) {
+    if (streamES_[l]) cudaStreamSynchronize(streamES_[l]);
+    if (streamRS_[l]) cudaStreamSynchronize(streamRS_[l]);
+  }
   for (int p = 0; p < kParities; p++) {
     if (dStage_[p]) cudaFree(dStage_[p]);
     if (hStage_[p]) cudaFreeHost(hStage_[p]);
@@ -213,7 +215,8 @@ Engine::~Engine() {
       if (e) cudaEventDestroy(e);
   }
   if (dOne_) cudaFree(dOne_);
-  if (sideDone_) cudaEventDestroy(sideDone_);
+  for (auto& e : sideDone_)
+    if (e) cudaEventDestroy(e);
   if (streamC_) {
     cudaStreamSynchronize(streamC_);
     cudaStreamDestroy(streamC_);
@@ -242,8 +245,10 @@ Engine::~Engine() {
     for (auto& e : evGroup_[p])
       if (e) cudaEventDestroy(e);
   }
-  if (streamES_) cudaStreamDestroy(streamES_);
-  if (streamRS_) cudaStreamDestroy(streamRS_);
+  for (int l = 0; l < kSideLanes; l++) {
+    if (streamES_[l]) cudaStreamDestroy(streamES_[l]);
+    if (streamRS_[l]) cudaStreamDestroy(streamRS_[l]);
+  }
   if (ownStreamE_ && streamE_) cudaStreamDestroy(streamE_);
   if (ownStream_ && stream_) cudaStreamDestroy(stream_);
 }
@@ -292,15 +297,16 @@ int Engine::setLookahead(int k) {
 // references, and the buffers a round claims; a pipelined engine of depth D
 // holds D more rounds' worth of claims.
 int Engine::poolSize(int ring, int k, int depth, bool side) {
-  return ring + (2 + depth) * k + 3 + depth + (side ? k + 1 : 0);
+  return ring + (2 + depth) * k + 3 + depth + (side ? 2 : 0);  // a stream is in one side round at a time
 }
 
-size_t Engine::footprint(int w, int h, int ring, int lookahead, int depth, bool side) {
+size_t Engine::footprint(int w, int h, int ring, int lookahead, int depth, int sideLanes) {
+  const bool side = sideLanes > 0;
   const Geometry g = Geometry::of(w, h);
   const size_t yb = (size_t)stride64(g.padW()) * g.padH(), cb = (size_t)stride64(g.padCW()) * g.padCH();
   const size_t mbs = (size_t)g.mbCols * g.mbRows;
   return (size_t)poolSize(ring, lookahead, depth, side) * (yb + 2 * cb) +
-         (size_t)(depth + 1 + (side ? 1 : 0)) * (lookahead + 1) * Slot::bytes(mbs);
+         ((size_t)(depth + 1) * (lookahead + 1) + 2 * (size_t)(side ? sideLanes : 0)) * Slot::bytes(mbs);
 }
 
 int Engine::addResidentStream(const uint8_t* const* pkts, const size_t* lens, int n, int ring, int* id) {
@@ -460,8 +466,10 @@ int Engine::setActive(int id, bool active) {
 int Engine::removeStream(int id) {
   if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) return kErrArg;
   if (streamE_) cudaStreamSynchronize(streamE_);
-  if (streamES_) cudaStreamSynchronize(streamES_);
-  if (streamRS_) cudaStreamSynchronize(streamRS_);
+  for (int l = 0; l < kSideLanes; l++) {
+    if (streamES_[l]) cudaStreamSynchronize(streamES_[l]);
+    if (streamRS_[l]) cudaStreamSynchronize(streamRS_[l]);
+  }
   cudaStreamSynchronize(stream_);
   deviceBytes_ -= streams_[(size_t)id]->bytes;
   streams_[(size_t)id]->release();
@@ -497,11 +505,16 @@ int Engine::configure(Stream& s, int w, int h) {
   // and the override slot.
   const int perParity = lookahead_ + 1;
   s.slots.resize((size_t)slotSets() * perParity);
+  size_t nSlots = 0;
   for (size_t i = 0; i < s.slots.size(); i++) {
     const int within = (int)(i % (size_t)perParity);
-    if ((within < k || within == perParity - 1) && !s.slots[i].alloc(s.mbs)) return kErrDevice;
+    const bool sideSet = (int)(i / (size_t)perParity) >= mainSets();
+    if (within < (sideSet ? 1 : k) || within == perParity - 1) {
+      if (!s.slots[i].alloc(s.mbs)) return kErrDevice;
+      nSlots++;
+    }
   }
-  const size_t b = (size_t)P * s.bufBytes + (size_t)slotSets() * (k + 1) * Slot::bytes(s.mbs);
+  const size_t b = (size_t)P * s.bufBytes + nSlots * Slot::bytes(s.mbs);
   s.bytes += b;
   deviceBytes_ += b;
   s.ready = true;
@@ -708,7 +721,7 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
     Stream& s = *streams_[(size_t)id];
     // A stream in the side lane stays out of main rounds; the side lane takes
     // only streams with no round in flight.
-    if (P == kSide ? (s.inSide || s.hasProv) : s.inSide) continue;
+    if (isSide(P) ? (s.inSide || s.hasProv) : s.inSide) continue;
     std::vector<int> chain;
     std::vector<char> busy;
     // Start from the provisional references after the stream's in-flight
@@ -777,7 +790,7 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
       s.pGolden = provGolden;
       s.hasProv = true;
       s.lastRound = R.id;
-      if (P == kSide) s.inSide = true;
+      if (isSide(P)) s.inSide = true;
     }
   }
   // Raw frames: scatter the packed planes into their pool buffer (engine
@@ -842,7 +855,7 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
   // reconstruction waits only for its own group: the long chains of a large
   // frame late in the round do not hold back the steps before it.
   const int nsteps = (int)R.steps.size();
-  R.groups = (P != kSide && pipeDepth_ && streamEG_[0] && nsteps > 1) ? std::min(entropyGroups_, nsteps) : 1;
+  R.groups = (!isSide(P) && pipeDepth_ && streamEG_[0] && nsteps > 1) ? std::min(entropyGroups_, nsteps) : 1;
   R.stepsPerGroup = (nsteps + R.groups - 1) / R.groups;
   R.groups = (nsteps + R.stepsPerGroup - 1) / R.stepsPerGroup;
   R.oDesc = 0;
@@ -1053,7 +1066,7 @@ int Engine::launchRecon(Round& R) {
   // for step s's inter pixels (event A) and step s+1's phase 1 waits for it
   // (event B).
   const int nsteps = (int)R.steps.size();
-  const bool split = P != kSide && streamB_ && nsteps > 1 && nsteps <= kMaxSteps;
+  const bool split = !isSide(P) && streamB_ && nsteps > 1 && nsteps <= kMaxSteps;
   for (int st = 0; st < nsteps; st++) {
     const StepInfo& si = R.steps[(size_t)st];
     if (grouped && st / R.stepsPerGroup != groupA) {
@@ -1136,7 +1149,7 @@ int Engine::collectRound(Round& R, std::vector<RoundResult>* results) {
     if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) continue;  // removed meanwhile
     Stream& s = *streams_[(size_t)id];
     s.roundBufs[P].clear();
-    if (P == kSide) s.inSide = false;
+    if (isSide(P)) s.inSide = false;
     if (R.jobs[(size_t)chain[0]].epoch != s.epoch) continue;  // planned before a rollback: discarded
     // A newer round of this stream was planned on top of this chain's
     // outcome; commit this chain as if it were the newest.
@@ -1270,36 +1283,59 @@ int Engine::decodeInto(int id, uint8_t* y, int ys, uint8_t* cb, uint8_t* cr, int
   return collectRound(R, results);
 }
 
-int Engine::enableSideLane() {
+int Engine::enableSideLane(int lanes) {
   for (auto& s : streams_)
     if (s) return kErrArg;  // pool and slot counts depend on it
-  if (!streamES_ && cudaStreamCreateWithFlags(&streamES_, cudaStreamNonBlocking) != cudaSuccess) return kErrDevice;
-  if (!streamRS_ && cudaStreamCreateWithFlags(&streamRS_, cudaStreamNonBlocking) != cudaSuccess) return kErrDevice;
-  if (!sideDone_ && cudaEventCreateWithFlags(&sideDone_, cudaEventDisableTiming) != cudaSuccess) return kErrDevice;
+  if (lanes < 1 || lanes > kSideLanes) return kErrArg;
+  sideLanes_ = lanes;
+  for (int l = 0; l < lanes; l++) {
+    if (!streamES_[l] && cudaStreamCreateWithFlags(&streamES_[l], cudaStreamNonBlocking) != cudaSuccess)
+      return kErrDevice;
+    if (!streamRS_[l] && cudaStreamCreateWithFlags(&streamRS_[l], cudaStreamNonBlocking) != cudaSuccess)
+      return kErrDevice;
+    if (!sideDone_[l] && cudaEventCreateWithFlags(&sideDone_[l], cudaEventDisableTiming) != cudaSuccess)
+      return kErrDevice;
+  }
   side_ = true;
   return kOK;
 }
 
-int Engine::launchSide(const std::vector<int>& ids, const std::vector<int>* maxFrames) {
-  if (!side_ || sideInflight_) return kErrArg;
-  Round& R = rounds_[kSide];
-  R.parity = kSide;
-  if (planRound(ids, maxFrames, R) || launchRecon(R)) {
+int Engine::freeSideLane() const {
+  if (!side_) return -1;
+  for (int l = 0; l < sideLanes_; l++)
+    if (!sideInflight_[l]) return l;
+  return -1;
+}
+
+bool Engine::anySideBusy() const {
+  for (bool b : sideInflight_)
+    if (b) return true;
+  return false;
+}
+
+int Engine::launchSide(int lane, const std::vector<int>& ids) {
+  if (!side_ || lane < 0 || lane >= sideLanes_ || sideInflight_[lane]) return kErrArg;
+  Round& R = rounds_[kSide + lane];
+  R.parity = kSide + lane;
+  const std::vector<int> one(ids.size(), 1);  // one frame per stream: the lane's slot set holds one
+  if (planRound(ids, &one, R) || launchRecon(R)) {
     for (Job& j : R.jobs)
       if (j.status == kOK) j.status = kErrDevice;
     R.nDesc = 0;
   }
-  if (cudaEventRecord(sideDone_, streamRS_) != cudaSuccess) return kErrDevice;
-  sideInflight_ = true;
+  if (cudaEventRecord(sideDone_[lane], streamRS_[lane]) != cudaSuccess) return kErrDevice;
+  sideInflight_[lane] = true;
   return kOK;
 }
 
-bool Engine::sideReady() { return sideInflight_ && cudaEventQuery(sideDone_) != cudaErrorNotReady; }
+bool Engine::sideReady(int lane) {
+  return sideBusy(lane) && cudaEventQuery(sideDone_[lane]) != cudaErrorNotReady;
+}
 
-int Engine::collectSide(std::vector<RoundResult>* results) {
-  if (!sideInflight_) return 0;
-  const int n = collectRound(rounds_[kSide], results);
-  sideInflight_ = false;
+int Engine::collectSide(int lane, std::vector<RoundResult>* results) {
+  if (!sideBusy(lane)) return 0;
+  const int n = collectRound(rounds_[kSide + lane], results);
+  sideInflight_[lane] = false;
   return n;
 }
 

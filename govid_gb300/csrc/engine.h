@@ -118,16 +118,21 @@ class Engine {
   bool pipelined() const { return pipeDepth_ > 0; }
   int pipeDepth() const { return pipeDepth_; }
   int drain(std::vector<RoundResult>* results);
-  // Side lane (set before adding streams): a round for a few streams (the
-  // serving loop sends key frames there) that runs on its own pair of CUDA
-  // streams next to the main rounds and is collected when it is done.  A
-  // stream in the side lane is left out of main rounds until collected; the
-  // caller sends a stream to it only between its main rounds.
-  int enableSideLane();
-  int launchSide(const std::vector<int>& ids, const std::vector<int>* maxFrames);
-  bool sideBusy() const { return sideInflight_; }
-  bool sideReady();  // the side round's work is complete
-  int collectSide(std::vector<RoundResult>* results);
+  // Side lanes (enabled before adding streams): rounds of one frame for each
+  // of a few streams (the serving loop sends key frames with long entropy
+  // chains there), each lane on its own pair of CUDA streams next to the
+  // main rounds and the other lanes, collected when done.  A stream in a
+  // side round is left out of main rounds until collected; the caller sends
+  // a stream to a side lane only between its main rounds.
+  static constexpr int kSideLanes = 4;
+  int enableSideLane(int lanes = 1);  // 1 to kSideLanes
+  int sideLanes() const { return sideLanes_; }
+  int freeSideLane() const;  // a lane with no round in flight, or -1
+  int launchSide(int lane, const std::vector<int>& ids);
+  bool sideBusy(int lane) const { return lane >= 0 && lane < kSideLanes && sideInflight_[lane]; }
+  bool anySideBusy() const;
+  bool sideReady(int lane);  // the lane's round is complete
+  int collectSide(int lane, std::vector<RoundResult>* results);
 
   int downloadFrame(const EngineFrameView& v, uint8_t* packed, size_t cap);
   // Queues the copy on the engine's copy stream, beside the reconstruction;
@@ -147,7 +152,7 @@ class Engine {
   int64_t launches() const { return launches_; }
   size_t deviceBytes() const { return deviceBytes_; }
   // Per-stream HBM footprint (pool + scratch) for a geometry.
-  static size_t footprint(int w, int h, int ring, int lookahead, int depth = 0, bool side = false);
+  static size_t footprint(int w, int h, int ring, int lookahead, int depth = 0, int sideLanes = 0);
   static int poolSize(int ring, int lookahead, int depth, bool side = false);
 
   // Kernel-time accounting: CUDA events recorded around each round's
@@ -178,23 +183,26 @@ class Engine {
   int launchRecon(Round& r);
   int collectRound(Round& r, std::vector<RoundResult>* results);
   // Streams of a round by parity: 0/1 main (pipelined rounds alternate), 2 side.
+  static bool isSide(int parity) { return parity >= kSide; }
   cudaStream_t entropyStream(int parity = 0) const {
-    return parity == kSide ? streamES_ : (pipeDepth_ ? streamE_ : stream_);
+    return isSide(parity) ? streamES_[parity - kSide] : (pipeDepth_ ? streamE_ : stream_);
   }
-  cudaStream_t reconStream(int parity = 0) const { return parity == kSide ? streamRS_ : stream_; }
+  cudaStream_t reconStream(int parity = 0) const { return isSide(parity) ? streamRS_[parity - kSide] : stream_; }
   int mainSets() const { return pipeDepth_ + 1; }
-  int slotSet(int parity) const { return parity == kSide ? mainSets() : parity; }
-  int slotSets() const { return mainSets() + (side_ ? 1 : 0); }
+  // Slot sets: one per main parity in use (lookahead + 1 slots), then one
+  // per side lane (a frame slot and the override slot).
+  int slotSet(int parity) const { return isSide(parity) ? mainSets() + (parity - kSide) : parity; }
+  int slotSets() const { return mainSets() + (side_ ? sideLanes_ : 0); }
   static constexpr int kMaxDepth = 3;
   static constexpr int kMainParities = kMaxDepth + 1;  // main rounds in flight at most
-  static constexpr int kSide = kMainParities;
-  static constexpr int kParities = kMainParities + 1;
+  static constexpr int kSide = kMainParities;           // parities kSide.. are the side lanes
+  static constexpr int kParities = kMainParities + kSideLanes;
 
   cudaStream_t stream_ = nullptr;   // reconstruction, copies, status read-back
   cudaStream_t streamE_ = nullptr;  // entropy stage of pipelined rounds
-  cudaStream_t streamES_ = nullptr, streamRS_ = nullptr;  // side lane: entropy, reconstruction
+  cudaStream_t streamES_[kSideLanes] = {}, streamRS_[kSideLanes] = {};  // side lanes: entropy, reconstruction
   cudaStream_t planStream_ = nullptr;  // reconstruction stream of the round being planned
-  cudaEvent_t sideDone_ = nullptr;
+  cudaEvent_t sideDone_[kSideLanes] = {};
   // Copy stream of downloadFrameAsync and the event after its last copy.
   cudaStream_t streamC_ = nullptr;
   cudaEvent_t copyDone_ = nullptr;
@@ -219,7 +227,9 @@ class Engine {
   cudaEvent_t stepB_[kMainParities][kMaxSteps] = {};
   bool ownStream_ = false, ownStreamE_ = false;
   int pipeDepth_ = 0;
-  bool side_ = false, sideInflight_ = false;
+  bool side_ = false;
+  int sideLanes_ = 0;
+  bool sideInflight_[kSideLanes] = {};
   std::vector<std::unique_ptr<Stream>> streams_;
   std::unique_ptr<Round[]> rounds_;  // by parity
   std::vector<int> pipe_;  // parities of the main rounds in flight, oldest first

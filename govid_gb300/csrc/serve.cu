@@ -56,10 +56,11 @@ struct ServeOptionsC {
   int maxFramesPerRound = 4;  // frames of one stream per round (the engine's lookahead)
   int ring = 3;
   int record = 0;
-  int keyLane = 1;  // long key frames decode on the engine's side lane
+  int keyLane = 1;  // side lanes for long key frames (0: none; at most Engine::kSideLanes)
   double startSpread = 0;  // streams admitted at start begin at a uniform offset in [0, startSpread) s
   int decodeAhead = 0;     // frames decoded ahead of each stream's requests (0: twice the lookahead)
   int lanes = 0;           // decode lanes (engines with their own thread and side lane); 0: 1
+  int longKeyMBs = 0;      // key frames whose largest tile has more macroblocks go to a side lane (0: 1500)
 };
 
 struct ServeStatsC {
@@ -102,7 +103,7 @@ class Server {
       if (st) return st;
       st = L->eng.init();
       if (st) return st;
-      if (opt_.keyLane && (st = L->eng.enableSideLane())) return st;
+      if (opt_.keyLane && (st = L->eng.enableSideLane(sideLanes()))) return st;
       L->eng.enableTiming(true);
       L->index = i;
       lanes_.push_back(std::move(L));
@@ -125,10 +126,10 @@ class Server {
       if (parseFrameHeader(sp->pkts[(size_t)i].data(), sp->pkts[(size_t)i].size(), &f) == kOK && f.type == kFrameKey)
         sp->keys.push_back(i);
     }
-    sp->longKey = opt_.keyLane && maxTileMBs(sp->pkts[0], fh) > kLongKeyMBs;
+    sp->longKey = opt_.keyLane && maxTileMBs(sp->pkts[0], fh) > (opt_.longKeyMBs > 0 ? opt_.longKeyMBs : kLongKeyMBs);
     sp->fps = fps;
     sp->loop = loop;
-    sp->footprint = Engine::footprint(sp->w, sp->h, ringOf(), lookahead_, 0, opt_.keyLane != 0);
+    sp->footprint = Engine::footprint(sp->w, sp->h, ringOf(), lookahead_, 0, sideLanes());
     for (auto& p : sp->pkts) sp->footprint += (p.size() + 15) / 16 * 16;
     specs_.push_back(std::move(sp));
     return kOK;
@@ -247,10 +248,11 @@ class Server {
     int index = 0;
     std::vector<int> admitted;  // spec indices
     std::vector<int> specOf;    // engine stream id -> spec index
-    std::vector<std::pair<int, uint64_t>> sidePlanned;
+    std::vector<std::pair<int, uint64_t>> sidePlanned[Engine::kSideLanes];
   };
 
   int ringOf() const { return std::max(opt_.ring, ahead_ + 2); }
+  int sideLanes() const { return opt_.keyLane > 0 ? std::min(opt_.keyLane, Engine::kSideLanes) : 0; }
 
   // The largest tile of a key frame's coded payload: frame header, then the
   // override length when present, qp, tile columns, tile rows
@@ -364,9 +366,10 @@ class Server {
     std::vector<RoundResult> res;
     std::vector<uint64_t> hashes;
     for (;;) {
-      std::vector<int> ids, counts, kids, kcap, reposition;
+      std::vector<int> ids, counts, kids, reposition;
       std::vector<int64_t> repoTo;
       std::vector<std::pair<int, uint64_t>> planned;
+      int sideLane = -1;
       {
         std::unique_lock<std::mutex> lk(mu_);
         if (stop_) break;
@@ -386,6 +389,7 @@ class Server {
           }
         }
         if (removed) admit(&L, false);
+        sideLane = L.eng.freeSideLane();  // the long key frames found now go there
         for (int si : L.admitted) {
           Spec& sp = *specs_[(size_t)si];
           if (sp.inSide || sp.finished) continue;
@@ -406,12 +410,11 @@ class Server {
             continue;
           }
           if (sp.longKey && isKey(sp, pos)) {
-            if (!L.eng.sideBusy() && kids.size() < 64) {
+            if (sideLane >= 0 && kids.size() < 64) {
               kids.push_back(sp.engineId);
-              kcap.push_back(1);
               sp.inSide = true;
               sp.inflight = 1;
-              L.sidePlanned.push_back({si, sp.epoch});
+              L.sidePlanned[sideLane].push_back({si, sp.epoch});
             }
             continue;
           }
@@ -426,7 +429,7 @@ class Server {
           sp.inflight = n;
           planned.push_back({si, sp.epoch});
         }
-        if (ids.empty() && kids.empty() && reposition.empty() && !L.eng.sideBusy()) {
+        if (ids.empty() && kids.empty() && reposition.empty() && !L.eng.anySideBusy()) {
           const double w0 = nowSec();
           cvDecode_.wait_for(lk, std::chrono::microseconds(500));
           st_.idleSec += nowSec() - w0;
@@ -434,7 +437,7 @@ class Server {
         }
       }
       for (size_t k = 0; k < reposition.size(); k++) L.eng.seekStream(reposition[k], repoTo[k]);
-      if (!kids.empty() && L.eng.launchSide(kids, &kcap)) {
+      if (!kids.empty() && L.eng.launchSide(sideLane, kids)) {
         std::lock_guard<std::mutex> lk(mu_);
         decodeStatus_ = kErrDevice;
         stop_ = true;
@@ -461,25 +464,28 @@ class Server {
         st_.mainRoundSec += r1 - r0;
         publish(L, res, hashes, planned);
         cvRequest_.notify_all();
-      } else if (L.eng.sideBusy() && !L.eng.sideReady()) {
-        std::this_thread::sleep_for(std::chrono::microseconds(100));
       }
-      if (L.eng.sideBusy() && L.eng.sideReady()) {
+      bool collected = false;
+      for (int l = 0; l < Engine::kSideLanes; l++) {
+        if (!L.eng.sideReady(l)) continue;
         res.clear();
-        L.eng.collectSide(&res);
+        L.eng.collectSide(l, &res);
         hashResults(L, res, &hashes);
         std::lock_guard<std::mutex> lk(mu_);
         st_.rounds++;
         st_.sideRounds++;
-        publish(L, res, hashes, L.sidePlanned);
-        for (const auto& pl : L.sidePlanned) specs_[(size_t)pl.first]->inSide = false;
-        L.sidePlanned.clear();
+        publish(L, res, hashes, L.sidePlanned[l]);
+        for (const auto& pl : L.sidePlanned[l]) specs_[(size_t)pl.first]->inSide = false;
+        L.sidePlanned[l].clear();
         cvRequest_.notify_all();
+        collected = true;
       }
+      if (ids.empty() && !collected && L.eng.anySideBusy())
+        std::this_thread::sleep_for(std::chrono::microseconds(100));
     }
-    if (L.eng.sideBusy()) {
+    for (int l = 0; l < Engine::kSideLanes; l++) {
       res.clear();
-      L.eng.collectSide(&res);
+      L.eng.collectSide(l, &res);
     }
   }
 
@@ -617,6 +623,7 @@ int ebivgpu_server_create(const ebivgpu_serve_options* o, ebivgpu_server** out) 
   c.startSpread = o->start_spread_s > 0 ? o->start_spread_s : 0;
   c.decodeAhead = o->decode_ahead > 0 ? o->decode_ahead : 0;
   c.lanes = o->decode_lanes > 0 ? o->decode_lanes : 0;
+  c.longKeyMBs = o->long_key_mbs > 0 ? o->long_key_mbs : 0;
   ebivgpu_server* h = new (std::nothrow) ebivgpu_server();
   if (!h) return kErrDevice;
   h->s.reset(new Server(c));
@@ -689,5 +696,14 @@ int64_t ebivgpu_server_frame_hashes(ebivgpu_server* h, int32_t* stream, int64_t*
 void ebivgpu_server_destroy(ebivgpu_server* h) { delete h; }
 
 uint64_t ebivgpu_frame_hash(const uint8_t* packed, size_t n) { return fnv1a(packed, n); }
+
+uint64_t ebivgpu_server_stream_footprint(const ebivgpu_serve_options* o, int width, int height, uint64_t packet_bytes) {
+  if (!o || width <= 0 || height <= 0) return 0;
+  const int lookahead = std::max(1, (int)o->max_frames_per_round);
+  const int ahead = std::max(o->decode_ahead > 0 ? (int)o->decode_ahead : 2 * lookahead, lookahead);
+  const int ring = std::max(o->ring >= 2 ? (int)o->ring : 3, ahead + 2);
+  const int side = o->key_lane > 0 ? std::min((int)o->key_lane, Engine::kSideLanes) : 0;
+  return Engine::footprint(width, height, ring, lookahead, 0, side) + packet_bytes;
+}
 
 }  // extern "C"

@@ -192,10 +192,11 @@ typedef struct {
   int32_t max_frames_per_round;/* per stream, when it fell behind */
   int32_t ring;
   int32_t record;              /* hash every delivered frame (testing) */
-  int32_t key_lane;            /* key frames decode on a side lane beside the main rounds (1 = on) */
+  int32_t key_lane;            /* side lanes for key frames with long entropy chains beside the main rounds (0 = none, 1-4) */
   double start_spread_s;       /* streams admitted at start begin uniformly within this many seconds */
   int32_t decode_ahead;        /* frames decoded ahead of each stream's requests (0: twice max_frames_per_round) */
   int32_t decode_lanes;        /* engines decoding side by side, each with its own thread and side lane (0: 1) */
+  int32_t long_key_mbs;        /* key frames whose largest tile has more macroblocks use the side lanes (0: 1500) */
 } ebivgpu_serve_options;
 typedef struct {
   int64_t requests, frames, errors, seeks, loops, rounds;
@@ -221,6 +222,10 @@ int64_t ebivgpu_server_frame_hashes(ebivgpu_server* s, int32_t* stream, int64_t*
 void ebivgpu_server_destroy(ebivgpu_server* s);
 /* FNV-1a 64 of a buffer (the hash the server records). */
 uint64_t ebivgpu_frame_hash(const uint8_t* packed, size_t n);
+/* The HBM footprint a server with options o admits a stream of this geometry
+ * by: its frame pool and decode slots, plus packet_bytes of resident packets
+ * (each packet rounded up to 16 bytes). */
+uint64_t ebivgpu_server_stream_footprint(const ebivgpu_serve_options* o, int width, int height, uint64_t packet_bytes);
 
 /* ---- Key-frame decode without device allocation ---------------------------
  * No reference counterpart: govid allocates its frame buffers on first use

@@ -21,11 +21,13 @@ def _streams():
     return out
 
 
-@pytest.mark.parametrize("lanes", [1, 3])
-def test_mix_equals_alone_with_seeks_and_loops(gpu_required, lanes):
+@pytest.mark.parametrize("lanes,side,long_key", [(1, 1, 0), (3, 1, 20), (1, 3, 20)])
+def test_mix_equals_alone_with_seeks_and_loops(gpu_required, lanes, side, long_key):
+    # long_key 20: every stream's key frames (tiles of more than 20
+    # macroblocks for most of them) take the side lanes.
     streams = _streams()
     srv = ebiv.Server(duration_s=1.5, frames_per_stream=40, seek_prob=0.1, seed=3, record=True,
-                      max_frames_per_round=3, decode_lanes=lanes)
+                      max_frames_per_round=3, decode_lanes=lanes, key_lane=side, long_key_mbs=long_key)
     for i, (pk, w, h) in enumerate(streams):
         srv.add_stream(pk, fps=60 if i % 2 else 30, loop=(i % 3 == 0))
     st = srv.run()
@@ -43,14 +45,15 @@ def test_admission_respects_hbm_budget(gpu_required):
     # packets (the slack, half a footprint, is far above 16 small packets)
     s0 = _streams()[0]
     streams = [s0] * 4
-    fp = ebiv.stream_footprint(s0[1], s0[2], 3, 2)
-    assert sum(len(p) for p in s0[0]) < fp // 8
+    probe = ebiv.Server(max_frames_per_round=2)
+    fp = probe.stream_footprint(s0[1], s0[2], s0[0])
+    assert fp > ebiv.stream_footprint(s0[1], s0[2], 3, 2)
     srv = ebiv.Server(duration_s=0.6, frames_per_stream=10, seek_prob=0.0, seed=5, hbm_budget_bytes=2 * fp + fp // 2,
                       max_frames_per_round=2)
     for pk, w, h in streams:
         srv.add_stream(pk, fps=60, loop=False)
     st = srv.run()
-    assert st["admitted_peak"] <= 2
+    assert st["admitted_peak"] == 2 and st["peak_bytes"] <= 2 * fp + fp // 2
     assert st["admitted_total"] == 4 and st["errors"] == 0
 
 
@@ -74,7 +77,7 @@ def test_decode_ahead_serves_requests_from_ready_frames(gpu_required):
 
 def test_stream_larger_than_the_budget_is_never_admitted(gpu_required):
     s0 = _streams()[0]
-    srv = ebiv.Server(duration_s=0.3, frames_per_stream=10, seed=2, hbm_budget_bytes=1 << 20,
+    srv = ebiv.Server(duration_s=0.3, frames_per_stream=10, seed=2, hbm_budget_bytes=64 << 10,
                       max_frames_per_round=2)
     srv.add_stream(s0[0], fps=60)
     st = srv.run()
