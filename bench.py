@@ -805,7 +805,8 @@ def run_serve(args):
         srv = ebiv.Server(duration_s=seconds, frames_per_stream=args.serve_frames, seek_prob=0.05,
                           seed=args.serve_seed, hbm_budget_bytes=120 << 30,
                           max_frames_per_round=args.serve_max_frames, ring=3, key_lane=args.serve_key_lanes,
-                          start_spread_s=1.0, record=record, decode_ahead=args.serve_ahead)
+                          start_spread_s=1.0, record=record, decode_ahead=args.serve_ahead,
+                          key_cache=args.serve_key_cache)
         counts, which = {}, []
         for i in range(args.serve_streams):
             k = i % len(clips)
@@ -836,7 +837,8 @@ def run_serve(args):
                           "idle_s": round(st["idle_s"], 3), "plan_s": round(st["plan_s"], 3),
                           "collect_s": round(st["collect_s"], 3), "kernel_ms": round(st["kernel_ms"], 1),
                           "entropy_ms": round(st["entropy_ms"], 1), "recon_ms": round(st["recon_ms"], 1)},
-        "side_lanes": args.serve_key_lanes, "start_spread_s": 1.0, "key_frames": st["key_frames"],
+        "side_lanes": args.serve_key_lanes, "key_cache": args.serve_key_cache, "key_installs": st["key_installs"],
+        "start_spread_s": 1.0, "key_frames": st["key_frames"],
     }
     del srv
     # Record run: every delivered frame's FNV-1a against the oracle's.
@@ -945,6 +947,9 @@ def main():
     ap.add_argument("--serve-max-frames", type=int, default=4, help="frames of one stream per serving round")
     ap.add_argument("--serve-ahead", type=int, default=6, help="frames decoded ahead of each stream's requests")
     ap.add_argument("--serve-key-lanes", type=int, default=3, help="side lanes for key frames with long chains")
+    ap.add_argument("--serve-key-cache", type=int, default=1,
+                    help="1: streams with long key frames reinstall key frames they decoded before; 2: and decode "
+                         "them all at admission (their requests start later)")
     ap.add_argument("--serve-seed", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the RGBA, ingest, alt-ref and analysis legs")

@@ -38,7 +38,7 @@ class ServeOptions(C.Structure):
                 ("seed", C.c_uint64), ("hbm_budget_bytes", C.c_uint64), ("max_frames_per_round", C.c_int32),
                 ("ring", C.c_int32), ("record", C.c_int32), ("key_lane", C.c_int32),
                 ("start_spread_s", C.c_double), ("decode_ahead", C.c_int32), ("decode_lanes", C.c_int32),
-                ("long_key_mbs", C.c_int32)]
+                ("long_key_mbs", C.c_int32), ("key_cache", C.c_int32)]
 
 
 class ServeStats(C.Structure):
@@ -51,7 +51,8 @@ class ServeStats(C.Structure):
                 ("seek_latency_p50_ms", C.c_double), ("seek_latency_p99_ms", C.c_double),
                 ("main_rounds", C.c_int64), ("side_rounds", C.c_int64), ("main_frames", C.c_int64),
                 ("main_round_s", C.c_double), ("idle_s", C.c_double), ("plan_s", C.c_double),
-                ("launch_s", C.c_double), ("collect_s", C.c_double)]
+                ("launch_s", C.c_double), ("collect_s", C.c_double), ("key_installs", C.c_int64),
+                ("warmed_streams", C.c_int64), ("warmup_s", C.c_double)]
 
 
 class Frame(C.Structure):

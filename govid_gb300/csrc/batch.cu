@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
 #include <chrono>
 #include <cstring>
 #include <new>
@@ -123,6 +124,19 @@ struct Engine::Stream {
   int64_t epoch = 0;
   std::vector<int> roundBufs[Engine::kParities];  // by round parity (the last: side lane)
   bool inSide = false;            // a side round holds this stream
+  // Key-frame cache: per key frame decoded while caching is on, its image,
+  // the golden image after it (only when an alt-ref override made them
+  // differ) and the table history after it.  A key frame resets the table
+  // history and every reference, so these are the whole decoder state after
+  // it (ebiv/codec.go:155-191).
+  struct CachedKey {
+    uint8_t* img = nullptr;
+    uint8_t* golden = nullptr;
+    TableHistory hist;
+  };
+  bool cacheKeys = false;
+  std::map<int64_t, CachedKey> keyCache;
+  size_t cacheBytes = 0;
 
   uint8_t* plane(int b, int k) const {
     return pool[(size_t)b] + (k == 0 ? 0 : yBytes + (size_t)(k - 1) * cBytes);
@@ -130,6 +144,11 @@ struct Engine::Stream {
   void release() {
     for (auto p : pool) cudaFree(p);
     pool.clear();
+    for (auto& kv : keyCache) {
+      cudaFree(kv.second.img);
+      if (kv.second.golden) cudaFree(kv.second.golden);
+    }
+    keyCache.clear();
     for (auto& sl : slots) sl.release();
     slots.clear();
     if (dPkts && ownsPkts) cudaFree(dPkts);
@@ -650,6 +669,27 @@ int Engine::finishFrame(Stream& s, Job& j, const int32_t* st, std::vector<RoundR
     if (status == kOK) {
       s.ref = j.work;
       out = j.work;
+    }
+  }
+  if (out >= 0 && r.keyframe && s.cacheKeys && !s.keyCache.count(j.pktIndex) && j.fh.coding != kCodingRaw) {
+    // Both images are complete (the round was collected) and no device work
+    // of a later round writes them before this copy returns.
+    Stream::CachedKey ck;
+    const bool og = s.golden != out;
+    if (cudaMalloc(&ck.img, s.bufBytes) == cudaSuccess &&
+        cudaMemcpy(ck.img, s.pool[(size_t)out], s.bufBytes, cudaMemcpyDeviceToDevice) == cudaSuccess &&
+        (!og || (cudaMalloc(&ck.golden, s.bufBytes) == cudaSuccess &&
+                 cudaMemcpy(ck.golden, s.pool[(size_t)s.golden], s.bufBytes, cudaMemcpyDeviceToDevice) ==
+                     cudaSuccess))) {
+      ck.hist = j.hAfter;
+      const size_t b = s.bufBytes * (og ? 2 : 1);
+      s.cacheBytes += b;
+      deviceBytes_ += b;
+      s.keyCache[j.pktIndex] = ck;
+    } else {
+      if (ck.img) cudaFree(ck.img);
+      if (ck.golden) cudaFree(ck.golden);
+      cudaGetLastError();  // the cache is an optimisation: a failed copy leaves the key uncached
     }
   }
   if (out >= 0) {
@@ -1353,6 +1393,72 @@ int Engine::drain(std::vector<RoundResult>* results) {
     pipe_.erase(pipe_.begin());
   }
   return n;
+}
+
+int Engine::setKeyCache(int id, bool on) {
+  if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id] || !streams_[(size_t)id]->resident)
+    return kErrArg;
+  streams_[(size_t)id]->cacheKeys = on;
+  return kOK;
+}
+
+bool Engine::keyCached(int id, int64_t index) const {
+  if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) return false;
+  return streams_[(size_t)id]->keyCache.count(index) != 0;
+}
+
+size_t Engine::keyCacheBytes(int id) const {
+  if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) return 0;
+  return streams_[(size_t)id]->cacheBytes;
+}
+
+int Engine::installKey(int id, int64_t index, std::vector<RoundResult>* results) {
+  if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) return kErrArg;
+  Stream& s = *streams_[(size_t)id];
+  const auto it = s.keyCache.find(index);
+  if (it == s.keyCache.end() || s.inSide || s.hasProv || !s.ready) return kErrArg;
+  for (const auto& rb : s.roundBufs)
+    if (!rb.empty()) return kErrArg;  // a round in flight holds this stream
+  std::vector<char> busy(s.pool.size(), 0);
+  if (s.ref >= 0) busy[(size_t)s.ref] = 1;
+  if (s.golden >= 0) busy[(size_t)s.golden] = 1;
+  for (int b : s.outputs) busy[(size_t)b] = 1;
+  const int b = freeBuffer(s.pool.size(), busy);
+  if (b < 0) return kErrDevice;
+  busy[(size_t)b] = 1;
+  int g = b;
+  if (it->second.golden) {
+    g = freeBuffer(s.pool.size(), busy);
+    if (g < 0) return kErrDevice;
+  }
+  if (cudaMemcpy(s.pool[(size_t)b], it->second.img, s.bufBytes, cudaMemcpyDeviceToDevice) != cudaSuccess ||
+      (g != b && cudaMemcpy(s.pool[(size_t)g], it->second.golden, s.bufBytes, cudaMemcpyDeviceToDevice) !=
+                     cudaSuccess))
+    return kErrDevice;
+  // The state Decode leaves after this key frame: references, table history,
+  // the next packet, and the frame as the newest output.
+  s.ref = b;
+  s.golden = g;
+  s.hist = it->second.hist;
+  s.next = index + 1;
+  s.outputs.push_back(b);
+  const int cap = s.ring + (s.resident ? lookahead_ : 1);
+  while ((int)s.outputs.size() > cap) s.outputs.erase(s.outputs.begin());
+  RoundResult r;
+  r.stream = s.id;
+  r.frameIndex = index;
+  r.keyframe = true;
+  r.status = kOK;
+  r.view.y = s.plane(b, 0);
+  r.view.cb = s.plane(b, 1);
+  r.view.cr = s.plane(b, 2);
+  r.view.yStride = s.strideY;
+  r.view.cStride = s.strideC;
+  r.view.width = s.geo.W;
+  r.view.height = s.geo.H;
+  r.view.buffer = b;
+  if (results) results->push_back(r);
+  return kOK;
 }
 
 int Engine::downloadFrame(const EngineFrameView& v, uint8_t* packed, size_t cap) {

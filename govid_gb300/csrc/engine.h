@@ -134,6 +134,17 @@ class Engine {
   bool sideReady(int lane);  // the lane's round is complete
   int collectSide(int lane, std::vector<RoundResult>* results);
 
+  // Key-frame cache of a resident stream (serving): with it on, every key
+  // frame the stream decodes keeps a copy of its image (and of the golden
+  // image when an override changed it) and of the table history after it.
+  // installKey puts the stream in the state decoding that key frame leaves
+  // (references, table history, next packet) without decoding it, and
+  // returns the frame as a result; the stream must have no round in flight.
+  int setKeyCache(int id, bool on);
+  bool keyCached(int id, int64_t index) const;
+  size_t keyCacheBytes(int id) const;
+  int installKey(int id, int64_t index, std::vector<RoundResult>* results);
+
   int downloadFrame(const EngineFrameView& v, uint8_t* packed, size_t cap);
   // Queues the copy on the engine's copy stream, beside the reconstruction;
   // complete after syncCopies().  Later rounds' device work waits for it

@@ -61,6 +61,7 @@ struct ServeOptionsC {
   int decodeAhead = 0;     // frames decoded ahead of each stream's requests (0: twice the lookahead)
   int lanes = 0;           // decode lanes (engines with their own thread and side lane); 0: 1
   int longKeyMBs = 0;      // key frames whose largest tile has more macroblocks go to a side lane (0: 1500)
+  int keyCache = 0;        // streams with long key frames: 1 cache keys as decoded, 2 also decode them at admission
 };
 
 struct ServeStatsC {
@@ -72,6 +73,8 @@ struct ServeStatsC {
   int64_t readyAtArrival = 0, unserved = 0;
   double seekP50 = 0, seekP99 = 0;
   int64_t mainRounds = 0, sideRounds = 0, mainFrames = 0;
+  int64_t keyInstalls = 0, warmedStreams = 0;
+  double warmupSec = 0;  // admission to first request of streams that decoded their key frames first
   double mainRoundSec = 0, idleSec = 0;  // decode thread: inside main rounds, waiting for work
   double planSec = 0, launchSec = 0, collectSec = 0;  // inside main rounds: host planning, launches, wait
 };
@@ -130,6 +133,12 @@ class Server {
     sp->fps = fps;
     sp->loop = loop;
     sp->footprint = Engine::footprint(sp->w, sp->h, ringOf(), lookahead_, 0, sideLanes());
+    if (sp->longKey && opt_.keyCache > 0) {  // one image per key frame (two when an override changed golden)
+      const Geometry g = Geometry::of(sp->w, sp->h);
+      auto s64 = [](int w) { return (size_t)((w + 63) & ~63); };  // the engine's 64-byte row stride
+      const size_t img = s64(g.padW()) * g.padH() + 2 * s64(g.padCW()) * g.padCH();
+      sp->footprint += 2 * img * sp->keys.size();
+    }
     for (auto& p : sp->pkts) sp->footprint += (p.size() + 15) / 16 * 16;
     specs_.push_back(std::move(sp));
     return kOK;
@@ -234,6 +243,9 @@ class Server {
     double nextArrival = 0;
     int64_t issued = 0, consumePos = 0;
     std::deque<Request> queue;
+    bool warming = false;     // decoding its key frames into the cache before its requests start
+    bool noInstall = false;   // an install failed: this stream decodes its key frames
+    double admittedAt = 0;
     // decode thread
     uint64_t decEpoch = 0;
     bool inSide = false;
@@ -307,6 +319,11 @@ class Server {
       sp.lane = L.index;
       if ((int)L.specOf.size() <= sp.engineId) L.specOf.resize((size_t)sp.engineId + 1, -1);
       L.specOf[(size_t)sp.engineId] = si;
+      if (sp.longKey && opt_.keyCache > 0) {
+        L.eng.setKeyCache(sp.engineId, true);
+        sp.warming = opt_.keyCache > 1;
+      }
+      sp.admittedAt = now();
       sp.startAt = now();
       if (initial && opt_.startSpread > 0)
         sp.startAt += std::uniform_real_distribution<double>(0, opt_.startSpread)(rng_);
@@ -333,7 +350,7 @@ class Server {
       uint64_t ep = ~0ull;
       for (const auto& pl : planned)
         if (pl.first == si) ep = pl.second;
-      if (ep != sp.epoch) continue;
+      if (ep != sp.epoch || sp.warming) continue;
       Ready rd;
       rd.frame = r.frameIndex;
       rd.status = r.status;
@@ -369,6 +386,7 @@ class Server {
       std::vector<int> ids, counts, kids, reposition;
       std::vector<int64_t> repoTo;
       std::vector<std::pair<int, uint64_t>> planned;
+      std::vector<std::pair<int, int64_t>> installs;  // (spec, key frame) served from the key cache
       int sideLane = -1;
       {
         std::unique_lock<std::mutex> lk(mu_);
@@ -393,10 +411,42 @@ class Server {
         for (int si : L.admitted) {
           Spec& sp = *specs_[(size_t)si];
           if (sp.inSide || sp.finished) continue;
+          if (sp.warming) {
+            // Admission: each key frame once through a side lane into the
+            // cache, then back to the first frame and the requests start.
+            int64_t want = -1;
+            for (int64_t k : sp.keys)
+              if (!L.eng.keyCached(sp.engineId, k)) {
+                want = k;
+                break;
+              }
+            const int64_t at = (int64_t)sp.pkts.size() - L.eng.remaining(sp.engineId);
+            if (want < 0) {
+              sp.warming = false;
+              reposition.push_back(sp.engineId);
+              repoTo.push_back(0);
+              sp.startAt = now();
+              st_.warmedStreams++;
+              st_.warmupSec += sp.startAt - sp.admittedAt;
+            } else if (at != want) {
+              reposition.push_back(sp.engineId);
+              repoTo.push_back(want);
+            } else if (sideLane >= 0 && kids.size() < 64) {
+              kids.push_back(sp.engineId);
+              sp.inSide = true;
+              L.sidePlanned[sideLane].push_back({si, sp.epoch});
+            }
+            continue;
+          }
           if (sp.decEpoch != sp.epoch) {  // a seek: restart at its key frame
             sp.decEpoch = sp.epoch;
-            reposition.push_back(sp.engineId);
-            repoTo.push_back(sp.seekTarget);
+            if (!sp.noInstall && L.eng.keyCached(sp.engineId, sp.seekTarget)) {
+              installs.push_back({si, sp.seekTarget});
+              sp.inflight = 1;
+            } else {
+              reposition.push_back(sp.engineId);
+              repoTo.push_back(sp.seekTarget);
+            }
             continue;  // planned next time round, after the engine moved
           }
           const int room = ahead_ - (int)sp.ready.size() - sp.inflight;
@@ -407,6 +457,11 @@ class Server {
             reposition.push_back(sp.engineId);  // looping: on from the first frame
             repoTo.push_back(0);
             st_.loops++;
+            continue;
+          }
+          if (sp.longKey && !sp.noInstall && isKey(sp, pos) && L.eng.keyCached(sp.engineId, pos)) {
+            installs.push_back({si, pos});
+            sp.inflight = 1;
             continue;
           }
           if (sp.longKey && isKey(sp, pos)) {
@@ -429,7 +484,7 @@ class Server {
           sp.inflight = n;
           planned.push_back({si, sp.epoch});
         }
-        if (ids.empty() && kids.empty() && reposition.empty() && !L.eng.anySideBusy()) {
+        if (ids.empty() && kids.empty() && reposition.empty() && installs.empty() && !L.eng.anySideBusy()) {
           const double w0 = nowSec();
           cvDecode_.wait_for(lk, std::chrono::microseconds(500));
           st_.idleSec += nowSec() - w0;
@@ -437,6 +492,25 @@ class Server {
         }
       }
       for (size_t k = 0; k < reposition.size(); k++) L.eng.seekStream(reposition[k], repoTo[k]);
+      if (!installs.empty()) {
+        res.clear();
+        for (const auto& in : installs) {
+          const int id = specs_[(size_t)in.first]->engineId;
+          if (L.eng.installKey(id, in.second, &res) != kOK) {  // not installable: decode key frames from now on
+            L.eng.seekStream(id, in.second);
+            std::lock_guard<std::mutex> lk(mu_);
+            specs_[(size_t)in.first]->inflight = 0;
+            specs_[(size_t)in.first]->noInstall = true;
+          }
+        }
+        hashResults(L, res, &hashes);
+        std::lock_guard<std::mutex> lk(mu_);
+        st_.keyInstalls += (int64_t)res.size();
+        std::vector<std::pair<int, uint64_t>> pl;
+        for (const auto& in : installs) pl.push_back({in.first, specs_[(size_t)in.first]->decEpoch});
+        publish(L, res, hashes, pl);
+        cvRequest_.notify_all();
+      }
       if (!kids.empty() && L.eng.launchSide(sideLane, kids)) {
         std::lock_guard<std::mutex> lk(mu_);
         decodeStatus_ = kErrDevice;
@@ -545,6 +619,7 @@ class Server {
         Spec& sp = *specs_[si];
         if (!sp.admitted || sp.done || sp.finished) continue;
         live = true;
+        if (sp.warming) continue;
         if (!sp.started) {
           sp.started = true;
           sp.nextArrival = sp.startAt;
@@ -624,6 +699,7 @@ int ebivgpu_server_create(const ebivgpu_serve_options* o, ebivgpu_server** out) 
   c.decodeAhead = o->decode_ahead > 0 ? o->decode_ahead : 0;
   c.lanes = o->decode_lanes > 0 ? o->decode_lanes : 0;
   c.longKeyMBs = o->long_key_mbs > 0 ? o->long_key_mbs : 0;
+  c.keyCache = o->key_cache > 0 ? o->key_cache : 0;
   ebivgpu_server* h = new (std::nothrow) ebivgpu_server();
   if (!h) return kErrDevice;
   h->s.reset(new Server(c));
@@ -678,6 +754,9 @@ int ebivgpu_server_run(ebivgpu_server* h, ebivgpu_serve_stats* out) {
   out->plan_s = st.planSec;
   out->launch_s = st.launchSec;
   out->collect_s = st.collectSec;
+  out->key_installs = st.keyInstalls;
+  out->warmed_streams = st.warmedStreams;
+  out->warmup_s = st.warmupSec;
   return r;
 }
 
@@ -703,7 +782,7 @@ uint64_t ebivgpu_server_stream_footprint(const ebivgpu_serve_options* o, int wid
   const int ahead = std::max(o->decode_ahead > 0 ? (int)o->decode_ahead : 2 * lookahead, lookahead);
   const int ring = std::max(o->ring >= 2 ? (int)o->ring : 3, ahead + 2);
   const int side = o->key_lane > 0 ? std::min((int)o->key_lane, Engine::kSideLanes) : 0;
-  return Engine::footprint(width, height, ring, lookahead, 0, side) + packet_bytes;
+  return Engine::footprint(width, height, ring, lookahead, 0, side) + packet_bytes;  // without a key cache
 }
 
 }  // extern "C"

@@ -361,11 +361,11 @@ class Server:
     def __init__(self, duration_s: float = 10.0, frames_per_stream: int = 600, seek_prob: float = 0.05,
                  seed: int = 1, hbm_budget_bytes: int = 120 << 30, max_frames_per_round: int = 4, ring: int = 3,
                  record: bool = False, key_lane: int = 1, start_spread_s: float = 0.0, decode_ahead: int = 0,
-                 decode_lanes: int = 0, long_key_mbs: int = 0):
+                 decode_lanes: int = 0, long_key_mbs: int = 0, key_cache: int = 0):
         L = _native.lib()
         o = _native.ServeOptions(duration_s, frames_per_stream, seek_prob, seed, hbm_budget_bytes,
                                  max_frames_per_round, ring, int(record), int(key_lane), float(start_spread_s),
-                                 int(decode_ahead), int(decode_lanes), int(long_key_mbs))
+                                 int(decode_ahead), int(decode_lanes), int(long_key_mbs), int(key_cache))
         h = C.c_void_p()
         _check(L.ebivgpu_server_create(C.byref(o), C.byref(h)), "server")
         self._h, self._L, self._o = h, L, o

@@ -197,6 +197,10 @@ typedef struct {
   int32_t decode_ahead;        /* frames decoded ahead of each stream's requests (0: twice max_frames_per_round) */
   int32_t decode_lanes;        /* engines decoding side by side, each with its own thread and side lane (0: 1) */
   int32_t long_key_mbs;        /* key frames whose largest tile has more macroblocks use the side lanes (0: 1500) */
+  int32_t key_cache;           /* streams with such key frames: 1 keep each decoded key frame (image, golden,
+                                  table history) and install it at a seek or when reached again instead of
+                                  decoding it; 2 also decode all of them at admission, before the stream's
+                                  requests start (0: off) */
 } ebivgpu_serve_options;
 typedef struct {
   int64_t requests, frames, errors, seeks, loops, rounds;
@@ -211,6 +215,8 @@ typedef struct {
   int64_t main_rounds, side_rounds, main_frames;    /* rounds of the decode thread, frames of main rounds */
   double main_round_s, idle_s;  /* decode threads: time inside main rounds, time with nothing to decode */
   double plan_s, launch_s, collect_s; /* main rounds: host planning, launches, waiting for the GPU */
+  int64_t key_installs, warmed_streams; /* key frames served from the key cache; streams warmed at admission */
+  double warmup_s;             /* summed admission-to-first-request time of the warmed streams */
 } ebivgpu_serve_stats;
 int ebivgpu_server_create(const ebivgpu_serve_options* o, ebivgpu_server** out);
 int ebivgpu_server_add_stream(ebivgpu_server* s, const uint8_t* const* pkts, const size_t* lens, int n, double fps,
@@ -224,7 +230,8 @@ void ebivgpu_server_destroy(ebivgpu_server* s);
 uint64_t ebivgpu_frame_hash(const uint8_t* packed, size_t n);
 /* The HBM footprint a server with options o admits a stream of this geometry
  * by: its frame pool and decode slots, plus packet_bytes of resident packets
- * (each packet rounded up to 16 bytes). */
+ * (each packet rounded up to 16 bytes); a stream with a key cache adds two
+ * frame images per key frame. */
 uint64_t ebivgpu_server_stream_footprint(const ebivgpu_serve_options* o, int width, int height, uint64_t packet_bytes);
 
 /* ---- Key-frame decode without device allocation ---------------------------

@@ -21,13 +21,17 @@ def _streams():
     return out
 
 
-@pytest.mark.parametrize("lanes,side,long_key", [(1, 1, 0), (3, 1, 20), (1, 3, 20)])
-def test_mix_equals_alone_with_seeks_and_loops(gpu_required, lanes, side, long_key):
+@pytest.mark.parametrize("lanes,side,long_key,cache", [(1, 1, 0, 0), (3, 1, 20, 0), (1, 3, 20, 0), (1, 2, 20, 1),
+                                                        (2, 2, 20, 2)])
+def test_mix_equals_alone_with_seeks_and_loops(gpu_required, lanes, side, long_key, cache):
     # long_key 20: every stream's key frames (tiles of more than 20
-    # macroblocks for most of them) take the side lanes.
+    # macroblocks for most of them) take the side lanes; with cache 1 those
+    # streams reinstall key frames they decoded before, with 2 they decode
+    # all of them at admission.
     streams = _streams()
     srv = ebiv.Server(duration_s=1.5, frames_per_stream=40, seek_prob=0.1, seed=3, record=True,
-                      max_frames_per_round=3, decode_lanes=lanes, key_lane=side, long_key_mbs=long_key)
+                      max_frames_per_round=3, decode_lanes=lanes, key_lane=side, long_key_mbs=long_key,
+                      key_cache=cache)
     for i, (pk, w, h) in enumerate(streams):
         srv.add_stream(pk, fps=60 if i % 2 else 30, loop=(i % 3 == 0))
     st = srv.run()
@@ -38,6 +42,10 @@ def test_mix_equals_alone_with_seeks_and_loops(gpu_required, lanes, side, long_k
     for s, f, h in seen:
         assert h == alone[s][f], f"stream {s} frame {f} differs in the mix"
     assert st["admitted_total"] == len(streams)
+    if cache:
+        assert st["key_installs"] > 0
+    if cache == 2:
+        assert st["warmed_streams"] == 2  # the two streams whose tiles exceed 20 macroblocks
 
 
 def test_admission_respects_hbm_budget(gpu_required):
