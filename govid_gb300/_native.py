@@ -52,7 +52,8 @@ class ServeStats(C.Structure):
                 ("main_rounds", C.c_int64), ("side_rounds", C.c_int64), ("main_frames", C.c_int64),
                 ("main_round_s", C.c_double), ("idle_s", C.c_double), ("plan_s", C.c_double),
                 ("launch_s", C.c_double), ("collect_s", C.c_double), ("key_installs", C.c_int64),
-                ("warmed_streams", C.c_int64), ("warmup_s", C.c_double)]
+                ("warmed_streams", C.c_int64), ("warmup_s", C.c_double), ("aside_rounds", C.c_int64),
+                ("prepare_s", C.c_double)]
 
 
 class Frame(C.Structure):
@@ -132,6 +133,7 @@ def lib() -> C.CDLL:
     # serving
     _sig(L, "ebivgpu_server_create", I, C.POINTER(ServeOptions), PP)
     _sig(L, "ebivgpu_server_stream_footprint", C.c_uint64, C.POINTER(ServeOptions), I, I, C.c_uint64)
+    _sig(L, "ebivgpu_server_request_log", I64, P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, I64)
     _sig(L, "ebivgpu_server_add_stream", I, P, C.POINTER(C.c_char_p), C.POINTER(S), I, C.c_double, I)
     _sig(L, "ebivgpu_server_run", I, P, C.POINTER(ServeStats))
     _sig(L, "ebivgpu_server_frame_hashes", I64, P, C.POINTER(C.c_int32), C.POINTER(I64), C.POINTER(C.c_uint64), I64)

@@ -137,6 +137,7 @@ struct Engine::Stream {
   bool cacheKeys = false;
   std::map<int64_t, CachedKey> keyCache;
   size_t cacheBytes = 0;
+  bool inAside = false;  // a side-lane round decodes one of its key frames into the cache
 
   uint8_t* plane(int b, int k) const {
     return pool[(size_t)b] + (k == 0 ? 0 : yBytes + (size_t)(k - 1) * cBytes);
@@ -200,6 +201,7 @@ struct Engine::Round {
   size_t oDesc = 0, oStat = 0, oJobs = 0, oEJobs = 0;
   bool launched = false;  // entropy launched; statuses pending
   bool reconLaunched = false;
+  bool aside = false;     // key frames decoded only into their streams' key caches
   void noteTile(const TileRange& t) {
     const int w = t.mbX1 - t.mbX0, h = t.mbY1 - t.mbY0;
     maxTileMBs = std::max(maxTileMBs, w * h);
@@ -212,6 +214,7 @@ struct Engine::Round {
     nDesc = nTiles = nEJobs = maxTileMBs = maxTileKeys = 0;
     groups = stepsPerGroup = 1;
     launched = false;
+    aside = false;
   }
 };
 
@@ -671,27 +674,8 @@ int Engine::finishFrame(Stream& s, Job& j, const int32_t* st, std::vector<RoundR
       out = j.work;
     }
   }
-  if (out >= 0 && r.keyframe && s.cacheKeys && !s.keyCache.count(j.pktIndex) && j.fh.coding != kCodingRaw) {
-    // Both images are complete (the round was collected) and no device work
-    // of a later round writes them before this copy returns.
-    Stream::CachedKey ck;
-    const bool og = s.golden != out;
-    if (cudaMalloc(&ck.img, s.bufBytes) == cudaSuccess &&
-        cudaMemcpy(ck.img, s.pool[(size_t)out], s.bufBytes, cudaMemcpyDeviceToDevice) == cudaSuccess &&
-        (!og || (cudaMalloc(&ck.golden, s.bufBytes) == cudaSuccess &&
-                 cudaMemcpy(ck.golden, s.pool[(size_t)s.golden], s.bufBytes, cudaMemcpyDeviceToDevice) ==
-                     cudaSuccess))) {
-      ck.hist = j.hAfter;
-      const size_t b = s.bufBytes * (og ? 2 : 1);
-      s.cacheBytes += b;
-      deviceBytes_ += b;
-      s.keyCache[j.pktIndex] = ck;
-    } else {
-      if (ck.img) cudaFree(ck.img);
-      if (ck.golden) cudaFree(ck.golden);
-      cudaGetLastError();  // the cache is an optimisation: a failed copy leaves the key uncached
-    }
-  }
+  if (out >= 0 && r.keyframe && s.cacheKeys && j.fh.coding != kCodingRaw)
+    cacheKey(s, j.pktIndex, out, s.golden, j.hAfter);
   if (out >= 0) {
     s.outputs.push_back(out);
     const int cap = s.ring + (s.resident ? lookahead_ : 1);
@@ -761,7 +745,7 @@ int Engine::planRound(const std::vector<int>& ids, const std::vector<int>* maxFr
     Stream& s = *streams_[(size_t)id];
     // A stream in the side lane stays out of main rounds; the side lane takes
     // only streams with no round in flight.
-    if (isSide(P) ? (s.inSide || s.hasProv) : s.inSide) continue;
+    if (isSide(P) ? (s.inSide || s.hasProv || s.inAside) : s.inSide) continue;
     std::vector<int> chain;
     std::vector<char> busy;
     // Start from the provisional references after the stream's in-flight
@@ -1182,6 +1166,20 @@ int Engine::collectRound(Round& R, std::vector<RoundResult>* results) {
     reconMs_ += b;
     kernelMs_ += a + b;
   }
+  if (R.aside) {  // key frames into the caches; the streams' state is untouched
+    for (const Job& j : R.jobs) {
+      if (j.stream < 0 || j.stream >= (int)streams_.size() || !streams_[(size_t)j.stream]) continue;
+      Stream& s = *streams_[(size_t)j.stream];
+      s.roundBufs[P].clear();
+      s.inAside = false;
+      const bool ok = j.status == kOK && j.gpu && j.mainDesc >= 0 && statuses[(size_t)j.mainDesc] == kOK &&
+                      j.fh.type == kFrameKey && j.work >= 0 &&
+                      (!j.hasOv || (j.ovPlanStatus == kOK && j.ovDesc >= 0 && statuses[(size_t)j.ovDesc] == kOK));
+      if (ok) cacheKey(s, j.pktIndex, j.work, j.hasOv ? j.ovBuf : j.work, j.hAfter);
+    }
+    R.clear();
+    return 0;
+  }
   // ---- commit each stream's chain in order; roll back at the first skipped frame
   int attempted = 0;
   for (const auto& chain : R.chains) {
@@ -1347,6 +1345,12 @@ int Engine::freeSideLane() const {
   return -1;
 }
 
+int Engine::freeSideLanes() const {
+  int n = 0;
+  for (int l = 0; l < sideLanes_; l++) n += sideInflight_[l] ? 0 : 1;
+  return n;
+}
+
 bool Engine::anySideBusy() const {
   for (bool b : sideInflight_)
     if (b) return true;
@@ -1395,6 +1399,86 @@ int Engine::drain(std::vector<RoundResult>* results) {
   return n;
 }
 
+// Copies a decoded key frame (pool buffer img; golden when an override made
+// it differ) and the table history after it into the stream's key cache.
+// Both images are complete (their round was collected) and no device work
+// of a later round writes them before these copies return.
+void Engine::cacheKey(Stream& s, int64_t index, int img, int golden, const TableHistory& hist) {
+  if (s.keyCache.count(index)) return;
+  Stream::CachedKey ck;
+  const bool og = golden != img;
+  if (cudaMalloc(&ck.img, s.bufBytes) == cudaSuccess &&
+      cudaMemcpy(ck.img, s.pool[(size_t)img], s.bufBytes, cudaMemcpyDeviceToDevice) == cudaSuccess &&
+      (!og || (cudaMalloc(&ck.golden, s.bufBytes) == cudaSuccess &&
+               cudaMemcpy(ck.golden, s.pool[(size_t)golden], s.bufBytes, cudaMemcpyDeviceToDevice) ==
+                   cudaSuccess))) {
+    ck.hist = hist;
+    const size_t b = s.bufBytes * (og ? 2 : 1);
+    s.cacheBytes += b;
+    deviceBytes_ += b;
+    s.keyCache[index] = ck;
+  } else {
+    if (ck.img) cudaFree(ck.img);
+    if (ck.golden) cudaFree(ck.golden);
+    cudaGetLastError();  // the cache is an optimisation: a failed copy leaves the key uncached
+  }
+}
+
+int Engine::launchAside(int lane, const std::vector<int>& ids, const std::vector<int64_t>& keys) {
+  if (!side_ || lane < 0 || lane >= sideLanes_ || sideInflight_[lane] || ids.size() != keys.size()) return kErrArg;
+  struct Saved {
+    int64_t next;
+    TableHistory hist;
+    bool hasProv;
+    int pRef, pGolden;
+    int64_t lastRound;
+  };
+  std::vector<int> use;
+  std::vector<Saved> saved;
+  for (size_t i = 0; i < ids.size(); i++) {
+    const int id = ids[i];
+    if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) continue;
+    Stream& s = *streams_[(size_t)id];
+    if (!s.resident || !s.ready || !s.cacheKeys || s.inSide || s.inAside || s.hasProv || keys[i] < 0 ||
+        keys[i] >= (int64_t)s.packets() || s.keyCache.count(keys[i]))
+      continue;
+    saved.push_back({s.next, s.hist, s.hasProv, s.pRef, s.pGolden, s.lastRound});
+    use.push_back(id);
+    s.next = keys[i];
+  }
+  if (use.empty()) return kErrArg;
+  Round& R = rounds_[kSide + lane];
+  R.parity = kSide + lane;
+  const std::vector<int> one(use.size(), 1);
+  const int planned = planRound(use, &one, R);
+  R.aside = true;
+  // Planning moved the streams as if they had decoded the key frame; their
+  // own decode resumes exactly where it was.
+  for (size_t i = 0; i < use.size(); i++) {
+    Stream& s = *streams_[(size_t)use[i]];
+    s.next = saved[i].next;
+    s.hist = saved[i].hist;
+    s.hasProv = saved[i].hasProv;
+    s.pRef = saved[i].pRef;
+    s.pGolden = saved[i].pGolden;
+    s.lastRound = saved[i].lastRound;
+    s.inSide = false;
+    s.inAside = true;
+  }
+  if (planned || launchRecon(R)) {
+    for (Job& j : R.jobs)
+      if (j.status == kOK) j.status = kErrDevice;
+    R.nDesc = 0;
+  }
+  if (cudaEventRecord(sideDone_[lane], streamRS_[lane]) != cudaSuccess) return kErrDevice;
+  sideInflight_[lane] = true;
+  return kOK;
+}
+
+bool Engine::inAside(int id) const {
+  return id >= 0 && id < (int)streams_.size() && streams_[(size_t)id] && streams_[(size_t)id]->inAside;
+}
+
 int Engine::setKeyCache(int id, bool on) {
   if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id] || !streams_[(size_t)id]->resident)
     return kErrArg;
@@ -1417,12 +1501,14 @@ int Engine::installKey(int id, int64_t index, std::vector<RoundResult>* results)
   Stream& s = *streams_[(size_t)id];
   const auto it = s.keyCache.find(index);
   if (it == s.keyCache.end() || s.inSide || s.hasProv || !s.ready) return kErrArg;
-  for (const auto& rb : s.roundBufs)
-    if (!rb.empty()) return kErrArg;  // a round in flight holds this stream
+  for (int q = 0; q < kSide; q++)
+    if (!s.roundBufs[q].empty()) return kErrArg;  // a main round in flight holds this stream
   std::vector<char> busy(s.pool.size(), 0);
   if (s.ref >= 0) busy[(size_t)s.ref] = 1;
   if (s.golden >= 0) busy[(size_t)s.golden] = 1;
   for (int b : s.outputs) busy[(size_t)b] = 1;
+  for (const auto& rb : s.roundBufs)  // an aside round's buffer
+    for (int b2 : rb) busy[(size_t)b2] = 1;
   const int b = freeBuffer(s.pool.size(), busy);
   if (b < 0) return kErrDevice;
   busy[(size_t)b] = 1;

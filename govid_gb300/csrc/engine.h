@@ -128,6 +128,7 @@ class Engine {
   int enableSideLane(int lanes = 1);  // 1 to kSideLanes
   int sideLanes() const { return sideLanes_; }
   int freeSideLane() const;  // a lane with no round in flight, or -1
+  int freeSideLanes() const;  // how many lanes have no round in flight
   int launchSide(int lane, const std::vector<int>& ids);
   bool sideBusy(int lane) const { return lane >= 0 && lane < kSideLanes && sideInflight_[lane]; }
   bool anySideBusy() const;
@@ -144,6 +145,11 @@ class Engine {
   bool keyCached(int id, int64_t index) const;
   size_t keyCacheBytes(int id) const;
   int installKey(int id, int64_t index, std::vector<RoundResult>* results);
+  // A side-lane round that decodes key frame keys[i] of stream ids[i] only
+  // into that stream's key cache: the stream keeps decoding in main rounds
+  // meanwhile, its state untouched (collectSide returns no result for it).
+  int launchAside(int lane, const std::vector<int>& ids, const std::vector<int64_t>& keys);
+  bool inAside(int id) const;
 
   int downloadFrame(const EngineFrameView& v, uint8_t* packed, size_t cap);
   // Queues the copy on the engine's copy stream, beside the reconstruction;
@@ -193,6 +199,7 @@ class Engine {
   int planRound(const std::vector<int>& ids, const std::vector<int>* maxFrames, Round& r);
   int launchRecon(Round& r);
   int collectRound(Round& r, std::vector<RoundResult>* results);
+  void cacheKey(Stream& s, int64_t index, int img, int golden, const TableHistory& hist);
   // Streams of a round by parity: 0/1 main (pipelined rounds alternate), 2 side.
   static bool isSide(int parity) { return parity >= kSide; }
   cudaStream_t entropyStream(int parity = 0) const {

@@ -73,8 +73,9 @@ struct ServeStatsC {
   int64_t readyAtArrival = 0, unserved = 0;
   double seekP50 = 0, seekP99 = 0;
   int64_t mainRounds = 0, sideRounds = 0, mainFrames = 0;
-  int64_t keyInstalls = 0, warmedStreams = 0;
+  int64_t keyInstalls = 0, warmedStreams = 0, asideRounds = 0;
   double warmupSec = 0;  // admission to first request of streams that decoded their key frames first
+  double prepareSec = 0;  // key_cache 2: key frames of the streams admitted at start, before the first request
   double mainRoundSec = 0, idleSec = 0;  // decode thread: inside main rounds, waiting for work
   double planSec = 0, launchSec = 0, collectSec = 0;  // inside main rounds: host planning, launches, wait
 };
@@ -156,6 +157,34 @@ class Server {
     for (auto& L : lanes_) {
       Lane* lp = L.get();
       dec.emplace_back([this, lp] { decodeLoop(*lp); });
+    }
+    if (opt_.keyCache > 1) {
+      // Preparation (key_cache 2): the streams admitted at start decode their
+      // key frames into their caches before any request; the request clock
+      // starts afterwards, so their requests begin as if admitted now.
+      // Every stream also fills its decode-ahead before the clock starts, as a
+      // player buffers before it starts playback.
+      std::unique_lock<std::mutex> lk(mu_);
+      for (;;) {
+        bool busy = false;
+        for (auto& sp : specs_) {
+          if (!sp->admitted) continue;
+          const int64_t left = (int64_t)sp->pkts.size();
+          busy = busy || sp->warming || (int64_t)sp->ready.size() < std::min<int64_t>(ahead_, left);
+        }
+        if (!busy || stop_) break;
+        cvRequest_.wait_for(lk, std::chrono::milliseconds(1));
+      }
+      const double shift = nowSec() - t0_;
+      st_.prepareSec = shift;
+      t0_ += shift;
+      for (auto& sp : specs_) {
+        if (!sp->admitted) continue;
+        sp->admittedAt = 0;
+        sp->startAt = opt_.startSpread > 0 ? std::uniform_real_distribution<double>(0, opt_.startSpread)(rng_) : 0;
+        for (Ready& rd : sp->ready) rd.at -= shift;  // decoded before the clock started
+      }
+      st_.warmupSec = 0;
     }
     requestLoop();
     {
@@ -387,15 +416,19 @@ class Server {
       std::vector<int64_t> repoTo;
       std::vector<std::pair<int, uint64_t>> planned;
       std::vector<std::pair<int, int64_t>> installs;  // (spec, key frame) served from the key cache
+      std::vector<int> asideIds;
+      std::vector<int64_t> asideKeys;
       int sideLane = -1;
       {
         std::unique_lock<std::mutex> lk(mu_);
         if (stop_) break;
         // Finished streams leave; waiting ones come in.
         bool removed = false;
-        for (size_t k = 0; k < L.admitted.size();) {
+        // Finished streams free their memory only when a waiting stream needs
+        // it (freeing synchronises the device, which would stall every lane).
+        for (size_t k = 0; k < L.admitted.size() && !waiting_.empty();) {
           Spec& sp = *specs_[(size_t)L.admitted[k]];
-          if (sp.finished && !sp.inSide) {
+          if (sp.finished && !sp.inSide && !L.eng.inAside(sp.engineId)) {
             L.eng.removeStream(sp.engineId);
             used_ -= sp.footprint;
             sp.done = true;
@@ -465,7 +498,9 @@ class Server {
             continue;
           }
           if (sp.longKey && isKey(sp, pos)) {
-            if (sideLane >= 0 && kids.size() < 64) {
+            // (A stream whose key frame is being decoded into its cache waits
+            // for that round instead.)
+            if (sideLane >= 0 && kids.size() < 64 && !L.eng.inAside(sp.engineId)) {
               kids.push_back(sp.engineId);
               sp.inSide = true;
               sp.inflight = 1;
@@ -484,7 +519,31 @@ class Server {
           sp.inflight = n;
           planned.push_back({si, sp.epoch});
         }
-        if (ids.empty() && kids.empty() && reposition.empty() && installs.empty() && !L.eng.anySideBusy()) {
+        // A side lane nobody waits on fills key caches in the background (one
+        // lane stays free for key frames a stream waits for): for up to 16
+        // streams, the first key frame not yet cached after where each stream
+        // decodes now.
+        if (opt_.keyCache > 0 && kids.empty() && sideLane >= 0 && L.eng.freeSideLanes() >= 2) {
+          for (int si : L.admitted) {
+            if (asideIds.size() >= 16) break;
+            Spec& sp = *specs_[(size_t)si];
+            if (!sp.longKey || sp.warming || sp.inSide || sp.finished || sp.noInstall ||
+                L.eng.inAside(sp.engineId))
+              continue;
+            const int64_t at = (int64_t)sp.pkts.size() - L.eng.remaining(sp.engineId);
+            int64_t want = -1;
+            for (size_t q = 0; q < sp.keys.size() && want < 0; q++) {
+              const int64_t k = sp.keys[(std::upper_bound(sp.keys.begin(), sp.keys.end(), at) - sp.keys.begin() + q) %
+                                        sp.keys.size()];
+              if (!L.eng.keyCached(sp.engineId, k)) want = k;
+            }
+            if (want < 0) continue;
+            asideIds.push_back(sp.engineId);
+            asideKeys.push_back(want);
+          }
+        }
+        if (ids.empty() && kids.empty() && reposition.empty() && installs.empty() && asideIds.empty() &&
+            !L.eng.anySideBusy()) {
           const double w0 = nowSec();
           cvDecode_.wait_for(lk, std::chrono::microseconds(500));
           st_.idleSec += nowSec() - w0;
@@ -510,6 +569,10 @@ class Server {
         for (const auto& in : installs) pl.push_back({in.first, specs_[(size_t)in.first]->decEpoch});
         publish(L, res, hashes, pl);
         cvRequest_.notify_all();
+      }
+      if (!asideIds.empty() && L.eng.launchAside(sideLane, asideIds, asideKeys) == kOK) {
+        std::lock_guard<std::mutex> lk(mu_);
+        st_.asideRounds++;
       }
       if (!kids.empty() && L.eng.launchSide(sideLane, kids)) {
         std::lock_guard<std::mutex> lk(mu_);
@@ -602,6 +665,7 @@ class Server {
       if (rd.keyframe) st_.keyFrames++;
       const double l = std::max(0.0, std::max(t, rd.at) - arrival);
       lat_.push_back(l);
+      log_.push_back({arrival, l, si, rd.frame, wasSeek});
       if (wasSeek) seekLat_.push_back(l);
       if (rd.at <= arrival) st_.readyAtArrival++;
       if (opt_.record) hashes_.push_back({si, rd.frame, rd.hash});
@@ -667,6 +731,18 @@ class Server {
   double t0_ = 0, endTime_ = 0;
   ServeStatsC st_;
   std::vector<double> lat_, seekLat_, latencies_;
+
+ public:
+  struct LogEntry {
+    double arrival, latency;
+    int stream;
+    int64_t frame;
+    bool seek;
+  };
+  const std::vector<LogEntry>& requestLog() const { return log_; }
+
+ private:
+  std::vector<LogEntry> log_;
   std::vector<Hash> hashes_;
 };
 
@@ -757,6 +833,8 @@ int ebivgpu_server_run(ebivgpu_server* h, ebivgpu_serve_stats* out) {
   out->key_installs = st.keyInstalls;
   out->warmed_streams = st.warmedStreams;
   out->warmup_s = st.warmupSec;
+  out->aside_rounds = st.asideRounds;
+  out->prepare_s = st.prepareSec;
   return r;
 }
 
@@ -768,6 +846,22 @@ int64_t ebivgpu_server_frame_hashes(ebivgpu_server* h, int32_t* stream, int64_t*
     stream[i] = v[(size_t)i].stream;
     frame[i] = v[(size_t)i].frame;
     hash[i] = v[(size_t)i].hash;
+  }
+  return (int64_t)v.size();
+}
+
+int64_t ebivgpu_server_request_log(ebivgpu_server* h, double* arrival_s, double* latency_ms, int32_t* stream,
+                                   int64_t* frame, int32_t* seek, int64_t cap) {
+  if (!h) return 0;
+  const auto& v = h->s->requestLog();
+  const int64_t n = std::min<int64_t>(cap, (int64_t)v.size());
+  for (int64_t i = 0; i < n; i++) {
+    const auto& e = v[(size_t)i];
+    if (arrival_s) arrival_s[i] = e.arrival;
+    if (latency_ms) latency_ms[i] = e.latency * 1000;
+    if (stream) stream[i] = e.stream;
+    if (frame) frame[i] = e.frame;
+    if (seek) seek[i] = e.seek ? 1 : 0;
   }
   return (int64_t)v.size();
 }

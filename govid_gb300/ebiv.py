@@ -386,6 +386,14 @@ class Server:
         _check(self._L.ebivgpu_server_run(self._h, C.byref(st)))
         return {k: getattr(st, k) for k, _ in _native.ServeStats._fields_}
 
+    def request_log(self) -> dict[str, np.ndarray]:
+        """Every delivered request: arrival (s), latency (ms), stream, frame, seek."""
+        n = int(self._L.ebivgpu_server_request_log(self._h, None, None, None, None, None, 0))
+        out = {"arrival_s": np.zeros(n), "latency_ms": np.zeros(n), "stream": np.zeros(n, np.int32),
+               "frame": np.zeros(n, np.int64), "seek": np.zeros(n, np.int32)}
+        self._L.ebivgpu_server_request_log(self._h, *(out[k].ctypes.data for k in out), n)
+        return out
+
     def frame_hashes(self) -> list[tuple[int, int, int]]:
         n = self._L.ebivgpu_server_frame_hashes(self._h, None, None, None, 0)
         s = (C.c_int32 * n)()

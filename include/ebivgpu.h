@@ -199,8 +199,10 @@ typedef struct {
   int32_t long_key_mbs;        /* key frames whose largest tile has more macroblocks use the side lanes (0: 1500) */
   int32_t key_cache;           /* streams with such key frames: 1 keep each decoded key frame (image, golden,
                                   table history) and install it at a seek or when reached again instead of
-                                  decoding it; 2 also decode all of them at admission, before the stream's
-                                  requests start (0: off) */
+                                  decoding it, and fill the caches in the background on side lanes nobody
+                                  waits on; 2 also decode all of them at admission, before the stream's
+                                  requests start (for the streams admitted at start, before the request
+                                  clock starts: a preparation step reported as prepare_s) (0: off) */
 } ebivgpu_serve_options;
 typedef struct {
   int64_t requests, frames, errors, seeks, loops, rounds;
@@ -217,6 +219,8 @@ typedef struct {
   double plan_s, launch_s, collect_s; /* main rounds: host planning, launches, waiting for the GPU */
   int64_t key_installs, warmed_streams; /* key frames served from the key cache; streams warmed at admission */
   double warmup_s;             /* summed admission-to-first-request time of the warmed streams */
+  int64_t aside_rounds;        /* side-lane rounds that filled key caches in the background */
+  double prepare_s;            /* key_cache 2: key frames of the streams admitted at start, before the first request */
 } ebivgpu_serve_stats;
 int ebivgpu_server_create(const ebivgpu_serve_options* o, ebivgpu_server** out);
 int ebivgpu_server_add_stream(ebivgpu_server* s, const uint8_t* const* pkts, const size_t* lens, int n, double fps,
@@ -225,6 +229,11 @@ int ebivgpu_server_run(ebivgpu_server* s, ebivgpu_serve_stats* out);
 /* (stream index in add order, frame index, FNV-1a of the packed planes) per
  * delivered frame when record was set; returns the total count. */
 int64_t ebivgpu_server_frame_hashes(ebivgpu_server* s, int32_t* stream, int64_t* frame, uint64_t* hash, int64_t cap);
+/* Every delivered request in delivery order: arrival time (s from the start
+ * of the request clock), latency (ms), stream (add order), frame index, and
+ * whether it was a seek; any array may be NULL; returns the total count. */
+int64_t ebivgpu_server_request_log(ebivgpu_server* s, double* arrival_s, double* latency_ms, int32_t* stream,
+                                   int64_t* frame, int32_t* seek, int64_t cap);
 void ebivgpu_server_destroy(ebivgpu_server* s);
 /* FNV-1a 64 of a buffer (the hash the server records). */
 uint64_t ebivgpu_frame_hash(const uint8_t* packed, size_t n);
