@@ -274,6 +274,7 @@ class Server {
     std::deque<Request> queue;
     bool warming = false;     // decoding its key frames into the cache before its requests start
     bool noInstall = false;   // an install failed: this stream decodes its key frames
+    int warmRounds = 0;       // side rounds spent warming its key cache
     double admittedAt = 0;
     // decode thread
     uint64_t decEpoch = 0;
@@ -454,6 +455,10 @@ class Server {
                 break;
               }
             const int64_t at = (int64_t)sp.pkts.size() - L.eng.remaining(sp.engineId);
+            if (want >= 0 && sp.warmRounds > (int)sp.keys.size() + 2) {  // a key frame that will not cache
+              want = -1;
+              sp.noInstall = true;
+            }
             if (want < 0) {
               sp.warming = false;
               reposition.push_back(sp.engineId);
@@ -467,6 +472,7 @@ class Server {
             } else if (sideLane >= 0 && kids.size() < 64) {
               kids.push_back(sp.engineId);
               sp.inSide = true;
+              sp.warmRounds++;
               L.sidePlanned[sideLane].push_back({si, sp.epoch});
             }
             continue;
