@@ -61,7 +61,7 @@ struct ServeOptionsC {
   int decodeAhead = 0;     // frames decoded ahead of each stream's requests (0: twice the lookahead)
   int lanes = 0;           // decode lanes (engines with their own thread and side lane); 0: 1
   int longKeyMBs = 0;      // key frames whose largest tile has more macroblocks go to a side lane (0: 1500)
-  int keyCache = 0;        // streams with long key frames: 1 cache keys as decoded, 2 also decode them at admission
+  int keyCache = 0;        // 1 long-key streams cache key frames as decoded, 2 also decode them at admission, 3 every stream as 2
 };
 
 struct ServeStatsC {
@@ -134,7 +134,7 @@ class Server {
     sp->fps = fps;
     sp->loop = loop;
     sp->footprint = Engine::footprint(sp->w, sp->h, ringOf(), lookahead_, 0, sideLanes());
-    if (sp->longKey && opt_.keyCache > 0) {  // one image per key frame (two when an override changed golden)
+    if (cachesKeys(*sp)) {  // one image per key frame (two when an override changed golden)
       const Geometry g = Geometry::of(sp->w, sp->h);
       auto s64 = [](int w) { return (size_t)((w + 63) & ~63); };  // the engine's 64-byte row stride
       const size_t img = s64(g.padW()) * g.padH() + 2 * s64(g.padCW()) * g.padCH();
@@ -294,6 +294,9 @@ class Server {
   };
 
   int ringOf() const { return std::max(opt_.ring, ahead_ + 2); }
+  // Streams that keep a key cache: those with long key frames (key_cache 1
+  // and 2), every stream (key_cache 3).
+  bool cachesKeys(const Spec& sp) const { return opt_.keyCache >= 3 || (sp.longKey && opt_.keyCache > 0); }
   int sideLanes() const { return opt_.keyLane > 0 ? std::min(opt_.keyLane, Engine::kSideLanes) : 0; }
 
   // The largest tile of a key frame's coded payload: frame header, then the
@@ -349,7 +352,7 @@ class Server {
       sp.lane = L.index;
       if ((int)L.specOf.size() <= sp.engineId) L.specOf.resize((size_t)sp.engineId + 1, -1);
       L.specOf[(size_t)sp.engineId] = si;
-      if (sp.longKey && opt_.keyCache > 0) {
+      if (cachesKeys(sp)) {
         L.eng.setKeyCache(sp.engineId, true);
         sp.warming = opt_.keyCache > 1;
       }
@@ -533,7 +536,7 @@ class Server {
           for (int si : L.admitted) {
             if (asideIds.size() >= 16) break;
             Spec& sp = *specs_[(size_t)si];
-            if (!sp.longKey || sp.warming || sp.inSide || sp.finished || sp.noInstall ||
+            if (!cachesKeys(sp) || sp.warming || sp.inSide || sp.finished || sp.noInstall ||
                 L.eng.inAside(sp.engineId))
               continue;
             const int64_t at = (int64_t)sp.pkts.size() - L.eng.remaining(sp.engineId);

@@ -202,7 +202,8 @@ typedef struct {
                                   decoding it, and fill the caches in the background on side lanes nobody
                                   waits on; 2 also decode all of them at admission, before the stream's
                                   requests start (for the streams admitted at start, before the request
-                                  clock starts: a preparation step reported as prepare_s) (0: off) */
+                                  clock starts: a preparation step reported as prepare_s); 3 as 2 for every
+                                  stream (0: off) */
 } ebivgpu_serve_options;
 typedef struct {
   int64_t requests, frames, errors, seeks, loops, rounds;
