@@ -959,10 +959,10 @@ def main():
     ap.add_argument("--serve-max-frames", type=int, default=4, help="frames of one stream per serving round")
     ap.add_argument("--serve-ahead", type=int, default=6, help="frames decoded ahead of each stream's requests")
     ap.add_argument("--serve-key-lanes", type=int, default=3, help="side lanes for key frames with long chains")
-    ap.add_argument("--serve-key-cache", type=int, default=2,
+    ap.add_argument("--serve-key-cache", type=int, default=3,
                     help="1: streams with long key frames reinstall key frames they decoded before; 2: and decode "
                          "them all at admission, and the streams admitted at start fill their decode-ahead, "
-                         "before the request clock starts (reported as prepare_s)")
+                         "before the request clock starts (reported as prepare_s); 3: as 2 for every stream")
     ap.add_argument("--serve-seed", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the RGBA, ingest, alt-ref and analysis legs")
