@@ -22,7 +22,7 @@ def _streams():
 
 
 @pytest.mark.parametrize("lanes,side,long_key,cache", [(1, 1, 0, 0), (3, 1, 20, 0), (1, 3, 20, 0), (1, 2, 20, 1),
-                                                        (2, 2, 20, 2)])
+                                                        (2, 2, 20, 2), (1, 3, 0, 3)])
 def test_mix_equals_alone_with_seeks_and_loops(gpu_required, lanes, side, long_key, cache):
     # long_key 20: every stream's key frames (tiles of more than 20
     # macroblocks for most of them) take the side lanes; with cache 1 those
@@ -46,6 +46,8 @@ def test_mix_equals_alone_with_seeks_and_loops(gpu_required, lanes, side, long_k
         assert st["key_installs"] > 0
     if cache == 2:
         assert st["warmed_streams"] == 2  # the two streams whose tiles exceed 20 macroblocks
+    if cache == 3:
+        assert st["warmed_streams"] == len(streams) and st["prepare_s"] > 0
 
 
 def test_admission_respects_hbm_budget(gpu_required):
