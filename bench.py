@@ -843,6 +843,7 @@ def run_serve(args):
                           "collect_s": round(st["collect_s"], 3), "kernel_ms": round(st["kernel_ms"], 1),
                           "entropy_ms": round(st["entropy_ms"], 1), "recon_ms": round(st["recon_ms"], 1)},
         "side_lanes": args.serve_key_lanes, "key_cache": args.serve_key_cache, "key_installs": st["key_installs"],
+        "seek_shortcuts": st["seek_shortcuts"], "follow_rounds": st["follow_rounds"],
         "prepare_s": round(st["prepare_s"], 3),
         "unprepared": {"key_cache": 1, "requests": ust["requests"], "frames": ust["frames"],
                        "frames_per_s": round(ust["frames_per_s"], 2), "elapsed_s": round(ust["elapsed_s"], 3),

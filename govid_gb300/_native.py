@@ -53,7 +53,7 @@ class ServeStats(C.Structure):
                 ("main_round_s", C.c_double), ("idle_s", C.c_double), ("plan_s", C.c_double),
                 ("launch_s", C.c_double), ("collect_s", C.c_double), ("key_installs", C.c_int64),
                 ("warmed_streams", C.c_int64), ("warmup_s", C.c_double), ("aside_rounds", C.c_int64),
-                ("prepare_s", C.c_double)]
+                ("prepare_s", C.c_double), ("follow_rounds", C.c_int64), ("seek_shortcuts", C.c_int64)]
 
 
 class Frame(C.Structure):

@@ -73,7 +73,7 @@ struct ServeStatsC {
   int64_t readyAtArrival = 0, unserved = 0;
   double seekP50 = 0, seekP99 = 0;
   int64_t mainRounds = 0, sideRounds = 0, mainFrames = 0;
-  int64_t keyInstalls = 0, warmedStreams = 0, asideRounds = 0;
+  int64_t keyInstalls = 0, warmedStreams = 0, asideRounds = 0, followRounds = 0, seekShortcuts = 0;
   double warmupSec = 0;  // admission to first request of streams that decoded their key frames first
   double prepareSec = 0;  // key_cache 2: key frames of the streams admitted at start, before the first request
   double mainRoundSec = 0, idleSec = 0;  // decode thread: inside main rounds, waiting for work
@@ -275,6 +275,7 @@ class Server {
     bool warming = false;     // decoding its key frames into the cache before its requests start
     bool noInstall = false;   // an install failed: this stream decodes its key frames
     int warmRounds = 0;       // side rounds spent warming its key cache
+    bool keysCached = false;  // every key frame is in its key cache (seeks are answered from it at once)
     double admittedAt = 0;
     // decode thread
     uint64_t decEpoch = 0;
@@ -420,6 +421,7 @@ class Server {
       std::vector<int64_t> repoTo;
       std::vector<std::pair<int, uint64_t>> planned;
       std::vector<std::pair<int, int64_t>> installs;  // (spec, key frame) served from the key cache
+      std::vector<char> installSeek;                   // the install answers a seek
       std::vector<int> asideIds;
       std::vector<int64_t> asideKeys;
       int sideLane = -1;
@@ -464,6 +466,7 @@ class Server {
             }
             if (want < 0) {
               sp.warming = false;
+              sp.keysCached = !sp.noInstall;
               reposition.push_back(sp.engineId);
               repoTo.push_back(0);
               sp.startAt = now();
@@ -484,6 +487,7 @@ class Server {
             sp.decEpoch = sp.epoch;
             if (!sp.noInstall && L.eng.keyCached(sp.engineId, sp.seekTarget)) {
               installs.push_back({si, sp.seekTarget});
+              installSeek.push_back(1);
               sp.inflight = 1;
             } else {
               reposition.push_back(sp.engineId);
@@ -503,6 +507,7 @@ class Server {
           }
           if (sp.longKey && !sp.noInstall && isKey(sp, pos) && L.eng.keyCached(sp.engineId, pos)) {
             installs.push_back({si, pos});
+            installSeek.push_back(0);
             sp.inflight = 1;
             continue;
           }
@@ -577,6 +582,21 @@ class Server {
         std::vector<std::pair<int, uint64_t>> pl;
         for (const auto& in : installs) pl.push_back({in.first, specs_[(size_t)in.first]->decEpoch});
         publish(L, res, hashes, pl);
+        // The frame after an installed seek target goes to a side round now
+        // rather than to the next main round: the requests that follow a
+        // seek arrive within a frame interval.
+        for (size_t q = 0; q < installs.size(); q++) {
+          Spec& sp = *specs_[(size_t)installs[q].first];
+          if (!installSeek[q] || sideLane < 0 || !asideIds.empty() || kids.size() >= 64 || sp.inSide || sp.noInstall ||
+              sp.epoch != sp.decEpoch || L.eng.inAside(sp.engineId) ||
+              L.eng.remaining(sp.engineId) <= 0 || (sp.longKey && isKey(sp, installs[q].second + 1)))
+            continue;
+          kids.push_back(sp.engineId);
+          sp.inSide = true;
+          sp.inflight = 1;
+          L.sidePlanned[sideLane].push_back({installs[q].first, sp.epoch});
+          st_.followRounds++;
+        }
         cvRequest_.notify_all();
       }
       if (!asideIds.empty() && L.eng.launchAside(sideLane, asideIds, asideKeys) == kOK) {
@@ -645,6 +665,18 @@ class Server {
         sp.ready.clear();
         sp.inflight = 0;
         sp.consumePos = head.seekTo;
+        if (sp.keysCached && !opt_.record) {
+          // The key frame's image is already in the stream's key cache: the
+          // request is answered now (the decode thread installs the same
+          // image as the stream's state, and its copy of the frame is
+          // dropped). Record runs take the install path, which they hash.
+          Ready rd;
+          rd.frame = head.seekTo;
+          rd.keyframe = true;
+          rd.at = t;
+          sp.ready.push_back(rd);
+          st_.seekShortcuts++;
+        }
         head.seekTo = -2;  // applied; the request wants the key frame
         st_.seeks++;
         cvDecode_.notify_all();
@@ -844,6 +876,8 @@ int ebivgpu_server_run(ebivgpu_server* h, ebivgpu_serve_stats* out) {
   out->warmup_s = st.warmupSec;
   out->aside_rounds = st.asideRounds;
   out->prepare_s = st.prepareSec;
+  out->follow_rounds = st.followRounds;
+  out->seek_shortcuts = st.seekShortcuts;
   return r;
 }
 

@@ -222,6 +222,8 @@ typedef struct {
   double warmup_s;             /* summed admission-to-first-request time of the warmed streams */
   int64_t aside_rounds;        /* side-lane rounds that filled key caches in the background */
   double prepare_s;            /* key_cache 2: key frames of the streams admitted at start, before the first request */
+  int64_t follow_rounds;       /* side rounds that decoded the frame after an installed seek target */
+  int64_t seek_shortcuts;      /* seeks answered at once from a stream whose key frames are all cached */
 } ebivgpu_serve_stats;
 int ebivgpu_server_create(const ebivgpu_serve_options* o, ebivgpu_server** out);
 int ebivgpu_server_add_stream(ebivgpu_server* s, const uint8_t* const* pkts, const size_t* lens, int n, double fps,
