@@ -319,7 +319,8 @@ int Engine::setLookahead(int k) {
 // references, and the buffers a round claims; a pipelined engine of depth D
 // holds D more rounds' worth of claims.
 int Engine::poolSize(int ring, int k, int depth, bool side) {
-  return ring + (2 + depth) * k + 3 + depth + (side ? 2 : 0);  // a stream is in one side round at a time
+  // A stream is in one side round at a time: its frames and an override.
+  return ring + (2 + depth) * k + 3 + depth + (side ? kSideFrames + 1 : 0);
 }
 
 size_t Engine::footprint(int w, int h, int ring, int lookahead, int depth, int sideLanes) {
@@ -328,7 +329,9 @@ size_t Engine::footprint(int w, int h, int ring, int lookahead, int depth, int s
   const size_t yb = (size_t)stride64(g.padW()) * g.padH(), cb = (size_t)stride64(g.padCW()) * g.padCH();
   const size_t mbs = (size_t)g.mbCols * g.mbRows;
   return (size_t)poolSize(ring, lookahead, depth, side) * (yb + 2 * cb) +
-         ((size_t)(depth + 1) * (lookahead + 1) + 2 * (size_t)(side ? sideLanes : 0)) * Slot::bytes(mbs);
+         ((size_t)(depth + 1) * (lookahead + 1) +
+          (size_t)(std::min(kSideFrames, lookahead) + 1) * (size_t)(side ? sideLanes : 0)) *
+             Slot::bytes(mbs);
 }
 
 int Engine::addResidentStream(const uint8_t* const* pkts, const size_t* lens, int n, int ring, int* id) {
@@ -531,7 +534,7 @@ int Engine::configure(Stream& s, int w, int h) {
   for (size_t i = 0; i < s.slots.size(); i++) {
     const int within = (int)(i % (size_t)perParity);
     const bool sideSet = (int)(i / (size_t)perParity) >= mainSets();
-    if (within < (sideSet ? 1 : k) || within == perParity - 1) {
+    if (within < (sideSet ? std::min(kSideFrames, k) : k) || within == perParity - 1) {
       if (!s.slots[i].alloc(s.mbs)) return kErrDevice;
       nSlots++;
     }
@@ -1357,12 +1360,16 @@ bool Engine::anySideBusy() const {
   return false;
 }
 
-int Engine::launchSide(int lane, const std::vector<int>& ids) {
+int Engine::launchSide(int lane, const std::vector<int>& ids, const std::vector<int>* frames) {
   if (!side_ || lane < 0 || lane >= sideLanes_ || sideInflight_[lane]) return kErrArg;
   Round& R = rounds_[kSide + lane];
   R.parity = kSide + lane;
-  const std::vector<int> one(ids.size(), 1);  // one frame per stream: the lane's slot set holds one
-  if (planRound(ids, &one, R) || launchRecon(R)) {
+  // Frames per stream: the lane's slot set holds min(kSideFrames, lookahead).
+  const int cap = std::min(kSideFrames, lookahead_);
+  std::vector<int> n(ids.size(), 1);
+  if (frames)
+    for (size_t i = 0; i < n.size() && i < frames->size(); i++) n[i] = std::max(1, std::min(cap, (*frames)[i]));
+  if (planRound(ids, &n, R) || launchRecon(R)) {
     for (Job& j : R.jobs)
       if (j.status == kOK) j.status = kErrDevice;
     R.nDesc = 0;

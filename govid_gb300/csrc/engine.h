@@ -118,18 +118,20 @@ class Engine {
   bool pipelined() const { return pipeDepth_ > 0; }
   int pipeDepth() const { return pipeDepth_; }
   int drain(std::vector<RoundResult>* results);
-  // Side lanes (enabled before adding streams): rounds of one frame for each
-  // of a few streams (the serving loop sends key frames with long entropy
-  // chains there), each lane on its own pair of CUDA streams next to the
-  // main rounds and the other lanes, collected when done.  A stream in a
+  // Side lanes (enabled before adding streams): rounds of one or two frames
+  // for each of a few streams (the serving loop sends key frames with long
+  // entropy chains there, and the frames after a seek), each lane on its own
+  // pair of CUDA streams next to the main rounds and the other lanes,
+  // collected when done.  A stream in a
   // side round is left out of main rounds until collected; the caller sends
   // a stream to a side lane only between its main rounds.
   static constexpr int kSideLanes = 4;
+  static constexpr int kSideFrames = 2;  // frames of one stream a side round decodes at most
   int enableSideLane(int lanes = 1);  // 1 to kSideLanes
   int sideLanes() const { return sideLanes_; }
   int freeSideLane() const;  // a lane with no round in flight, or -1
   int freeSideLanes() const;  // how many lanes have no round in flight
-  int launchSide(int lane, const std::vector<int>& ids);
+  int launchSide(int lane, const std::vector<int>& ids, const std::vector<int>* frames = nullptr);
   bool sideBusy(int lane) const { return lane >= 0 && lane < kSideLanes && sideInflight_[lane]; }
   bool anySideBusy() const;
   bool sideReady(int lane);  // the lane's round is complete

@@ -25,6 +25,7 @@
 #include <mutex>
 #include <new>
 #include <random>
+#include <set>
 #include <thread>
 #include <vector>
 
@@ -422,6 +423,7 @@ class Server {
       std::vector<std::pair<int, uint64_t>> planned;
       std::vector<std::pair<int, int64_t>> installs;  // (spec, key frame) served from the key cache
       std::vector<char> installSeek;                   // the install answers a seek
+      std::set<int> followIds;                         // engine ids of follow-up side frames
       std::vector<int> asideIds;
       std::vector<int64_t> asideKeys;
       int sideLane = -1;
@@ -589,13 +591,15 @@ class Server {
           Spec& sp = *specs_[(size_t)installs[q].first];
           if (!installSeek[q] || sideLane < 0 || !asideIds.empty() || kids.size() >= 64 || sp.inSide || sp.noInstall ||
               sp.epoch != sp.decEpoch || L.eng.inAside(sp.engineId) ||
-              L.eng.remaining(sp.engineId) <= 0 || (sp.longKey && isKey(sp, installs[q].second + 1)))
+              L.eng.remaining(sp.engineId) <= 0 ||
+              (sp.longKey && (isKey(sp, installs[q].second + 1) || isKey(sp, installs[q].second + 2))))
             continue;
           kids.push_back(sp.engineId);
           sp.inSide = true;
-          sp.inflight = 1;
+          sp.inflight = (int)std::min<int64_t>(Engine::kSideFrames, L.eng.remaining(sp.engineId));
           L.sidePlanned[sideLane].push_back({installs[q].first, sp.epoch});
           st_.followRounds++;
+          followIds.insert(sp.engineId);
         }
         cvRequest_.notify_all();
       }
@@ -603,7 +607,10 @@ class Server {
         std::lock_guard<std::mutex> lk(mu_);
         st_.asideRounds++;
       }
-      if (!kids.empty() && L.eng.launchSide(sideLane, kids)) {
+      std::vector<int> kframes(kids.size(), 1);  // long key frames: one; frames after a seek: two
+      for (size_t q = 0; q < kids.size(); q++)
+        if (followIds.count(kids[q])) kframes[q] = Engine::kSideFrames;
+      if (!kids.empty() && L.eng.launchSide(sideLane, kids, &kframes)) {
         std::lock_guard<std::mutex> lk(mu_);
         decodeStatus_ = kErrDevice;
         stop_ = true;
