@@ -126,7 +126,7 @@ class Engine {
   // side round is left out of main rounds until collected; the caller sends
   // a stream to a side lane only between its main rounds.
   static constexpr int kSideLanes = 4;
-  static constexpr int kSideFrames = 2;  // frames of one stream a side round decodes at most
+  static constexpr int kSideFrames = 4;  // frames of one stream a side round decodes at most
   int enableSideLane(int lanes = 1);  // 1 to kSideLanes
   int sideLanes() const { return sideLanes_; }
   int freeSideLane() const;  // a lane with no round in flight, or -1
