@@ -239,6 +239,7 @@ Engine::~Engine() {
   if (dOne_) cudaFree(dOne_);
   for (auto& e : sideDone_)
     if (e) cudaEventDestroy(e);
+  if (mainDone_) cudaEventDestroy(mainDone_);
   if (streamC_) {
     cudaStreamSynchronize(streamC_);
     cudaStreamDestroy(streamC_);
@@ -1503,13 +1504,42 @@ size_t Engine::keyCacheBytes(int id) const {
   return streams_[(size_t)id]->cacheBytes;
 }
 
+int Engine::launchMain(const std::vector<int>& ids, const std::vector<int>* maxFrames) {
+  if (pipeDepth_ || mainInflight_) return kErrArg;
+  if (!mainDone_ && cudaEventCreateWithFlags(&mainDone_, cudaEventDisableTiming) != cudaSuccess) return kErrDevice;
+  Round& R = rounds_[0];
+  R.parity = 0;
+  const bool failed = planRound(ids, maxFrames, R) != 0 || launchRecon(R) != 0;
+  if (failed) {
+    for (Job& j : R.jobs)
+      if (j.status == kOK) j.status = kErrDevice;
+    R.nDesc = 0;
+  }
+  if (cudaEventRecord(mainDone_, reconStream(0)) != cudaSuccess) return kErrDevice;
+  mainInflight_ = true;
+  return failed ? -1 : kOK;
+}
+
+bool Engine::mainReady() { return mainInflight_ && cudaEventQuery(mainDone_) != cudaErrorNotReady; }
+
+int Engine::collectMain(std::vector<RoundResult>* results) {
+  if (!mainInflight_) return 0;
+  const int n = collectRound(rounds_[0], results);
+  mainInflight_ = false;
+  return n;
+}
+
 int Engine::installKey(int id, int64_t index, std::vector<RoundResult>* results) {
-  if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id]) return kErrArg;
+  if (id < 0 || id >= (int)streams_.size() || !streams_[(size_t)id] || pipeDepth_) return kErrArg;
   Stream& s = *streams_[(size_t)id];
   const auto it = s.keyCache.find(index);
-  if (it == s.keyCache.end() || s.inSide || s.hasProv || !s.ready) return kErrArg;
-  for (int q = 0; q < kSide; q++)
-    if (!s.roundBufs[q].empty()) return kErrArg;  // a main round in flight holds this stream
+  if (it == s.keyCache.end() || s.inSide || !s.ready) return kErrArg;
+  // A main round in flight may hold this stream: its frames there are
+  // discarded at collection (the stream's epoch moves on) and its buffers
+  // stay untouched until then.
+  bool inMain = false;
+  for (int q = 0; q < kSide; q++) inMain = inMain || !s.roundBufs[q].empty();
+  if (s.hasProv && !inMain) return kErrArg;
   std::vector<char> busy(s.pool.size(), 0);
   if (s.ref >= 0) busy[(size_t)s.ref] = 1;
   if (s.golden >= 0) busy[(size_t)s.golden] = 1;
@@ -1530,6 +1560,10 @@ int Engine::installKey(int id, int64_t index, std::vector<RoundResult>* results)
     return kErrDevice;
   // The state Decode leaves after this key frame: references, table history,
   // the next packet, and the frame as the newest output.
+  if (inMain) {
+    s.epoch++;
+    s.hasProv = false;
+  }
   s.ref = b;
   s.golden = g;
   s.hist = it->second.hist;

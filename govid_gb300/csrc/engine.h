@@ -143,6 +143,15 @@ class Engine {
   // installKey puts the stream in the state decoding that key frame leaves
   // (references, table history, next packet) without decoding it, and
   // returns the frame as a result; the stream must have no round in flight.
+  // The synchronous engine's round in two halves (serving): launchMain plans
+  // and launches it, mainReady() says when its work is done, collectMain
+  // returns its results.  While it runs, installKey may take a stream of the
+  // round (the round's frames of that stream are then discarded) and side
+  // rounds run beside it.
+  int launchMain(const std::vector<int>& ids, const std::vector<int>* maxFrames);
+  bool mainBusy() const { return mainInflight_; }
+  bool mainReady();
+  int collectMain(std::vector<RoundResult>* results);
   int setKeyCache(int id, bool on);
   bool keyCached(int id, int64_t index) const;
   size_t keyCacheBytes(int id) const;
@@ -249,6 +258,8 @@ class Engine {
   int pipeDepth_ = 0;
   bool side_ = false;
   int sideLanes_ = 0;
+  bool mainInflight_ = false;
+  cudaEvent_t mainDone_ = nullptr;
   bool sideInflight_[kSideLanes] = {};
   std::vector<std::unique_ptr<Stream>> streams_;
   std::unique_ptr<Round[]> rounds_;  // by parity

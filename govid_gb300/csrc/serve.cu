@@ -216,9 +216,6 @@ class Server {
     st.seekP99 = pctl(seekLat_, 0.99);
     st.framesPerSec = st.elapsed > 0 ? st.frames / st.elapsed : 0;
     for (auto& L : lanes_) {
-      st.planSec += L->eng.planSeconds();
-      st.launchSec += L->eng.launchSeconds();
-      st.collectSec += L->eng.collectSeconds();
       st.kernelMs += L->eng.kernelMillis();
       st.entropyMs += L->eng.entropyMillis();
       st.reconMs += L->eng.reconMillis();
@@ -277,6 +274,7 @@ class Server {
     bool noInstall = false;   // an install failed: this stream decodes its key frames
     int warmRounds = 0;       // side rounds spent warming its key cache
     bool keysCached = false;  // every key frame is in its key cache (seeks are answered from it at once)
+    bool inMain = false;      // frames of it are in the main round in flight
     double admittedAt = 0;
     // decode thread
     uint64_t decEpoch = 0;
@@ -293,6 +291,8 @@ class Server {
     std::vector<int> admitted;  // spec indices
     std::vector<int> specOf;    // engine stream id -> spec index
     std::vector<std::pair<int, uint64_t>> sidePlanned[Engine::kSideLanes];
+    std::vector<std::pair<int, uint64_t>> mainPlanned;  // (spec, epoch) of the main round in flight
+    double mainLaunchedAt = 0;
   };
 
   int ringOf() const { return std::max(opt_.ring, ahead_ + 2); }
@@ -413,11 +413,33 @@ class Server {
     }
   }
 
+  // Collects the main round when its work is done (decode thread).
+  bool collectMainIfReady(Lane& L, std::vector<RoundResult>& res, std::vector<uint64_t>& hashes) {
+    if (!L.eng.mainBusy() || !L.eng.mainReady()) return false;
+    res.clear();
+    const double c0 = nowSec();
+    L.eng.collectMain(&res);
+    const double c1 = nowSec();
+    hashResults(L, res, &hashes);
+    std::lock_guard<std::mutex> lk(mu_);
+    st_.rounds++;
+    st_.mainRounds++;
+    st_.mainFrames += (int64_t)res.size();
+    st_.mainRoundSec += c1 - L.mainLaunchedAt;
+    st_.collectSec += c1 - c0;
+    publish(L, res, hashes, L.mainPlanned);
+    for (const auto& pl : L.mainPlanned) specs_[(size_t)pl.first]->inMain = false;
+    L.mainPlanned.clear();
+    cvRequest_.notify_all();
+    return true;
+  }
+
   void decodeLoop(Lane& L) {
     cudaSetDevice(device_);
     std::vector<RoundResult> res;
     std::vector<uint64_t> hashes;
     for (;;) {
+      collectMainIfReady(L, res, hashes);
       std::vector<int> ids, counts, kids, reposition;
       std::vector<int64_t> repoTo;
       std::vector<std::pair<int, uint64_t>> planned;
@@ -436,7 +458,7 @@ class Server {
         // it (freeing synchronises the device, which would stall every lane).
         for (size_t k = 0; k < L.admitted.size() && !waiting_.empty();) {
           Spec& sp = *specs_[(size_t)L.admitted[k]];
-          if (sp.finished && !sp.inSide && !L.eng.inAside(sp.engineId)) {
+          if (sp.finished && !sp.inSide && !sp.inMain && !L.eng.inAside(sp.engineId)) {
             L.eng.removeStream(sp.engineId);
             used_ -= sp.footprint;
             sp.done = true;
@@ -449,10 +471,11 @@ class Server {
         }
         if (removed) admit(&L, false);
         sideLane = L.eng.freeSideLane();  // the long key frames found now go there
+        const bool mainFree = !L.eng.mainBusy();
         for (int si : L.admitted) {
           Spec& sp = *specs_[(size_t)si];
           if (sp.inSide || sp.finished) continue;
-          if (sp.warming) {
+          if (sp.warming && !sp.inMain) {
             // Admission: each key frame once through a side lane into the
             // cache, then back to the first frame and the requests start.
             int64_t want = -1;
@@ -486,17 +509,21 @@ class Server {
             continue;
           }
           if (sp.decEpoch != sp.epoch) {  // a seek: restart at its key frame
-            sp.decEpoch = sp.epoch;
             if (!sp.noInstall && L.eng.keyCached(sp.engineId, sp.seekTarget)) {
+              // (even while the main round in flight holds the stream: its
+              // frames there are discarded)
+              sp.decEpoch = sp.epoch;
               installs.push_back({si, sp.seekTarget});
               installSeek.push_back(1);
               sp.inflight = 1;
-            } else {
+            } else if (!sp.inMain) {
+              sp.decEpoch = sp.epoch;
               reposition.push_back(sp.engineId);
               repoTo.push_back(sp.seekTarget);
             }
             continue;  // planned next time round, after the engine moved
           }
+          if (sp.inMain || sp.warming) continue;  // its frames are in the main round in flight
           const int room = ahead_ - (int)sp.ready.size() - sp.inflight;
           if (room <= 0) continue;
           int64_t pos = (int64_t)sp.pkts.size() - L.eng.remaining(sp.engineId);
@@ -524,6 +551,7 @@ class Server {
             }
             continue;
           }
+          if (!mainFree) continue;
           int n = std::min(room, lookahead_);
           n = (int)std::min<int64_t>(n, (int64_t)sp.pkts.size() - pos);
           if (sp.longKey) {  // stop before the next long key frame
@@ -533,6 +561,7 @@ class Server {
           ids.push_back(sp.engineId);
           counts.push_back(n);
           sp.inflight = n;
+          sp.inMain = true;
           planned.push_back({si, sp.epoch});
         }
         // A side lane nobody waits on fills key caches in the background (one
@@ -543,7 +572,7 @@ class Server {
           for (int si : L.admitted) {
             if (asideIds.size() >= 16) break;
             Spec& sp = *specs_[(size_t)si];
-            if (!cachesKeys(sp) || sp.warming || sp.inSide || sp.finished || sp.noInstall ||
+            if (!cachesKeys(sp) || sp.warming || sp.inSide || sp.inMain || sp.finished || sp.noInstall ||
                 L.eng.inAside(sp.engineId))
               continue;
             const int64_t at = (int64_t)sp.pkts.size() - L.eng.remaining(sp.engineId);
@@ -558,12 +587,13 @@ class Server {
             asideKeys.push_back(want);
           }
         }
-        if (ids.empty() && kids.empty() && reposition.empty() && installs.empty() && asideIds.empty() &&
-            !L.eng.anySideBusy()) {
+        if (ids.empty() && kids.empty() && reposition.empty() && installs.empty() && asideIds.empty()) {
+          const bool gpuBusy = L.eng.mainBusy() || L.eng.anySideBusy();
           const double w0 = nowSec();
-          cvDecode_.wait_for(lk, std::chrono::microseconds(500));
-          st_.idleSec += nowSec() - w0;
-          continue;
+          // GPU work in flight: poll it often; none: wait for requests.
+          cvDecode_.wait_for(lk, std::chrono::microseconds(gpuBusy ? 50 : 500));
+          if (!gpuBusy) st_.idleSec += nowSec() - w0;
+          if (!gpuBusy) continue;
         }
       }
       for (size_t k = 0; k < reposition.size(); k++) L.eng.seekStream(reposition[k], repoTo[k]);
@@ -618,25 +648,19 @@ class Server {
         break;
       }
       if (!ids.empty()) {
-        res.clear();
         const double r0 = nowSec();
-        const int rc = L.eng.roundFor(ids, &res, &counts);
+        const int rc = L.eng.launchMain(ids, &counts);
         const double r1 = nowSec();
-        if (rc < 0) {
-          std::lock_guard<std::mutex> lk(mu_);
+        std::lock_guard<std::mutex> lk(mu_);
+        L.mainPlanned = planned;
+        L.mainLaunchedAt = r0;
+        st_.planSec += r1 - r0;
+        if (rc != kOK && !L.eng.mainBusy()) {
           decodeStatus_ = kErrDevice;
           stop_ = true;
           cvRequest_.notify_all();
           break;
         }
-        hashResults(L, res, &hashes);
-        std::lock_guard<std::mutex> lk(mu_);
-        st_.rounds++;
-        st_.mainRounds++;
-        st_.mainFrames += (int64_t)res.size();
-        st_.mainRoundSec += r1 - r0;
-        publish(L, res, hashes, planned);
-        cvRequest_.notify_all();
       }
       bool collected = false;
       for (int l = 0; l < Engine::kSideLanes; l++) {
@@ -653,8 +677,11 @@ class Server {
         cvRequest_.notify_all();
         collected = true;
       }
-      if (ids.empty() && !collected && L.eng.anySideBusy())
-        std::this_thread::sleep_for(std::chrono::microseconds(100));
+      (void)collected;
+    }
+    if (L.eng.mainBusy()) {
+      res.clear();
+      L.eng.collectMain(&res);
     }
     for (int l = 0; l < Engine::kSideLanes; l++) {
       res.clear();
