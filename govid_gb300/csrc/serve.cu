@@ -508,6 +508,7 @@ class Server {
             }
             continue;
           }
+          int64_t pos = -1;  // where the stream decodes next (after a reposition made below)
           if (sp.decEpoch != sp.epoch) {  // a seek: restart at its key frame
             if (!sp.noInstall && L.eng.keyCached(sp.engineId, sp.seekTarget)) {
               // (even while the main round in flight holds the stream: its
@@ -516,23 +517,24 @@ class Server {
               installs.push_back({si, sp.seekTarget});
               installSeek.push_back(1);
               sp.inflight = 1;
-            } else if (!sp.inMain) {
-              sp.decEpoch = sp.epoch;
-              reposition.push_back(sp.engineId);
-              repoTo.push_back(sp.seekTarget);
+              continue;
             }
-            continue;  // planned next time round, after the engine moved
+            if (sp.inMain) continue;  // once the round in flight is collected
+            sp.decEpoch = sp.epoch;
+            reposition.push_back(sp.engineId);  // applied before this pass launches anything
+            repoTo.push_back(sp.seekTarget);
+            pos = sp.seekTarget;
           }
           if (sp.inMain || sp.warming) continue;  // its frames are in the main round in flight
           const int room = ahead_ - (int)sp.ready.size() - sp.inflight;
           if (room <= 0) continue;
-          int64_t pos = (int64_t)sp.pkts.size() - L.eng.remaining(sp.engineId);
+          if (pos < 0) pos = (int64_t)sp.pkts.size() - L.eng.remaining(sp.engineId);
           if (pos >= (int64_t)sp.pkts.size()) {
             if (!sp.loop) continue;
             reposition.push_back(sp.engineId);  // looping: on from the first frame
             repoTo.push_back(0);
             st_.loops++;
-            continue;
+            pos = 0;
           }
           if (sp.longKey && !sp.noInstall && isKey(sp, pos) && L.eng.keyCached(sp.engineId, pos)) {
             installs.push_back({si, pos});
@@ -568,7 +570,8 @@ class Server {
         // lane stays free for key frames a stream waits for): for up to 16
         // streams, the first key frame not yet cached after where each stream
         // decodes now.
-        if (opt_.keyCache > 0 && kids.empty() && sideLane >= 0 && L.eng.freeSideLanes() >= 2) {
+        // (Only when no main round runs: the background rounds would slow it.)
+        if (opt_.keyCache > 0 && mainFree && kids.empty() && sideLane >= 0 && L.eng.freeSideLanes() >= 2) {
           for (int si : L.admitted) {
             if (asideIds.size() >= 16) break;
             Spec& sp = *specs_[(size_t)si];
