@@ -8,11 +8,11 @@
 // source.go:84-187), batching all streams' next frames into shared rounds;
 // requests are served in order from the decoded frames as they arrive.  A
 // seek request moves the stream to a key frame (ebiv/reader.go:222-238
-// semantics: decoding restarts there exactly); a looping stream continues
-// from its first frame at the end.  Streams are admitted while the sum of
-// their HBM footprints (frame pool + scratch + packets) fits the budget; a
-// finished stream releases its memory and the next waiting stream is
-// admitted.
+// semantics: decoding restarts there exactly, from the stream's key-frame
+// cache when it holds that frame); a looping stream continues from its first
+// frame at the end.  Streams are admitted while the sum of their HBM
+// footprints (frame pool, scratch, packets, key caches) fits the budget; a
+// finished stream releases its memory when a waiting stream needs it.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -81,17 +81,32 @@ struct ServeStatsC {
   double planSec = 0, launchSec = 0, collectSec = 0;  // inside main rounds: host planning, launches, wait
 };
 
-// Two threads.  The decode thread owns the engine: it keeps every admitted
-// stream up to `decodeAhead` frames ahead of its requests, in rounds of up
-// to `maxFramesPerRound` frames per stream (their entropy stages in one
-// launch); key frames whose tiles carry long entropy chains go to the
-// engine's side lane so they never hold up a round.  It also admits streams
-// (HBM budget) and removes finished ones.  The request thread generates
-// each stream's Poisson requests, serves them in order from the decoded
-// frames, and applies seeks (a new epoch: frames decoded for the old
-// position are dropped, decoding restarts at the key frame).  A request's
-// latency runs from its arrival to the moment its frame is decoded and
-// handed out (zero wait when the frame was ready before it was asked for).
+// Threads: one decode thread per decode lane (an engine of its own; one by
+// default) and one request thread.
+//
+// * A decode thread keeps every stream of its lane up to `decodeAhead` frames
+//   ahead of its requests, in main rounds of up to `maxFramesPerRound` frames
+//   per stream (their entropy stages in one launch). It launches a main round
+//   and collects it when the GPU is done, handling seeks and side rounds
+//   meanwhile.
+// * Key frames whose tiles carry long entropy chains go to the engine's side
+//   lanes, so they never hold up a main round. So do the frames after a seek
+//   target, which need to arrive within a frame interval.
+// * With a key cache, a stream keeps its decoded key frames (image, golden,
+//   table history) and installs one at a seek instead of decoding it; key
+//   frames may be decoded into the caches ahead of time (at admission, or in
+//   side rounds nobody waits on).
+// * A decode thread also admits streams (HBM budget) and removes finished
+//   ones when a waiting stream needs the memory.
+// * The request thread generates each stream's Poisson requests, serves them
+//   in order from the decoded frames, and applies seeks: a new epoch drops the
+//   frames decoded for the old position, and decoding restarts at the key
+//   frame. A stream whose key frames are all cached has its seek answered from
+//   the cache at once.
+//
+// A request's latency runs from its arrival to the moment its frame is
+// decoded and handed out: zero wait when the frame was ready before it was
+// asked for.
 class Server {
  public:
   explicit Server(const ServeOptionsC& o) : opt_(o), rng_(o.seed) {
