@@ -103,6 +103,7 @@ def lib() -> C.CDLL:
     _sig(L, "ebivgpu_frame_rgba_pooled", C.c_void_p, P, I)
     _sig(L, "ebivgpu_status_string", C.c_char_p, I)
     _sig(L, "ebivgpu_device_available", I)
+    _sig(L, "ebivgpu_abi_sizes", I, C.POINTER(S), I)
     # batch
     _sig(L, "ebivgpu_batch_create", I, PP)
     _sig(L, "ebivgpu_batch_destroy", None, P)

@@ -190,6 +190,14 @@ struct ebivgpu_codec {
 
 extern "C" {
 
+int ebivgpu_abi_sizes(size_t* sizes, int n) {
+  const size_t v[] = {sizeof(ebivgpu_frame), sizeof(ebivgpu_plane_view), sizeof(ebivgpu_serve_options),
+                      sizeof(ebivgpu_serve_stats), sizeof(ebivgpu_source_frame)};
+  const int k = (int)(sizeof(v) / sizeof(v[0]));
+  for (int i = 0; i < n && i < k && sizes; i++) sizes[i] = v[i];
+  return k;
+}
+
 int ebivgpu_device_available(void) {
   int n = 0;
   return cudaGetDeviceCount(&n) == cudaSuccess && n > 0 ? 1 : 0;

@@ -394,6 +394,11 @@ int64_t ebivgpu_source_decoded(ebivgpu_source* s);
 int64_t ebivgpu_source_duration(ebivgpu_source* s);
 int ebivgpu_source_lookahead(ebivgpu_source* s);
 
+/* sizeof of the public structs, for bindings to check their layouts:
+ * ebivgpu_frame, ebivgpu_plane_view, ebivgpu_serve_options,
+ * ebivgpu_serve_stats, ebivgpu_source_frame (the first n); returns 5. */
+int ebivgpu_abi_sizes(size_t* sizes, int n);
+
 /* Non-zero when a CUDA device is usable from this process. */
 int ebivgpu_device_available(void);
 

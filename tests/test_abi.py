@@ -30,3 +30,13 @@ def test_device_probe_and_status_strings():
     L = _native.lib()
     assert L.ebivgpu_device_available() in (0, 1)
     assert L.ebivgpu_status_string(1) == b"ebiv: corrupt stream"
+
+
+def test_struct_layouts_match_the_header():
+    # The ctypes mirrors of the public structs have the C sizes (a field
+    # added on one side only would shift every later field).
+    L = _native.lib()
+    sizes = (C.c_size_t * 5)()
+    assert L.ebivgpu_abi_sizes(sizes, 5) == 5
+    mirrors = [_native.Frame, _native.PlaneView, _native.ServeOptions, _native.ServeStats, _native.SourceFrame]
+    assert [C.sizeof(m) for m in mirrors] == list(sizes)
