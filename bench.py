@@ -63,7 +63,7 @@ METRIC = "EBIV 1080p frames/s (batched vs per-stream on GPU, bit-exact; p99 ms; 
 # entropy, inter and intra kernels of a pipelined 32-frame-lookahead pass
 # (ncu dram__bytes_read.sum + dram__bytes_write.sum over every launch of a
 # 60-frame prefix decoded twice, per frame; profiles/decode_1080p_launches_traffic.md).
-DRAM_BYTES_PER_FRAME = 6.42e6
+DRAM_BYTES_PER_FRAME = 6.22e6
 
 
 def log(*a):
