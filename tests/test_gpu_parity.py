@@ -63,6 +63,25 @@ def test_tiling_grids(gpu_required, grid):
     _check(cont, 256, 160, rec)
 
 
+@pytest.mark.parametrize("split", [(10, 8, 4, 4), (5, 5, 8, 8), (1, 1, 2, 2)])
+def test_tile_grids_larger_than_the_frame(gpu_required, split):
+    # TestTileGridSplit's shapes (ebiv/tile_test.go:12-45): grids clamp to the
+    # macroblock grid; a header asking for more tiles than that is corrupt on
+    # the GPU exactly where the oracle says so (ebiv/decode_intra.go:60-63).
+    from test_oracle_known_answers import _with_tile_counts
+
+    mbc, mbr, cols, rows = split
+    w, h = 16 * mbc, 16 * mbr
+    cont, _, rec = encode_gen(w, h, 3, ebiv.synth_pan, intra=20, gop=3, tiles=(cols, rows))
+    _check(cont, w, h, rec)
+    pkts = [p.data for p in ebiv.Reader(cont).packets()]
+    over = [_with_tile_counts(p, min(cols, mbc) + 1, min(rows, mbr)) for p in pkts]
+    want = ebiv_oracle.decode_all(over)
+    got = gpu_decode_all(over)
+    assert [g[0] for g in got] == [x[0] for x in want]
+    assert want[0][0] == ebiv.ErrCorrupt.status
+
+
 def test_golden_flash(gpu_required):
     # TestGoldenRefFlashingSequence: 128x96, 9 frames, q16, gop 9
     cont, _, rec = encode_gen(128, 96, 9, flash_gen, intra=16, gop=9)

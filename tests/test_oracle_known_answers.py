@@ -264,3 +264,40 @@ def test_key_frames_from_chosen_levels_decode_in_the_oracle():
     assert st == 0 and ebiv_oracle.wide_residuals() > 0
     with pytest.raises(ebiv.ErrArgument):
         ebiv.encode_key_from_levels(w, h, 22, 0, small[:-1])
+
+
+# TestTileGridSplit's shapes (ebiv/tile_test.go:12-45): (mbCols, mbRows, cols, rows),
+# grids larger than the frame included (newTileGrid clamps, ebiv/frame.go:87-102).
+TILE_SPLITS = [(10, 8, 1, 1), (10, 8, 3, 2), (10, 8, 4, 4), (5, 5, 8, 8), (1, 1, 2, 2)]
+
+
+def _with_tile_counts(pkt, cols, rows):
+    """The packet with its coded header's one-byte tile-count varints replaced
+    (codedHeader.appendTo, ebiv/frame.go:187-194)."""
+    from govid_gb300 import ebiv
+
+    b = ebiv.parse_frame_header(pkt)["body_offset"]
+    assert pkt[b + 1] < 128 and pkt[b + 2] < 128 and cols < 128 and rows < 128
+    return pkt[: b + 1] + bytes([cols, rows]) + pkt[b + 3:]
+
+
+@pytest.mark.parametrize("split", TILE_SPLITS)
+def test_tile_grid_split_decodes_and_clamps(split):
+    # The encoder writes the clamped grid; the oracle decodes every grid to the
+    # encoder's reconstruction. A header asking for more tiles than the
+    # macroblock grid holds is corrupt: parsePayload reads cols*rows tile
+    # records, then decodeCoded's grid check (ebiv/decode_intra.go:60-63) fails.
+    from govid_gb300 import ebiv
+    from helpers import encode_gen
+
+    mbc, mbr, cols, rows = split
+    cont, _, rec = encode_gen(16 * mbc, 16 * mbr, 3, ebiv.synth_pan, intra=20, gop=3, tiles=(cols, rows))
+    pkts = [p.data for p in ebiv.Reader(cont).packets()]
+    for p in pkts:
+        b = ebiv.parse_frame_header(p)["body_offset"]
+        assert (p[b + 1], p[b + 2]) == (min(cols, mbc), min(rows, mbr))
+    got = ebiv_oracle.decode_all(pkts)
+    assert [g[0] for g in got] == [0, 0, 0]
+    assert [g[1] for g in got] == rec
+    over = ebiv_oracle.decode_all([_with_tile_counts(p, min(cols, mbc) + 1, min(rows, mbr)) for p in pkts])
+    assert over[0][0] == ebiv.ErrCorrupt.status
