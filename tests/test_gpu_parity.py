@@ -104,6 +104,24 @@ def test_odd_sizes(gpu_required, size):
     _check(cont, w, h, rec)
 
 
+@pytest.mark.parametrize("size", [(16, 16), (17, 15), (64, 48), (31, 47), (160, 90)])
+def test_coded_round_trip_sizes(gpu_required, size):
+    # TestCodedRoundTripSizes: q16, gop 3, 3 frames
+    w, h = size
+    cont, _, rec = encode_gen(w, h, 3, ebiv.synth_frame, intra=16, gop=3)
+    _check(cont, w, h, rec)
+
+
+def test_scene_cut_clip(gpu_required):
+    # TestSceneCutKeyframes: 128x96, 30 frames, a hard cut at 12, gop 20 (key
+    # frames at 0 and 12; the next one would be frame 32)
+    cut = 12
+    cont, _, rec = encode_gen(128, 96, 30, lambda w, h, i: ebiv.synth_frame(w, h, 1 if i < cut else 9),
+                              intra=16, gop=20)
+    assert [e.keyframe for e in ebiv.Reader(cont).index()].count(True) == 2
+    _check(cont, 128, 96, rec)
+
+
 def test_raw_frames(gpu_required):
     # TestRawRoundTrip: lossless raw key frames decode to the source
     cont, srcs, _ = encode_gen(64, 48, 3, ebiv.synth_frame)
