@@ -1,5 +1,5 @@
 """The CPU reference of the learned MV proposer's net (oracle/mvnet_ref.py)
-checked against central finite differences in float64, so it can judge the
+checked against central finite differences in float64, so it can check the
 GPU backward kernels."""
 import numpy as np
 
