@@ -5,14 +5,22 @@
 
 namespace ebiv {
 
-// frameIndexAt — ebiv/format.go:263-275
+// frameIndexAt — ebiv/format.go:263-275.  The estimate is within a frame of
+// the answer unless t * fpsNum wraps (Go int64 arithmetic), where the
+// reference's correction walk can run for ~2^63 steps; a walk that needs
+// 2^20 steps or more gives -1 instead, as the GPU seek does.
 int64_t FileHeader::frameIndexAt(int64_t t) const {
   if (t <= 0) return 0;
   const int64_t num = (int64_t)((uint64_t)t * (uint64_t)fpsNum);
   const int64_t den = (int64_t)((uint64_t)fpsDen * 1000000000ull);
   int64_t i = num / den;
-  while (frameTime(i + 1) <= t) i++;
-  while (i > 0 && frameTime(i) > t) i--;
+  int steps = 0;
+  while (frameTime(i + 1) <= t)
+    if (++steps >= kSeekWalkLimit) return -1;
+    else i++;
+  while (i > 0 && frameTime(i) > t)
+    if (++steps >= kSeekWalkLimit) return -1;
+    else i--;
   return i;
 }
 
@@ -83,8 +91,12 @@ int Reader::readIndex() {
   const uint64_t offset = rd64(footer);
   const uint32_t count = rd32(footer + 8);
   const uint32_t want = rd32(footer + 12);
+  // An offset past the file fails in the reference too (the bounds check, or
+  // the seek to a wrapped negative position); checking it first keeps the sum
+  // below from overflowing.
+  if (offset < (uint64_t)kFileHeaderSize || offset > (uint64_t)size) return kErrCorrupt;
   const int64_t end = (int64_t)offset + (int64_t)count * kIndexEntrySize;
-  if (offset < (uint64_t)kFileHeaderSize || offset > (uint64_t)size || end != size - kFooterSize) return kErrCorrupt;
+  if (end != size - kFooterSize) return kErrCorrupt;
   const uint8_t* buf = data_.data() + offset;
   if (crc32IEEE(buf, (size_t)count * kIndexEntrySize) != want) return kErrCorrupt;
   index_.resize(count);
@@ -125,7 +137,8 @@ int Reader::scanFrames() {
 int Reader::nextPacket(const uint8_t** data, size_t* n, int64_t* ts, bool* key) {
   if (closed_ || next_ >= (int)index_.size()) return kErrEOF;
   const IndexEntry& e = index_[(size_t)next_];
-  *data = data_.data() + e.offset + kFrameRecordSize;
+  if (!e.readable()) return kErrIO;  // reader.go:203-205: the seek fails, next stays
+  *data = data_.data() + e.payloadAt();
   *n = e.size;
   if (ts) *ts = hdr_.frameTime(next_);
   if (key) *key = e.keyframe;
@@ -135,8 +148,10 @@ int Reader::nextPacket(const uint8_t** data, size_t* n, int64_t* ts, bool* key) 
 
 int Reader::packet(int i, const uint8_t** data, size_t* n) const {
   if (i < 0 || i >= (int)index_.size()) return kErrArg;
-  *data = data_.data() + index_[(size_t)i].offset + kFrameRecordSize;
-  *n = index_[(size_t)i].size;
+  const IndexEntry& e = index_[(size_t)i];
+  if (!e.readable()) return kErrIO;
+  *data = data_.data() + e.payloadAt();
+  *n = e.size;
   return kOK;
 }
 
@@ -144,6 +159,7 @@ int Reader::packet(int i, const uint8_t** data, size_t* n) const {
 int Reader::seek(int64_t t, int64_t* landed) {
   if (closed_ || index_.empty()) return kErrEOF;
   int64_t target = hdr_.frameIndexAt(t);
+  if (target < 0) return kErrCorrupt;  // a frame rate the walk cannot settle
   if (target >= (int64_t)index_.size()) target = (int64_t)index_.size() - 1;
   target = keyframeBefore((int)target);
   next_ = (int)target;

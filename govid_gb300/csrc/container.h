@@ -25,13 +25,22 @@ struct FileHeader {
     const int64_t p = (int64_t)((uint64_t)i * (uint64_t)fpsDen * 1000000000ull);
     return p / (int64_t)fpsNum;
   }
+  // -1 when the correction walk needs kSeekWalkLimit steps or more.
   int64_t frameIndexAt(int64_t t) const;
+  static constexpr int kSeekWalkLimit = 1 << 20;
 };
 
 struct IndexEntry {
   uint64_t offset = 0;
   uint32_t size = 0;
   bool keyframe = false;
+  // Where the payload is read: offset + the record header, in Go's wrapping
+  // int64 (ebiv/reader.go:203).  validateEntry's uint64 sum can wrap, so an
+  // index entry may carry an offset near 2^64: the reference then seeks to a
+  // negative position and NextPacket fails (kErrIO here), or, for the eight
+  // offsets that wrap to 0..7, reads from there.
+  int64_t payloadAt() const { return (int64_t)(offset + 8u); }
+  bool readable() const { return payloadAt() >= 0; }
 };
 
 // Parsed per-packet header (ebiv/format.go:333-409).
@@ -51,9 +60,10 @@ class Reader {
   const FileHeader& header() const { return hdr_; }
   const std::vector<IndexEntry>& index() const { return index_; }
   int frameCount() const { return (int)index_.size(); }
-  // NextPacket — returns kErrEOF at the end.
+  // NextPacket — returns kErrEOF at the end, kErrIO (without advancing) for
+  // an entry whose payload position is negative.
   int nextPacket(const uint8_t** data, size_t* n, int64_t* ts, bool* key);
-  // Packet i without moving the read position.
+  // Packet i without moving the read position (kErrIO when unreadable).
   int packet(int i, const uint8_t** data, size_t* n) const;
   // Seek — positions at the last key frame at or before t; returns its time.
   int seek(int64_t t, int64_t* landed);

@@ -325,8 +325,17 @@ int ebivgpu_container_info(ebivgpu_container* c, int64_t* info6) {
   return kOK;
 }
 
+// An index entry whose payload lies outside the container: validateEntry's
+// uint64 sum (ebiv/reader.go:115-123) wraps for offsets near 2^64, and the
+// reference then fails NextPacket with a seek to a negative position
+// (reader.go:203-205).  Offsets that wrap to 0..7 stay inside the file.
+static bool entryReadable(const ebivgpu_container* c, size_t i) {
+  return c->off[i] <= c->n && c->size[i] <= c->n - c->off[i];
+}
+
 int ebivgpu_container_entry(ebivgpu_container* c, int i, uint64_t* payload_offset, uint32_t* size, int* keyframe) {
   if (!c || i < 0 || i >= (int)c->off.size()) return kErrArg;
+  if (!entryReadable(c, (size_t)i)) return kErrIO;
   if (payload_offset) *payload_offset = c->off[(size_t)i];
   if (size) *size = c->size[(size_t)i];
   if (keyframe) *keyframe = c->key[(size_t)i];
@@ -353,6 +362,11 @@ int ebivgpu_batch_add_container(ebivgpu_batch* b, ebivgpu_container* c, int ring
   if (!b || !c || !stream_id) return kErrArg;
   Engine* e = batchEngine(b);
   if (!e) return kErrArg;
+  // The stream reads every packet in place, ahead of its frame: a container
+  // with an unreadable entry is refused here (the reference reports it when
+  // playback reaches that frame).
+  for (size_t i = 0; i < c->off.size(); i++)
+    if (!entryReadable(c, i)) return kErrIO;
   return e->addContainerStream(c->host, c->dev, c->off.data(), c->size.data(), (int)c->off.size(), ring, stream_id);
 }
 

@@ -24,7 +24,11 @@
 //     blocking or reporting "not ready";
 //   * a consumer holding so many frames that none can be decoded (more than
 //     depth + lookahead + 4) gets kErrArg from next() and poll() instead of
-//     waiting forever.
+//     waiting forever;
+//   * the packets are read at open, so a container whose index holds an
+//     entry NextPacket cannot read (an offset that wraps validateEntry's sum
+//     to a negative position, ebiv/reader.go:115-123,203-205) is refused
+//     there with kErrIO; the reference plays up to that frame.
 #include <cuda_runtime.h>
 
 #include <condition_variable>

@@ -65,6 +65,10 @@ class EOF(EbivError):
     status = 9
 
 
+class ErrIO(EbivError):
+    status = 10
+
+
 class ErrDevice(EbivError):
     status = 11
 
@@ -73,8 +77,13 @@ class ErrArgument(EbivError):
     status = 12
 
 
+class ErrTooLarge(EbivError):
+    status = 13
+
+
 _ERRORS = {c.status: c for c in (ErrCorrupt, ErrNoKeyframe, ErrDimensions, ErrUnsupported, ErrVersion,
-                                  ErrBadMagic, ErrConfig, ErrWriterClosed, EOF, ErrDevice, ErrArgument)}
+                                  ErrBadMagic, ErrConfig, ErrWriterClosed, EOF, ErrIO, ErrDevice, ErrArgument,
+                                  ErrTooLarge)}
 
 
 def _check(status: int, what: str = "") -> None:

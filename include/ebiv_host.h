@@ -77,10 +77,18 @@ int ebiv_reader_open(const uint8_t* data, size_t n, ebiv_reader** out);
 int ebiv_reader_info(ebiv_reader* r, int64_t* info8);
 /* NextPacket: *data stays valid until the reader is destroyed. */
 int ebiv_reader_next_packet(ebiv_reader* r, const uint8_t** data, size_t* n, int64_t* ts_ns, int* keyframe);
+/* ebiv_reader_next_packet and ebiv_reader_packet return EBIV_ERR_IO for an
+ * index entry whose payload position, int64(Offset) + 8, is negative (an
+ * offset near 2^64 passes validateEntry's wrapping sum, ebiv/reader.go:115-123;
+ * the reference's seek then fails, reader.go:203-205); next_packet stays on
+ * that entry. */
 int ebiv_reader_packet(ebiv_reader* r, int index, const uint8_t** data, size_t* n, int* keyframe);
 int ebiv_reader_seek(ebiv_reader* r, int64_t t_ns, int64_t* landed_ns);
 int64_t ebiv_reader_duration(ebiv_reader* r);
 int64_t ebiv_reader_frame_time(ebiv_reader* r, int64_t i);
+/* frameIndexAt (ebiv/format.go:263-275); -1 for a frame rate so hostile that
+ * its correction walk does not settle within 2^20 steps, where
+ * ebiv_reader_seek returns EBIV_ERR_CORRUPT. */
 int64_t ebiv_reader_frame_index_at(ebiv_reader* r, int64_t t_ns);
 int ebiv_reader_close(ebiv_reader* r);
 void ebiv_reader_destroy(ebiv_reader* r);

@@ -292,14 +292,18 @@ int ebivgpu_decode_key_noalloc(const uint8_t* pkt, size_t n, uint8_t* y, int32_t
  * a scan of the frame records when the footer does not validate (statuses as
  * NewDemuxer's).  info6: width, height, fps_num, fps_den, frames, index
  * rebuilt by scanning (0/1).  ebivgpu_container_entry: frame i's payload
- * offset in the container, payload size, key flag.  ebivgpu_container_seek
+ * offset in the container, payload size, key flag; EBIV_ERR_IO for an index
+ * entry whose payload lies outside the container (an offset near 2^64 passes
+ * validateEntry's wrapping sum, ebiv/reader.go:115-123, and the reference's
+ * NextPacket then fails, reader.go:203-205).  ebivgpu_container_seek
  * resolves Seek(t) on the GPU: the last key frame at or before the frame
  * shown at t (frameIndexAt, ebiv/format.go:263-275) and its time; a frame
  * rate so hostile that frameIndexAt's correction walk does not settle within
  * 2^20 steps returns EBIV_ERR_CORRUPT.  ebivgpu_batch_add_container adds a
  * resident batch stream that decodes straight from the pinned bytes: no
  * packet is copied into HBM, the kernels read them over the host link; the
- * container must outlive the stream. */
+ * container must outlive the stream, and one with an unreadable entry is
+ * refused (EBIV_ERR_IO). */
 typedef struct ebivgpu_container ebivgpu_container;
 int ebivgpu_container_open(const uint8_t* data, size_t n, ebivgpu_container** out);
 void ebivgpu_container_close(ebivgpu_container* c);

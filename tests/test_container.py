@@ -76,6 +76,83 @@ def test_ntsc_frame_times_are_exact():
             assert r.frame_index_at(t - 1) == i - 1
 
 
+def _hostile_rate(data: bytes) -> bytes:
+    """The container with 2^32-1 frames per second (FileHeader FPSNum/FPSDen,
+    ebiv/format.go:230-265); the index's CRC does not cover the header."""
+    b = bytearray(data)
+    b[16:20] = (0xFFFFFFFF).to_bytes(4, "little")
+    b[20:24] = (1).to_bytes(4, "little")
+    return bytes(b)
+
+
+def test_seek_with_a_wrapping_frame_rate_is_an_error_not_a_hang():
+    # frameIndexAt (ebiv/format.go:263-275) estimates from t*FPSNum in
+    # wrapping int64; at 2^32-1 frames per second and t = 2^62 ns the estimate
+    # is meaningless and the reference's correction walk would run for ~2^63
+    # steps. Here the walk stops at 2^20 steps with an error, as on the GPU.
+    r = ebiv.Reader(_hostile_rate(_clip(10, 4)))
+    assert r.frame_index_at(1 << 62) == -1
+    with pytest.raises(ebiv.ErrCorrupt):
+        r.seek(1 << 62)
+    assert r.seek(r.frame_time(9)) == r.frame_time(8)  # ordinary seeks still resolve
+
+
+def with_index(data: bytes, edit) -> bytes:
+    """The container with its footer index entries edited in place by
+    edit([[offset, size, flags], ...]) and the index CRC recomputed
+    (ebiv/reader.go:65-113)."""
+    import struct
+    import zlib
+
+    b = bytearray(data)
+    off, count, _ = struct.unpack_from("<QII", b, len(b) - 20)
+    ents = [list(struct.unpack_from("<QII", b, off + 16 * i)) for i in range(count)]
+    edit(ents)
+    raw = b"".join(struct.pack("<QII", *e) for e in ents)
+    b[off:off + 16 * count] = raw
+    struct.pack_into("<I", b, len(b) - 8, zlib.crc32(raw) & 0xFFFFFFFF)
+    return bytes(b)
+
+
+def wrapping_entries(data: bytes) -> bytes:
+    """Frame 2's offset wraps validateEntry's uint64 sum to position 0, frame
+    5's to a negative position."""
+    def edit(e):
+        e[2][:2] = [2**64 - 8, 40]
+        e[5][:2] = [2**64 - 16, 40]
+    return with_index(data, edit)
+
+
+def test_index_entries_whose_offset_wraps():
+    # validateEntry (ebiv/reader.go:115-123) sums in uint64, so an offset near
+    # 2^64 passes and the reference keeps the index. NextPacket then seeks to
+    # int64(Offset)+8 (reader.go:203): position 0 for 2^64-8, so it returns
+    # the file's first bytes; a negative position for 2^64-16, so it fails
+    # and stays on that frame until a seek.
+    import ebiv_container
+
+    bad = wrapping_entries(_clip(10, 4))
+    r = ebiv.Reader(bad)
+    assert not r.rebuilt_index and r.frame_count == 10
+    assert r.packet(2).data == bad[:40]
+    with pytest.raises(ebiv.ErrIO):
+        r.packet(5)
+    got = []
+    with pytest.raises(ebiv.ErrIO):
+        while True:
+            got.append(r.next_packet().data)
+    assert len(got) == 5 and got[2] == bad[:40]
+    with pytest.raises(ebiv.ErrIO):
+        r.next_packet()
+    r.seek(r.frame_time(8))
+    assert r.next_packet().keyframe
+    _, entries, rebuilt = ebiv_container.demux(bad)
+    assert not rebuilt and entries[2][0] == 0 and entries[5][0] is None
+    with pytest.raises(ebiv_container.ContainerError) as e:
+        ebiv_container.packets(bad)
+    assert e.value.status == ebiv.ErrIO.status
+
+
 @pytest.mark.parametrize("bad,err", [(b"", ebiv.ErrBadMagic), (b"XXXX" + bytes(60), ebiv.ErrBadMagic)])
 def test_bad_files(bad, err):
     with pytest.raises(err):

@@ -51,6 +51,51 @@ def test_device_index_and_seek_match_the_host_demuxer(gpu_required, name):
             assert frame == r.frame_index_at(landed)
 
 
+def test_device_seek_with_a_wrapping_frame_rate_is_an_error(gpu_required):
+    # The device seek caps frameIndexAt's correction walk exactly as the host
+    # demuxer does: the same hostile frame rate is an error on both, and
+    # ordinary seeks on that file land on the same frame.
+    from test_container import _clip, _hostile_rate
+
+    data = _hostile_rate(_clip(10, 4))
+    r = ebiv.Reader(data)
+    dc = ebiv.DeviceContainer(data)
+    with pytest.raises(ebiv.ErrCorrupt):
+        dc.seek(1 << 62)
+    with pytest.raises(ebiv.ErrCorrupt):
+        r.seek(1 << 62)
+    for t in [-1, 0, 1, 2, 3, 10**9]:
+        landed = r.seek(t)
+        frame, dl = dc.seek(t)
+        assert dl == landed, f"t={t}"
+
+
+def test_device_index_keeps_wrapping_entries_and_never_reads_outside(gpu_required):
+    # The device-built index keeps the entries whose offsets wrap
+    # validateEntry's uint64 sum, as the reference and the host demuxer do
+    # (ebiv/reader.go:115-123): the one that lands at position 0 reads the
+    # file's first bytes, the one that lands at a negative position is an I/O
+    # error, and an in-place stream over the file is refused before any
+    # packet is read.
+    from test_container import _clip, wrapping_entries
+
+    bad = wrapping_entries(_clip(10, 4))
+    r = ebiv.Reader(bad)
+    dc = ebiv.DeviceContainer(bad)
+    assert dc.frame_count == r.frame_count == 10 and not dc.rebuilt_index
+    off, n, key = dc.entry(2)
+    assert (off, n) == (0, 40) and bad[off:off + n] == r.packet(2).data
+    with pytest.raises(ebiv.ErrIO):
+        dc.entry(5)
+    for i in (0, 1, 3, 4, 6, 7, 8, 9):
+        off, n, key = dc.entry(i)
+        assert bad[off:off + n] == r.packet(i).data and key == r.packet(i).keyframe
+    b = ebiv.Batch(lookahead=2)
+    with pytest.raises(ebiv.ErrIO):
+        b.add_container(dc)
+    b.close()
+
+
 def test_batch_decodes_in_place_from_the_container(gpu_required):
     clip = workloads.single_640()
     data = workloads.load([clip], in_child=False)[0]
