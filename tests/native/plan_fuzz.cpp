@@ -37,12 +37,6 @@
 #include "container.h"
 #include "payload.h"
 
-namespace ebiv {
-// The container reader's index check takes its CRC-32 from the encoder's
-// sources; the harness reads packets only, so the reader is never called.
-uint32_t crc32IEEE(const uint8_t*, size_t) { std::abort(); }
-}  // namespace ebiv
-
 using namespace ebiv;
 
 namespace {
