@@ -26,6 +26,21 @@ def _status(codec, pkt):
         return e.status
 
 
+@pytest.mark.parametrize("w,h,cw,ch,ys,cs", [(64, 48, 32, 24, 64, 64), (1920, 1080, 960, 540, 1920, 960),
+                                             (65, 49, 33, 25, 128, 64), (1, 1, 1, 1, 64, 64)])
+def test_frame_geometry_matches_the_reference_table(gpu_required, w, h, cw, ch, ys, cs):
+    # TestGeometry (ebiv/format_test.go:188-219): the chroma sizes and the
+    # 64-byte-aligned strides of the frames the Codec returns, and a raw key
+    # frame's bytes round-trip.
+    rng = np.random.default_rng(7 * w + h)
+    body = rng.integers(0, 256, w * h + 2 * cw * ch, dtype=np.uint8).tobytes()
+    assert len(body) == ebiv.packed_size(w, h)
+    f = ebiv.Codec().decode(_raw_key(w, h)[:6] + body)
+    assert (f.width, f.height) == (w, h)
+    assert f.y.shape == (h, ys) and f.cb.shape == (ch, cs) and f.cr.shape == (ch, cs)
+    assert f.packed() == body
+
+
 def test_bad_packets(gpu_required):
     assert _status(ebiv.Codec(), b"") == ebiv.ErrCorrupt.status
     assert _status(ebiv.Codec(), bytes([1])) == ebiv.ErrNoKeyframe.status
