@@ -103,15 +103,16 @@ class Source {
     rgba_ = (flags & EBIVGPU_SOURCE_RGBA) != 0;
     if (int st = reader_.open(data, n)) return st;
     if (reader_.frameCount() == 0) return kErrEOF;
+    // Every container error is reported before the GPU is touched.
+    std::vector<const uint8_t*> pk((size_t)reader_.frameCount());
+    std::vector<size_t> len(pk.size());
+    for (int i = 0; i < reader_.frameCount(); i++)
+      if (int st = reader_.packet(i, &pk[(size_t)i], &len[(size_t)i])) return st;
     if (cudaGetDevice(&device_) != cudaSuccess) return kErrDevice;
     lookahead_ = depth < kMaxLookahead ? depth : kMaxLookahead;
     if (int st = engine_.init()) return st;
     engineReady_ = true;
     if (engine_.setLookahead(lookahead_) || engine_.setPipelined(kPipeline)) return kErrArg;
-    std::vector<const uint8_t*> pk((size_t)reader_.frameCount());
-    std::vector<size_t> len(pk.size());
-    for (int i = 0; i < reader_.frameCount(); i++)
-      if (int st = reader_.packet(i, &pk[(size_t)i], &len[(size_t)i])) return st;
     if (int st = engine_.addResidentStream(pk.data(), len.data(), (int)pk.size(), 3, &sid_)) return st;
     slots_.resize((size_t)(depth_ + 2 * lookahead_ + kConsumerFrames));
     for (size_t i = 0; i < slots_.size(); i++) freeList_.push_back((int)i);

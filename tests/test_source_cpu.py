@@ -1,7 +1,8 @@
 """Argument and container errors of the decode-ahead source, which it
 reports before touching a GPU (so they run on CPU): govid's
 TestAsyncPlayerEmptyStream (async_test.go) — an empty stream is io.EOF at
-creation — and NewDemuxer's container errors."""
+creation — NewDemuxer's container errors, and a container whose index holds
+an entry NextPacket cannot read (the source reads every packet at creation)."""
 import ctypes as C
 
 import pytest
@@ -33,3 +34,10 @@ def test_container_errors_and_bad_arguments():
     assert L.ebivgpu_source_seek(None, 0, None) == ebiv.ErrArgument.status
     L.ebivgpu_source_release(None, 0)
     L.ebivgpu_source_destroy(None)
+
+
+def test_unreadable_index_entry_is_refused_at_creation():
+    from test_container import _clip, wrapping_entries
+
+    with pytest.raises(ebiv.ErrIO):
+        ebiv.AsyncSource(wrapping_entries(_clip(10, 4)), depth=4)
