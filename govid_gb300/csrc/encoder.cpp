@@ -429,7 +429,9 @@ void putClassValue(TokStream& s, int classCtx, uint64_t v) {
   s.put(classCtx, cls);
   if (cls > 1) putRawBits(s, v - (1ull << (cls - 1)), cls - 1);
 }
-inline uint64_t zigzagEncode(int64_t v) { return (uint64_t)((v << 1) ^ (v >> 31)); }
+// The left shift is taken on the unsigned value: shifting a negative signed
+// value left is undefined before C++20; the bits are the same.
+inline uint64_t zigzagEncode(int64_t v) { return ((uint64_t)v << 1) ^ (uint64_t)(v >> 31); }
 void putMVComponent(TokStream& s, int classCtx, int delta) { putClassValue(s, classCtx, zigzagEncode(delta)); }
 
 // encodeBlock — ebiv/residual.go:30-75
