@@ -25,6 +25,9 @@
 //   * a consumer holding so many frames that none can be decoded (more than
 //     depth + lookahead + 4) gets kErrArg from next() and poll() instead of
 //     waiting forever;
+//   * a seek the demuxer refuses (a frame rate whose frameIndexAt walk does
+//     not settle) changes nothing; the reference has already started a new
+//     generation then, dropping the queued frames;
 //   * the packets are read at open, so a container whose index holds an
 //     entry NextPacket cannot read (an offset that wraps validateEntry's sum
 //     to a negative position, ebiv/reader.go:115-123,203-205) is refused
@@ -171,9 +174,9 @@ class Source {
   // dropped, a parked worker woken.
   int seek(int64_t t, int64_t* landed) {
     std::lock_guard<std::mutex> lk(mu_);
-    gen_++;
     int64_t at = 0;
-    if (int st = reader_.seek(t, &at)) return st;
+    if (int st = reader_.seek(t, &at)) return st;  // a refused seek changes nothing
+    gen_++;
     target_ = reader_.position();
     parked_ = false;
     terminalTaken_ = false;
