@@ -125,12 +125,12 @@ int planPayload(const uint8_t* base, size_t bodyOffset, size_t len, bool key, in
   // decodeCoded's grid check — ebiv/decode_intra.go:60-63
   const TileGrid grid(mbCols, mbRows, (int)cols, (int)rows);
   if ((uint64_t)grid.count() != plan->tiles.size()) return kErrCorrupt;
-  uint32_t base = 0;
+  uint32_t mbBase = 0;
   for (int i = 0; i < grid.count(); i++) {
     int x0, x1, y0, y1;
     grid.bounds(i, &x0, &x1, &y0, &y1);
-    plan->tiles[(size_t)i].mbBase = base;
-    base += (uint32_t)((x1 - x0) * (y1 - y0));
+    plan->tiles[(size_t)i].mbBase = mbBase;
+    mbBase += (uint32_t)((x1 - x0) * (y1 - y0));
     plan->tiles[(size_t)i].mbX0 = (uint16_t)x0;
     plan->tiles[(size_t)i].mbX1 = (uint16_t)x1;
     plan->tiles[(size_t)i].mbY0 = (uint16_t)y0;

@@ -680,7 +680,6 @@ class Server {
           break;
         }
       }
-      bool collected = false;
       for (int l = 0; l < Engine::kSideLanes; l++) {
         if (!L.eng.sideReady(l)) continue;
         res.clear();
@@ -693,9 +692,7 @@ class Server {
         for (const auto& pl : L.sidePlanned[l]) specs_[(size_t)pl.first]->inSide = false;
         L.sidePlanned[l].clear();
         cvRequest_.notify_all();
-        collected = true;
       }
-      (void)collected;
     }
     if (L.eng.mainBusy()) {
       res.clear();
