@@ -142,10 +142,12 @@ def _index_at(b: bytes):
 def _mutate_container(data: bytes, rng) -> bytes:
     b = bytearray(data)
     kind = int(rng.integers(0, 7))
+    if not b:  # an earlier truncation left nothing to change
+        return bytes(b)
     if kind == 0:  # a file header byte
-        b[int(rng.integers(0, 48))] = int(rng.integers(0, 256))
+        b[int(rng.integers(0, min(48, len(b))))] = int(rng.integers(0, 256))
     elif kind == 1:  # a footer byte
-        b[len(b) - 1 - int(rng.integers(0, 20))] ^= 1 << int(rng.integers(0, 8))
+        b[len(b) - 1 - int(rng.integers(0, min(20, len(b))))] ^= 1 << int(rng.integers(0, 8))
     elif kind == 2:  # any byte (frame records included)
         i = int(rng.integers(0, len(b)))
         b[i] = int(rng.integers(0, 256))
